@@ -1,0 +1,311 @@
+/*
+ * rt_gb300.h — C ABI of the GB300 renderer for the RayTracer per-pixel loop.
+ *
+ * This is the drop-in boundary. The C++ classes Scene / RayTracer / Sphere / Plane /
+ * Box / BallPlane / Model (raytrace_gb300/cpp/) flatten a scene into an rt_scene_desc and
+ * call these functions; so can any C, ctypes or FFI caller. All calls return RT_OK (0) or a
+ * negative RT_ERR_* code and never throw. rt_last_error() gives a message for the last
+ * failing call on a context.
+ *
+ * Reference interfaces replaced (paths within the XZiar/RayTrace project):
+ *   - RayTracer::start / stop / isFinish / useTime / output   RayTracer.h:44-56, RayTracer.cpp:614-701
+ *   - DrawObject::RTPrepare (Model octant lists)              3DElement.h:200, Model.cpp:402-480
+ *   - the per-pixel loop parallelRT + RTfrac recursion        RayTracer.cpp:5-45, 450-596
+ *   - Sphere / Plane / Box / BallPlane / Model ::intersect    Basic3DObject.cpp:135-551, Model.cpp:748-811
+ * Units and conventions follow the reference: the camera looks along n with u to the right
+ * and v up, pixel (col,row) maps to xcur = col - W/2, ycur = row - H/2, and output row 0 is
+ * the bottom row (RayTracer.cpp:20-27).
+ */
+#ifndef RT_GB300_H
+#define RT_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RT_ABI_VERSION 1
+
+/* ---- status codes ---------------------------------------------------------------- */
+#define RT_OK               0
+#define RT_ERR_INVALID     -1   /* bad argument, size or id                        */
+#define RT_ERR_CUDA        -2   /* CUDA runtime error or no usable GPU             */
+#define RT_ERR_OOM         -3   /* device allocation failed                        */
+#define RT_ERR_CANCELLED   -4   /* rt_cancel() ended the render                    */
+#define RT_ERR_OVERFLOW    -5   /* a ray queue overflowed (render is retried)      */
+#define RT_ERR_TIMEOUT     -6   /* a bounded device wait gave up                   */
+#define RT_ERR_BUDGET      -7   /* the serving HBM budget cannot admit the request */
+#define RT_ERR_NOT_FOUND   -8   /* unknown scene / frame / request id              */
+#define RT_ERR_BUSY        -9   /* the object is in use by an unfinished render    */
+
+/* ---- scene vocabulary (values match the reference's macros) --------------------- */
+#define RT_OBJECT_SPHERE     0x1   /* MY_OBJECT_SPHERE     3DElement.h:4  */
+#define RT_OBJECT_CUBE       0x2   /* MY_OBJECT_CUBE       3DElement.h:5  */
+#define RT_OBJECT_MODEL      0x3   /* MY_OBJECT_MODEL      3DElement.h:6  */
+#define RT_OBJECT_PLANE      0x4   /* MY_OBJECT_PLANE      3DElement.h:7  */
+#define RT_OBJECT_BALLPLANE  0x5   /* MY_OBJECT_BALLPLANE  3DElement.h:8  */
+
+#define RT_LIGHT_PARALLEL    0x1   /* MY_LIGHT_PARALLEL    3DElement.h:13 */
+#define RT_LIGHT_POINT       0x2   /* MY_LIGHT_POINT       3DElement.h:14 */
+#define RT_LIGHT_SPOT        0x3   /* MY_LIGHT_SPOT (shaded as parallel, RayTracer.cpp:482-503) */
+
+/* render modes = the reference's start() types (RayTracer.h:5-13) */
+#define RT_MODE_CHECK        0x1
+#define RT_MODE_DEPTH        0x2
+#define RT_MODE_NORMAL       0x3
+#define RT_MODE_TEXTURE      0x4
+#define RT_MODE_MATERIAL     0x5
+#define RT_MODE_SHADOW       0x6
+#define RT_MODE_REFLECT      0x7
+#define RT_MODE_REFRACT      0x8
+#define RT_MODE_RAYTRACE     0x80
+
+/* render flags */
+#define RT_FLAG_REF_TILES    0x1   /* render only the 64x64-tile region the reference covers
+                                      (W and H floored to multiples of 64, RayTracer.cpp:13) */
+#define RT_FLAG_HIT_PLANES   0x2   /* also write per-pixel primary hit id / distance planes   */
+#define RT_FLAG_COUNT_WORK   0x4   /* count BVH nodes visited and primitives tested (slower)  */
+
+typedef struct rt_camera {
+    float position[3];
+    float u[3], v[3], n[3];      /* right, up, toward (Camera, 3DElement.h:225-237) */
+    int32_t width, height;
+    float fovy;                  /* degrees */
+    float znear, zfar;
+} rt_camera;
+
+typedef struct rt_light {
+    int32_t type;                /* RT_LIGHT_* */
+    int32_t on;                  /* Light::bLight */
+    float position[3];
+    float ambient[3], diffuse[3], specular[3];
+    float attenuation[3];        /* constant, linear, quadratic */
+} rt_light;
+
+typedef struct rt_material {
+    float ambient[3], diffuse[3], specular[3];
+    float shininess, reflect, refract, rfr;
+    int32_t texture;             /* index into rt_scene_desc.textures, -1 = none */
+} rt_material;
+
+typedef struct rt_texture {
+    int32_t w, h;
+    const uint8_t *bgr;          /* w*h*3 bytes, B,G,R per texel, row y at offset (y*w+x)*3 */
+} rt_texture;
+
+typedef struct rt_object {
+    int32_t type;                /* RT_OBJECT_* */
+    int32_t show;                /* DrawObject::bShow; hidden objects are skipped */
+    int32_t material;            /* sphere/cube/plane/ballplane material index */
+    int32_t texture;             /* plane texture index, -1 = none */
+    float position[3];
+    float radius;                /* sphere, ballplane */
+    float normal[3];             /* plane, ballplane frame (Plane::rotate, Basic3DObject.cpp:312-330) */
+    float axisx[3], axisy[3];
+    float bmin[3], bmax[3];      /* cube: min/max relative to position; model: VerMin/VerMax */
+    int64_t tri_first;           /* model: first triangle in the scene triangle arrays */
+    int64_t tri_count;           /* model: number of triangles */
+} rt_object;
+
+/*
+ * A scene in flat form. Triangles of every Model are concatenated; triangle i has its three
+ * points at tri_p[9i..9i+8] (model space, before the object's position is added), vertex
+ * normals at tri_n[9i..], texture coordinates at tri_uv[6i..] (NULL = all zero) and material
+ * tri_mtl[i] (the part material). tri_id[i] is the primitive id reported for that triangle
+ * (NULL = its index within its model).
+ */
+typedef struct rt_scene_desc {
+    rt_camera camera;
+    float env_light[3];                  /* Scene::EnvLight */
+    int32_t n_lights;   const rt_light    *lights;
+    int32_t n_materials; const rt_material *materials;
+    int32_t n_textures; const rt_texture  *textures;
+    int32_t n_objects;  const rt_object   *objects;
+    int64_t n_tris;
+    const float   *tri_p;
+    const float   *tri_n;
+    const float   *tri_uv;
+    const int32_t *tri_mtl;
+    const int32_t *tri_id;
+} rt_scene_desc;
+
+typedef struct rt_render_desc {
+    int32_t width, height;       /* 0 = the scene camera's */
+    int32_t spp;                 /* samples per pixel (>1 = Philox-jittered sub-pixel offsets) */
+    int32_t max_level;           /* RayTracer::maxLevel: levels 0..max_level are traced */
+    int32_t mode;                /* RT_MODE_* */
+    int32_t flags;               /* RT_FLAG_* */
+    uint64_t seed;               /* jitter seed */
+    const rt_camera *camera;     /* NULL = the scene camera */
+} rt_render_desc;
+
+typedef struct rt_render_stats {
+    int64_t rays_primary;        /* W*H*spp rays generated */
+    int64_t rays_secondary;      /* reflect + refract rays traced */
+    int64_t rays_shadow;         /* shadow rays traced */
+    int64_t nodes_visited;       /* with RT_FLAG_COUNT_WORK */
+    int64_t tris_tested;         /* with RT_FLAG_COUNT_WORK */
+    int64_t spheres_tested;      /* with RT_FLAG_COUNT_WORK */
+    float   ms;                  /* device time of the last render (CUDA events) */
+    int32_t overflow_retries;
+} rt_render_stats;
+
+typedef struct rt_ctx rt_ctx;
+
+/* ---- context ------------------------------------------------------------------------ */
+int         rt_version(void);
+int         rt_ctx_create(int device, rt_ctx **out);
+void        rt_ctx_destroy(rt_ctx *ctx);
+const char *rt_last_error(const rt_ctx *ctx);
+int         rt_ctx_synchronize(rt_ctx *ctx);
+/* stream used by every call of this context (NULL = the context's own stream) */
+int         rt_ctx_set_stream(rt_ctx *ctx, void *cuda_stream);
+
+/* ---- scenes: upload + device LBVH build (replaces RTPrepare, Model.cpp:402-480) ------ */
+int rt_scene_upload(rt_ctx *ctx, const rt_scene_desc *desc, int32_t *scene_id);
+int rt_scene_update_camera(rt_ctx *ctx, int32_t scene_id, const rt_camera *cam);
+int rt_scene_rebuild(rt_ctx *ctx, int32_t scene_id);      /* re-run the LBVH build */
+int rt_scene_release(rt_ctx *ctx, int32_t scene_id);
+int rt_scene_device_bytes(rt_ctx *ctx, int32_t scene_id, int64_t *bytes);
+/* last LBVH build time in ms (device time, CUDA events) */
+int rt_scene_build_ms(rt_ctx *ctx, int32_t scene_id, float *ms);
+
+/* ---- frames (device framebuffers) ------------------------------------------------------ */
+int rt_frame_create(rt_ctx *ctx, int32_t width, int32_t height, int32_t *frame_id);
+int rt_frame_release(rt_ctx *ctx, int32_t frame_id);
+/*
+ * Copy a finished frame to host buffers (any may be NULL):
+ *   rgb      float[H*W*3]  colour before clamping (Color before put, 3DElement.cpp:463-468)
+ *   rgb8     uint8[H*W*3]  Color::put of rgb
+ *   hit_obj  int32[H*W]    primary hit object index (-1 = miss), sample 0
+ *   hit_prim int32[H*W]    primary hit primitive id (triangle id, ballplane sphere 1..16, else 0)
+ *   hit_t    float[H*W]    primary hit distance (1e20 = miss)
+ * Rows are bottom-up, row stride W. The call waits for the frame's render.
+ */
+int rt_frame_download(rt_ctx *ctx, int32_t frame_id, float *rgb, uint8_t *rgb8,
+                      int32_t *hit_obj, int32_t *hit_prim, float *hit_t);
+/* device pointers of a frame (rgb float, rgb8) for zero-copy consumers */
+int rt_frame_device_ptrs(rt_ctx *ctx, int32_t frame_id, void **rgb, void **rgb8);
+
+/* ---- one render (the plain per-scene path) ----------------------------------------------- */
+/* enqueue on the context stream; returns immediately */
+int rt_render(rt_ctx *ctx, int32_t scene_id, int32_t frame_id, const rt_render_desc *rd);
+/* wait for the last render of the context; fills stats if not NULL */
+int rt_render_wait(rt_ctx *ctx, rt_render_stats *stats);
+/* cooperative cancel of the running render (RayTracer::stop, RayTracer.cpp:698-701) */
+int rt_cancel(rt_ctx *ctx);
+/* 1 if the last render finished, 0 if still running (RayTracer::isFinish) */
+int rt_poll(rt_ctx *ctx);
+
+/*
+ * End-to-end drop-in for RayTracer::start + wait: upload the host scene, build the LBVH,
+ * render, and write the reference's uint8 output (bottom-up rows of stride 3*W over the
+ * 64x64 tiles when RT_FLAG_REF_TILES is set) plus optional float rgb, all from host memory.
+ */
+int rt_render_host(rt_ctx *ctx, const rt_scene_desc *desc, const rt_render_desc *rd,
+                   uint8_t *out_rgb8, float *out_rgb, rt_render_stats *stats);
+
+/* ---- batched multi-scene rendering (persistent wavefront kernel + CUDA graph) ------------ */
+typedef struct rt_batch_tuning {
+    int32_t block;               /* threads per block of the traversal kernels (0 = autotune) */
+    int32_t tile;                /* rays taken per work-counter fetch (0 = autotune) */
+    int32_t stack;               /* traversal stack depth (0 = autotune) */
+    int32_t use_graph;           /* capture the per-bounce launch sequence as a CUDA graph */
+} rt_batch_tuning;
+
+/* render n (scene, frame, desc) jobs as one wavefront; returns after enqueueing */
+int rt_batch_render(rt_ctx *ctx, int32_t n, const int32_t *scene_ids, const int32_t *frame_ids,
+                    const rt_render_desc *rds, const rt_batch_tuning *tuning);
+/* the same jobs through a loop of plain per-scene renders (the comparison path) */
+int rt_batch_render_plain(rt_ctx *ctx, int32_t n, const int32_t *scene_ids,
+                          const int32_t *frame_ids, const rt_render_desc *rds);
+/* pick block / tile / stack for these jobs by timing candidates; writes the choice */
+int rt_batch_autotune(rt_ctx *ctx, int32_t n, const int32_t *scene_ids, const int32_t *frame_ids,
+                      const rt_render_desc *rds, rt_batch_tuning *out);
+
+/* ---- serving: continuous batching over resident scenes ---------------------------------- */
+typedef struct rt_server rt_server;
+
+typedef struct rt_server_config {
+    int64_t hbm_budget_bytes;    /* admission budget for scenes + frames + queues */
+    int32_t max_inflight;        /* frame slots admitted at once */
+    int32_t max_level;
+    int32_t spp;
+    int64_t queue_rays;          /* capacity of the shared wavefront queue (0 = default) */
+} rt_server_config;
+
+typedef struct rt_request {
+    int32_t scene;               /* server scene id */
+    int32_t width, height;
+    rt_camera camera;
+    double arrival_s;            /* arrival time on the server clock */
+} rt_request;
+
+typedef struct rt_request_result {
+    int64_t request;
+    int32_t status;              /* RT_OK or RT_ERR_* */
+    int32_t width, height;
+    double arrival_s, admit_s, done_s;
+    int64_t rays;                /* ray segments traced for this frame */
+} rt_request_result;
+
+typedef struct rt_serve_stats {
+    int64_t requests, completed, rejected, evictions, rebuilds;
+    double p50_ms, p99_ms, mean_ms, max_ms;
+    double mrays_per_s;          /* all ray segments / wall time */
+    double wall_s;
+    int64_t rays;
+    int64_t peak_bytes;
+} rt_serve_stats;
+
+int    rt_server_create(rt_ctx *ctx, const rt_server_config *cfg, rt_server **out);
+void   rt_server_destroy(rt_server *srv);
+/* register a scene; the host copy is kept so an evicted scene can be rebuilt on a miss */
+int    rt_server_add_scene(rt_server *srv, const rt_scene_desc *desc, int32_t *scene);
+int    rt_server_submit(rt_server *srv, const rt_request *req, int64_t *request_id);
+/* one continuous-batching step: admit, trace one bounce of every in-flight frame, retire */
+int    rt_server_step(rt_server *srv, int32_t *n_inflight);
+/* drain: step until nothing is queued or in flight */
+int    rt_server_drain(rt_server *srv);
+/* result + image of a finished request (rgb may be NULL); RT_ERR_NOT_FOUND if not done */
+int    rt_server_result(rt_server *srv, int64_t request_id, rt_request_result *res, float *rgb);
+int    rt_server_resident(rt_server *srv, int32_t scene, int32_t *resident);
+double rt_server_now(rt_server *srv);
+/* run a Poisson arrival stream of requests over the registered scenes in real time */
+int    rt_server_run_poisson(rt_server *srv, double lambda_per_s, double duration_s, uint64_t seed,
+                             rt_serve_stats *stats);
+
+/* ---- LBVH pieces exposed for tests ------------------------------------------------------ */
+/* 30-bit Morton codes of triangle centroids over the AABB of the centroids, radix-sorted
+   (stable): codes[i] and perm[i] are the i-th smallest code and its triangle index */
+int rt_morton_sort(rt_ctx *ctx, const float *tri_p, int64_t n_tris, uint32_t *codes, uint32_t *perm);
+/* download the LBVH of a scene: nodes float[(2n-1)*8] (min xyz, left | max xyz, right) and
+   the sorted triangle order perm[n] */
+int rt_scene_bvh_download(rt_ctx *ctx, int32_t scene_id, float *nodes, uint32_t *perm,
+                          int64_t *n_nodes);
+
+/* ---- seeded synthetic scenes (the benchmark workloads) ---------------------------------- */
+typedef struct rt_scene_host rt_scene_host;
+/* config 0..4 as in the benchmark definition, index = scene number inside configs 3/4 */
+int  rt_scenegen(int32_t config, int32_t index, rt_scene_host **out);
+/* a small scene for tests: plane + n spheres (+ an icosphere of the given frequency, 0 = none) */
+int  rt_scenegen_small(uint64_t seed, int32_t n_spheres, int32_t ico_freq, int32_t width,
+                       int32_t height, int32_t refractive_every, rt_scene_host **out);
+/* every object kind in one scene: plane, ballplane, cubes, spheres, a mesh, parallel + point light */
+int  rt_scenegen_extras(uint64_t seed, int32_t width, int32_t height, rt_scene_host **out);
+/* deep copy of a caller-built description (render parameters attached) */
+int  rt_scene_host_from_desc(const rt_scene_desc *desc, int32_t spp, int32_t max_level, uint64_t seed,
+                             rt_scene_host **out);
+const rt_scene_desc *rt_scene_host_desc(const rt_scene_host *s);
+int  rt_scene_host_render_params(const rt_scene_host *s, int32_t *spp, int32_t *max_level,
+                                 uint64_t *seed);
+int  rt_scene_host_save(const rt_scene_host *s, const char *path);
+int  rt_scene_host_load(const char *path, rt_scene_host **out);
+void rt_scene_host_free(rt_scene_host *s);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,813 @@
+// rt_capi.cu — the C ABI (include/rt_gb300.h): contexts, scene upload + LBVH build, frames,
+// the plain per-scene render path, the batched multi-scene path and the test hooks.
+//
+// Scene flattening into device tables replaces the per-pixel virtual calls over
+// Scene::Objects (RayTracer.cpp:458-465); the LBVH replaces Model::RTPrepare
+// (Model.cpp:402-480); one render = the parallelRT tile loop (RayTracer.cpp:5-45) over every
+// pixel, as a wavefront of raygen -> (extend -> shade -> shadow) x (maxLevel+1) -> resolve.
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/rt_gb300.h"
+#include "rt_capi_internal.h"
+#include "rt_kernels.cuh"
+#include "rt_lbvh.cuh"
+
+using namespace rtg;
+
+// ---- helpers -------------------------------------------------------------------------------------
+int ctx_fail(rt_ctx *ctx, int code, const char *fmt, ...)
+{
+    if (ctx) {
+        char buf[512];
+        va_list ap;
+        va_start(ap, fmt);
+        vsnprintf(buf, sizeof buf, fmt, ap);
+        va_end(ap);
+        ctx->err = buf;
+    }
+    return code;
+}
+
+#define CK(ctx, call)                                                                                             \
+    do {                                                                                                          \
+        cudaError_t e_ = (call);                                                                                  \
+        if (e_ != cudaSuccess)                                                                                    \
+            return ctx_fail(ctx, e_ == cudaErrorMemoryAllocation ? RT_ERR_OOM : RT_ERR_CUDA, "%s: %s (%s:%d)",       \
+                            #call, cudaGetErrorString(e_), __FILE__, __LINE__);                                  \
+    } while (0)
+
+DevBuf::~DevBuf() { release(); }
+void DevBuf::release()
+{
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+}
+cudaError_t DevBuf::ensure(size_t need)
+{
+    if (need <= bytes && p) return cudaSuccess;
+    release();
+    size_t b = std::max<size_t>(need, 256);
+    cudaError_t e = cudaMalloc(&p, b);
+    if (e != cudaSuccess) {
+        p = nullptr;
+        cudaGetLastError();
+        return e;
+    }
+    bytes = b;
+    return cudaSuccess;
+}
+
+static size_t a256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+// ---- version / context -------------------------------------------------------------------------------
+extern "C" int rt_version(void) { return RT_ABI_VERSION; }
+
+extern "C" int rt_ctx_create(int device, rt_ctx **out)
+{
+    if (!out) return RT_ERR_INVALID;
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0) {
+        cudaGetLastError();
+        return RT_ERR_CUDA;
+    }
+    if (device < 0 || device >= ndev) return RT_ERR_INVALID;
+    if (cudaSetDevice(device) != cudaSuccess) return RT_ERR_CUDA;
+    std::unique_ptr<rt_ctx> c(new rt_ctx());
+    c->device = device;
+    if (cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess) return RT_ERR_CUDA;
+    c->stream = c->own_stream;
+    if (cudaEventCreate(&c->ev_start) != cudaSuccess || cudaEventCreate(&c->ev_stop) != cudaSuccess) return RT_ERR_CUDA;
+    if (cudaHostAlloc((void **)&c->cancel_host, sizeof(int), cudaHostAllocMapped) != cudaSuccess) return RT_ERR_CUDA;
+    *c->cancel_host = 0;
+    if (cudaHostGetDevicePointer((void **)&c->cancel_dev, (void *)c->cancel_host, 0) != cudaSuccess) return RT_ERR_CUDA;
+    if (cudaMallocHost((void **)&c->counters_host, sizeof(Counters)) != cudaSuccess) return RT_ERR_CUDA;
+    *out = c.release();
+    return RT_OK;
+}
+
+extern "C" void rt_ctx_destroy(rt_ctx *ctx)
+{
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    ctx->scenes.clear();
+    ctx->frames.clear();
+    ctx->graphs.clear();
+    ctx->ws = Workspace();
+    if (ctx->cancel_host) cudaFreeHost((void *)ctx->cancel_host);
+    if (ctx->counters_host) cudaFreeHost(ctx->counters_host);
+    cudaEventDestroy(ctx->ev_start);
+    cudaEventDestroy(ctx->ev_stop);
+    cudaStreamDestroy(ctx->own_stream);
+    delete ctx;
+}
+
+extern "C" const char *rt_last_error(const rt_ctx *ctx) { return ctx ? ctx->err.c_str() : "no context"; }
+
+extern "C" int rt_ctx_synchronize(rt_ctx *ctx)
+{
+    if (!ctx) return RT_ERR_INVALID;
+    CK(ctx, cudaStreamSynchronize(ctx->stream));
+    return RT_OK;
+}
+
+extern "C" int rt_ctx_set_stream(rt_ctx *ctx, void *stream)
+{
+    if (!ctx) return RT_ERR_INVALID;
+    ctx->stream = stream ? (cudaStream_t)stream : ctx->own_stream;
+    return RT_OK;
+}
+
+// ---- scenes ------------------------------------------------------------------------------------------
+static bool finite3(const float *v) { return std::isfinite(v[0]) && std::isfinite(v[1]) && std::isfinite(v[2]); }
+
+int validate_desc(rt_ctx *ctx, const rt_scene_desc *d)
+{
+    if (!d) return ctx_fail(ctx, RT_ERR_INVALID, "scene desc is NULL");
+    if (d->n_lights < 0 || d->n_lights > 8) return ctx_fail(ctx, RT_ERR_INVALID, "n_lights %d outside [0,8]", d->n_lights);
+    if (d->n_materials < 0 || d->n_objects < 0 || d->n_textures < 0 || d->n_tris < 0)
+        return ctx_fail(ctx, RT_ERR_INVALID, "negative count in scene desc");
+    if ((d->n_lights && !d->lights) || (d->n_materials && !d->materials) || (d->n_objects && !d->objects) ||
+        (d->n_textures && !d->textures))
+        return ctx_fail(ctx, RT_ERR_INVALID, "NULL table with a non-zero count");
+    if (d->n_tris > 0 && (!d->tri_p || !d->tri_n || !d->tri_mtl))
+        return ctx_fail(ctx, RT_ERR_INVALID, "triangles need tri_p, tri_n and tri_mtl");
+    if (d->n_tris >= (int64_t)1 << 30) return ctx_fail(ctx, RT_ERR_INVALID, "too many triangles (%lld)", (long long)d->n_tris);
+    for (int i = 0; i < d->n_textures; ++i)
+        if (d->textures[i].w <= 0 || d->textures[i].h <= 0 || !d->textures[i].bgr)
+            return ctx_fail(ctx, RT_ERR_INVALID, "texture %d is empty", i);
+    for (int i = 0; i < d->n_objects; ++i) {
+        const rt_object &o = d->objects[i];
+        if (o.type < RT_OBJECT_SPHERE || o.type > RT_OBJECT_BALLPLANE)
+            return ctx_fail(ctx, RT_ERR_INVALID, "object %d has unknown type %d", i, o.type);
+        if (o.type != RT_OBJECT_MODEL && (o.material < 0 || o.material >= d->n_materials))
+            return ctx_fail(ctx, RT_ERR_INVALID, "object %d material %d out of range", i, o.material);
+        if (o.type == RT_OBJECT_PLANE && o.texture >= d->n_textures)
+            return ctx_fail(ctx, RT_ERR_INVALID, "object %d texture out of range", i);
+        if (o.type == RT_OBJECT_MODEL &&
+            (o.tri_first < 0 || o.tri_count < 0 || o.tri_first + o.tri_count > d->n_tris))
+            return ctx_fail(ctx, RT_ERR_INVALID, "object %d triangle range out of bounds", i);
+        if (!finite3(o.position)) return ctx_fail(ctx, RT_ERR_INVALID, "object %d position not finite", i);
+    }
+    for (int i = 0; i < d->n_materials; ++i)
+        if (d->materials[i].texture >= d->n_textures)
+            return ctx_fail(ctx, RT_ERR_INVALID, "material %d texture out of range", i);
+    for (int64_t i = 0; i < d->n_tris; ++i)
+        if (d->tri_mtl[i] < 0 || d->tri_mtl[i] >= d->n_materials)
+            return ctx_fail(ctx, RT_ERR_INVALID, "triangle %lld material out of range", (long long)i);
+    return RT_OK;
+}
+
+static void f4(float4 &d, const float *v, float w = 0.0f) { d = make_float4(v[0], v[1], v[2], w); }
+
+// host side of the device tables
+struct HostTables {
+    std::vector<DevPrim> prims;
+    std::vector<DevMaterial> mtl;
+    std::vector<DevLight> lights;
+    std::vector<DevTexture> tex;
+    std::vector<uint8_t> texels;
+    std::vector<float> obj_pos;
+    // shown models' triangles, compacted
+    std::vector<std::pair<int64_t, int64_t>> tri_ranges;   // (first, count) per shown model
+    std::vector<int> tri_range_obj;
+    int64_t n_tris = 0;
+};
+
+static void build_tables(const rt_scene_desc *d, HostTables &h)
+{
+    for (int i = 0; i < d->n_materials; ++i) {
+        const rt_material &m = d->materials[i];
+        DevMaterial dm{};
+        for (int k = 0; k < 3; ++k) dm.ka[k] = m.ambient[k], dm.kd[k] = m.diffuse[k], dm.ks[k] = m.specular[k];
+        dm.shininess = m.shininess, dm.reflect = m.reflect, dm.refract = m.refract, dm.rfr = m.rfr;
+        dm.tex = m.texture;
+        h.mtl.push_back(dm);
+    }
+    if (h.mtl.empty()) h.mtl.push_back(DevMaterial{});
+    for (int i = 0; i < d->n_lights; ++i) {
+        const rt_light &l = d->lights[i];
+        DevLight dl{};
+        dl.type = l.type, dl.on = l.on;
+        for (int k = 0; k < 3; ++k) {
+            dl.pos[k] = l.position[k], dl.amb[k] = l.ambient[k], dl.dif[k] = l.diffuse[k];
+            dl.spec[k] = l.specular[k], dl.att[k] = l.attenuation[k];
+        }
+        h.lights.push_back(dl);
+    }
+    for (int i = 0; i < d->n_textures; ++i) {
+        const rt_texture &t = d->textures[i];
+        DevTexture dt{t.w, t.h, (long long)h.texels.size()};
+        h.texels.insert(h.texels.end(), t.bgr, t.bgr + (size_t)t.w * t.h * 3);
+        h.tex.push_back(dt);
+    }
+    if (h.texels.empty()) h.texels.push_back(0xff);
+    h.obj_pos.assign((size_t)std::max(1, d->n_objects) * 3, 0.0f);
+    for (int k = 0; k < d->n_objects; ++k) {
+        const rt_object &o = d->objects[k];
+        for (int j = 0; j < 3; ++j) h.obj_pos[3 * k + j] = o.position[j];
+        if (!o.show) continue;
+        DevPrim p{};
+        p.obj = k;
+        p.mtl = o.material;
+        p.tex = -1;
+        switch (o.type) {
+        case RT_OBJECT_SPHERE:
+            p.type = kPrimSphere;
+            f4(p.a, o.position, o.radius * o.radius);
+            p.b = make_float4(o.radius, 0, 0, 0);
+            h.prims.push_back(p);
+            break;
+        case RT_OBJECT_PLANE:
+            p.type = kPrimPlane;
+            f4(p.a, o.position);
+            f4(p.b, o.normal);
+            f4(p.c, o.axisx);
+            f4(p.d, o.axisy);
+            p.tex = o.texture;
+            h.prims.push_back(p);
+            break;
+        case RT_OBJECT_CUBE: {   // BorderTest(ray, min + position, max + position)
+            p.type = kPrimBox;
+            float mn[3], mx[3];
+            for (int j = 0; j < 3; ++j) mn[j] = o.bmin[j] + o.position[j], mx[j] = o.bmax[j] + o.position[j];
+            f4(p.a, mn);
+            f4(p.b, mx);
+            f4(p.c, o.position);
+            f4(p.d, o.bmax);
+            h.prims.push_back(p);
+            break;
+        }
+        case RT_OBJECT_BALLPLANE: {   // 4x4 spheres visited cx-major (Basic3DObject.cpp:492-497)
+            const float r = o.radius;
+            int cnt = 0;
+            for (float cx = r * -6; cx < r * 8; cx += r * 4)
+                for (float cy = r * -6; cy < r * 8; cy += r * 4) {
+                    ++cnt;
+                    float c[3];
+                    for (int j = 0; j < 3; ++j) {
+                        float t = o.axisx[j] * cx + o.axisy[j] * cy;
+                        c[j] = t + o.position[j];
+                    }
+                    DevPrim s = p;
+                    s.type = kPrimSphere;
+                    s.sub = cnt;
+                    f4(s.a, c, r * r);
+                    s.b = make_float4(r, 0, 0, 0);
+                    h.prims.push_back(s);
+                }
+            break;
+        }
+        case RT_OBJECT_MODEL:
+            if (o.tri_count > 0) {
+                h.tri_ranges.push_back({o.tri_first, o.tri_count});
+                h.tri_range_obj.push_back(k);
+                h.n_tris += o.tri_count;
+            }
+            break;
+        }
+    }
+}
+
+extern "C" int rt_scene_upload(rt_ctx *ctx, const rt_scene_desc *d, int32_t *scene_id)
+{
+    if (!ctx || !scene_id) return RT_ERR_INVALID;
+    int rc = validate_desc(ctx, d);
+    if (rc) return rc;
+    CK(ctx, cudaSetDevice(ctx->device));
+    HostTables h;
+    build_tables(d, h);
+    std::unique_ptr<SceneDev> sc(new SceneDev());
+    sc->camera = d->camera;
+    const int64_t n = h.n_tris;
+    sc->n_tris = (int)n;
+    // one allocation for tables, triangle inputs and the LBVH
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        size_t o = off;
+        off += a256(bytes);
+        return o;
+    };
+    const size_t o_prims = take(sizeof(DevPrim) * std::max<size_t>(1, h.prims.size()));
+    const size_t o_mtl = take(sizeof(DevMaterial) * h.mtl.size());
+    const size_t o_lights = take(sizeof(DevLight) * std::max<size_t>(1, h.lights.size()));
+    const size_t o_tex = take(sizeof(DevTexture) * std::max<size_t>(1, h.tex.size()));
+    const size_t o_texels = take(h.texels.size());
+    const size_t o_objpos = take(sizeof(float) * h.obj_pos.size());
+    const bool has_uv = d->tri_uv != nullptr;
+    const size_t o_tp = take(sizeof(float) * 9 * (size_t)n), o_tn = take(sizeof(float) * 9 * (size_t)n);
+    const size_t o_tuv = has_uv ? take(sizeof(float) * 6 * (size_t)n) : 0;
+    const size_t o_tm = take(sizeof(int) * (size_t)n), o_ti = take(sizeof(int) * (size_t)n), o_to = take(sizeof(int) * (size_t)n);
+    const size_t o_nodes = take(sizeof(float4) * 2 * (size_t)std::max<int64_t>(1, 2 * n - 1));
+    const size_t o_tri = take(sizeof(float4) * 3 * (size_t)n), o_trin = take(sizeof(float4) * 3 * (size_t)n);
+    const size_t o_triuv = has_uv ? take(sizeof(float2) * 3 * (size_t)n) : 0;
+    const size_t o_hdr = take(sizeof(DevScene));
+    CK(ctx, sc->mem.ensure(off));
+    char *base = (char *)sc->mem.p;
+    cudaStream_t s = ctx->stream;
+    // staging copies of the compacted triangle inputs
+    std::vector<float> tp((size_t)n * 9), tn((size_t)n * 9), tuv(has_uv ? (size_t)n * 6 : 0);
+    std::vector<int> tm((size_t)n), ti((size_t)n), to((size_t)n);
+    {
+        size_t w = 0;
+        for (size_t r = 0; r < h.tri_ranges.size(); ++r) {
+            const int64_t first = h.tri_ranges[r].first, cnt = h.tri_ranges[r].second;
+            std::memcpy(&tp[w * 9], d->tri_p + first * 9, sizeof(float) * 9 * (size_t)cnt);
+            std::memcpy(&tn[w * 9], d->tri_n + first * 9, sizeof(float) * 9 * (size_t)cnt);
+            if (has_uv) std::memcpy(&tuv[w * 6], d->tri_uv + first * 6, sizeof(float) * 6 * (size_t)cnt);
+            for (int64_t i = 0; i < cnt; ++i) {
+                tm[w + i] = d->tri_mtl[first + i];
+                ti[w + i] = d->tri_id ? d->tri_id[first + i] : (int)i;
+                to[w + i] = h.tri_range_obj[r];
+            }
+            w += (size_t)cnt;
+        }
+    }
+    CK(ctx, cudaMemcpyAsync(base + o_prims, h.prims.data(), sizeof(DevPrim) * h.prims.size(), cudaMemcpyHostToDevice, s));
+    CK(ctx, cudaMemcpyAsync(base + o_mtl, h.mtl.data(), sizeof(DevMaterial) * h.mtl.size(), cudaMemcpyHostToDevice, s));
+    CK(ctx, cudaMemcpyAsync(base + o_lights, h.lights.data(), sizeof(DevLight) * h.lights.size(), cudaMemcpyHostToDevice, s));
+    CK(ctx, cudaMemcpyAsync(base + o_tex, h.tex.data(), sizeof(DevTexture) * h.tex.size(), cudaMemcpyHostToDevice, s));
+    CK(ctx, cudaMemcpyAsync(base + o_texels, h.texels.data(), h.texels.size(), cudaMemcpyHostToDevice, s));
+    CK(ctx, cudaMemcpyAsync(base + o_objpos, h.obj_pos.data(), sizeof(float) * h.obj_pos.size(), cudaMemcpyHostToDevice, s));
+    if (n > 0) {
+        CK(ctx, cudaMemcpyAsync(base + o_tp, tp.data(), sizeof(float) * tp.size(), cudaMemcpyHostToDevice, s));
+        CK(ctx, cudaMemcpyAsync(base + o_tn, tn.data(), sizeof(float) * tn.size(), cudaMemcpyHostToDevice, s));
+        if (has_uv) CK(ctx, cudaMemcpyAsync(base + o_tuv, tuv.data(), sizeof(float) * tuv.size(), cudaMemcpyHostToDevice, s));
+        CK(ctx, cudaMemcpyAsync(base + o_tm, tm.data(), sizeof(int) * (size_t)n, cudaMemcpyHostToDevice, s));
+        CK(ctx, cudaMemcpyAsync(base + o_ti, ti.data(), sizeof(int) * (size_t)n, cudaMemcpyHostToDevice, s));
+        CK(ctx, cudaMemcpyAsync(base + o_to, to.data(), sizeof(int) * (size_t)n, cudaMemcpyHostToDevice, s));
+    }
+    DevScene &H = sc->hdr;
+    H.prims = (const DevPrim *)(base + o_prims);
+    H.n_prims = (int)h.prims.size();
+    H.n_tris = (int)n;
+    H.nodes = (const float4 *)(base + o_nodes);
+    H.tri = (const float4 *)(base + o_tri);
+    H.trin = (const float4 *)(base + o_trin);
+    H.triuv = has_uv ? (const float2 *)(base + o_triuv) : nullptr;
+    H.mtl = (const DevMaterial *)(base + o_mtl);
+    H.lights = (const DevLight *)(base + o_lights);
+    H.tex = (const DevTexture *)(base + o_tex);
+    H.texels = (const uint8_t *)(base + o_texels);
+    H.n_lights = (int)h.lights.size();
+    H.n_mtl = (int)h.mtl.size();
+    for (int k = 0; k < 3; ++k) H.env[k] = d->env_light[k];
+    sc->d_hdr = (DevScene *)(base + o_hdr);
+    CK(ctx, cudaMemcpyAsync(sc->d_hdr, &H, sizeof(DevScene), cudaMemcpyHostToDevice, s));
+    sc->in.tri_p = (const float *)(base + o_tp);
+    sc->in.tri_n = (const float *)(base + o_tn);
+    sc->in.tri_uv = has_uv ? (const float *)(base + o_tuv) : nullptr;
+    sc->in.tri_mtl = (const int *)(base + o_tm);
+    sc->in.tri_id = (const int *)(base + o_ti);
+    sc->in.tri_obj = (const int *)(base + o_to);
+    sc->in.obj_pos = (const float *)(base + o_objpos);
+    sc->in.n = (int)n;
+    sc->out.nodes = (float4 *)(base + o_nodes);
+    sc->out.tri = (float4 *)(base + o_tri);
+    sc->out.trin = (float4 *)(base + o_trin);
+    sc->out.triuv = has_uv ? (float2 *)(base + o_triuv) : nullptr;
+    sc->bytes = (int64_t)off;
+    const int id = ctx->next_scene++;
+    ctx->scenes[id] = std::move(sc);
+    rc = rt_scene_rebuild(ctx, id);
+    if (rc) {
+        ctx->scenes.erase(id);
+        return rc;
+    }
+    *scene_id = id;
+    return RT_OK;
+}
+
+extern "C" int rt_scene_rebuild(rt_ctx *ctx, int32_t id)
+{
+    if (!ctx) return RT_ERR_INVALID;
+    auto it = ctx->scenes.find(id);
+    if (it == ctx->scenes.end()) return ctx_fail(ctx, RT_ERR_NOT_FOUND, "unknown scene %d", id);
+    SceneDev &sc = *it->second;
+    if (sc.n_tris <= 0) {
+        sc.build_ms = 0.0f;
+        return RT_OK;
+    }
+    CK(ctx, ctx->lbvh_scratch.ensure(lbvh_scratch_bytes(sc.n_tris)));
+    cudaEvent_t a, b;
+    CK(ctx, cudaEventCreate(&a));
+    CK(ctx, cudaEventCreate(&b));
+    cudaEventRecord(a, ctx->stream);
+    cudaError_t e = lbvh_build(sc.in, sc.out, ctx->lbvh_scratch.p, ctx->stream);
+    cudaEventRecord(b, ctx->stream);
+    if (e == cudaSuccess) e = cudaEventSynchronize(b);
+    float ms = 0.0f;
+    if (e == cudaSuccess) cudaEventElapsedTime(&ms, a, b);
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    if (e != cudaSuccess) return ctx_fail(ctx, RT_ERR_CUDA, "LBVH build: %s", cudaGetErrorString(e));
+    sc.build_ms = ms;
+    return RT_OK;
+}
+
+extern "C" int rt_scene_update_camera(rt_ctx *ctx, int32_t id, const rt_camera *cam)
+{
+    if (!ctx || !cam) return RT_ERR_INVALID;
+    auto it = ctx->scenes.find(id);
+    if (it == ctx->scenes.end()) return ctx_fail(ctx, RT_ERR_NOT_FOUND, "unknown scene %d", id);
+    it->second->camera = *cam;
+    return RT_OK;
+}
+
+extern "C" int rt_scene_release(rt_ctx *ctx, int32_t id)
+{
+    if (!ctx) return RT_ERR_INVALID;
+    auto it = ctx->scenes.find(id);
+    if (it == ctx->scenes.end()) return ctx_fail(ctx, RT_ERR_NOT_FOUND, "unknown scene %d", id);
+    cudaStreamSynchronize(ctx->stream);
+    ctx->scenes.erase(it);
+    return RT_OK;
+}
+
+extern "C" int rt_scene_device_bytes(rt_ctx *ctx, int32_t id, int64_t *bytes)
+{
+    if (!ctx || !bytes) return RT_ERR_INVALID;
+    auto it = ctx->scenes.find(id);
+    if (it == ctx->scenes.end()) return ctx_fail(ctx, RT_ERR_NOT_FOUND, "unknown scene %d", id);
+    *bytes = it->second->bytes;
+    return RT_OK;
+}
+
+extern "C" int rt_scene_build_ms(rt_ctx *ctx, int32_t id, float *ms)
+{
+    if (!ctx || !ms) return RT_ERR_INVALID;
+    auto it = ctx->scenes.find(id);
+    if (it == ctx->scenes.end()) return ctx_fail(ctx, RT_ERR_NOT_FOUND, "unknown scene %d", id);
+    *ms = it->second->build_ms;
+    return RT_OK;
+}
+
+// ---- frames --------------------------------------------------------------------------------------------
+int frame_alloc(rt_ctx *ctx, int32_t w, int32_t h, FrameDev &f)
+{
+    if (w <= 0 || h <= 0 || w > 16384 || h > 16384)
+        return ctx_fail(ctx, RT_ERR_INVALID, "frame size %dx%d outside [1,16384]", w, h);
+    const size_t np = (size_t)w * h;
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        size_t o = off;
+        off += a256(bytes);
+        return o;
+    };
+    const size_t o_acc = take(24 * np), o_rgb = take(12 * np), o_rgb8 = take(3 * np), o_po = take(4 * np),
+                 o_pp = take(4 * np), o_pt = take(4 * np);
+    CK(ctx, f.mem.ensure(off));
+    char *b = (char *)f.mem.p;
+    f.w = w, f.h = h;
+    f.fb.acc = (long long *)(b + o_acc);
+    f.fb.rgb = (float *)(b + o_rgb);
+    f.fb.rgb8 = (uint8_t *)(b + o_rgb8);
+    f.fb.plane_obj = (int *)(b + o_po);
+    f.fb.plane_prim = (int *)(b + o_pp);
+    f.fb.plane_t = (float *)(b + o_pt);
+    f.bytes = (int64_t)off;
+    return RT_OK;
+}
+
+extern "C" int rt_frame_create(rt_ctx *ctx, int32_t w, int32_t h, int32_t *frame_id)
+{
+    if (!ctx || !frame_id) return RT_ERR_INVALID;
+    CK(ctx, cudaSetDevice(ctx->device));
+    std::unique_ptr<FrameDev> f(new FrameDev());
+    int rc = frame_alloc(ctx, w, h, *f);
+    if (rc) return rc;
+    CK(ctx, cudaMemsetAsync(f->mem.p, 0, f->bytes, ctx->stream));
+    const int id = ctx->next_frame++;
+    ctx->frames[id] = std::move(f);
+    *frame_id = id;
+    return RT_OK;
+}
+
+extern "C" int rt_frame_release(rt_ctx *ctx, int32_t id)
+{
+    if (!ctx) return RT_ERR_INVALID;
+    auto it = ctx->frames.find(id);
+    if (it == ctx->frames.end()) return ctx_fail(ctx, RT_ERR_NOT_FOUND, "unknown frame %d", id);
+    cudaStreamSynchronize(ctx->stream);
+    ctx->frames.erase(it);
+    return RT_OK;
+}
+
+extern "C" int rt_frame_device_ptrs(rt_ctx *ctx, int32_t id, void **rgb, void **rgb8)
+{
+    if (!ctx) return RT_ERR_INVALID;
+    auto it = ctx->frames.find(id);
+    if (it == ctx->frames.end()) return ctx_fail(ctx, RT_ERR_NOT_FOUND, "unknown frame %d", id);
+    if (rgb) *rgb = it->second->fb.rgb;
+    if (rgb8) *rgb8 = it->second->fb.rgb8;
+    return RT_OK;
+}
+
+extern "C" int rt_frame_download(rt_ctx *ctx, int32_t id, float *rgb, uint8_t *rgb8, int32_t *hit_obj,
+                                 int32_t *hit_prim, float *hit_t)
+{
+    if (!ctx) return RT_ERR_INVALID;
+    auto it = ctx->frames.find(id);
+    if (it == ctx->frames.end()) return ctx_fail(ctx, RT_ERR_NOT_FOUND, "unknown frame %d", id);
+    FrameDev &f = *it->second;
+    const size_t np = (size_t)f.w * f.h;
+    cudaStream_t s = ctx->stream;
+    if (rgb) CK(ctx, cudaMemcpyAsync(rgb, f.fb.rgb, 12 * np, cudaMemcpyDeviceToHost, s));
+    if (rgb8) CK(ctx, cudaMemcpyAsync(rgb8, f.fb.rgb8, 3 * np, cudaMemcpyDeviceToHost, s));
+    if (hit_obj) CK(ctx, cudaMemcpyAsync(hit_obj, f.fb.plane_obj, 4 * np, cudaMemcpyDeviceToHost, s));
+    if (hit_prim) CK(ctx, cudaMemcpyAsync(hit_prim, f.fb.plane_prim, 4 * np, cudaMemcpyDeviceToHost, s));
+    if (hit_t) CK(ctx, cudaMemcpyAsync(hit_t, f.fb.plane_t, 4 * np, cudaMemcpyDeviceToHost, s));
+    CK(ctx, cudaStreamSynchronize(s));
+    return RT_OK;
+}
+
+// ---- workspace --------------------------------------------------------------------------------------------
+int ws_ensure(rt_ctx *ctx, Workspace &ws, long long qcap, int njobs)
+{
+    if (qcap > (1ll << 30)) return ctx_fail(ctx, RT_ERR_OOM, "ray queue of %lld rays is too large", qcap);
+    if (qcap <= ws.qcap && njobs <= ws.jobcap && ws.mem.p) return RT_OK;
+    qcap = std::max(qcap, ws.qcap);
+    njobs = std::max(njobs, ws.jobcap);
+    cudaStreamSynchronize(ctx->stream);
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        size_t o = off;
+        off += a256(bytes);
+        return o;
+    };
+    const size_t q = (size_t)qcap;
+    size_t oq[2][4];
+    for (int k = 0; k < 2; ++k)
+        for (int j = 0; j < 4; ++j) oq[k][j] = take(16 * q);
+    size_t os[5];
+    for (int j = 0; j < 5; ++j) os[j] = take(16 * q);
+    const size_t o_hit = take(16 * q), o_nob = take(4 * q), o_ctr = take(sizeof(Counters)),
+                 o_jobs = take(sizeof(DevJob) * (size_t)njobs), o_end = take(8 * (size_t)njobs), o_tot = take(32),
+                 o_scn = take(sizeof(DevScene) * (size_t)njobs);
+    CK(ctx, ws.mem.ensure(off));
+    char *b = (char *)ws.mem.p;
+    for (int k = 0; k < 2; ++k) {
+        ws.wf.q[k].o = (float4 *)(b + oq[k][0]);
+        ws.wf.q[k].d = (float4 *)(b + oq[k][1]);
+        ws.wf.q[k].w = (float4 *)(b + oq[k][2]);
+        ws.wf.q[k].m = (int4 *)(b + oq[k][3]);
+        ws.wf.q[k].capacity = (int)q;
+    }
+    ws.wf.sq.p = (float4 *)(b + os[0]);
+    ws.wf.sq.n = (float4 *)(b + os[1]);
+    ws.wf.sq.v = (float4 *)(b + os[2]);
+    ws.wf.sq.wc = (float4 *)(b + os[3]);
+    ws.wf.sq.ws = (float4 *)(b + os[4]);
+    ws.wf.sq.capacity = (int)q;
+    ws.wf.hit = (float4 *)(b + o_hit);
+    ws.wf.newobj = (int *)(b + o_nob);
+    ws.wf.C = (Counters *)(b + o_ctr);
+    ws.jobs = (DevJob *)(b + o_jobs);
+    ws.job_end = (long long *)(b + o_end);
+    ws.scalars = (long long *)(b + o_tot);
+    ws.scenes = (DevScene *)(b + o_scn);
+    ws.wf.jobs = ws.jobs;
+    ws.wf.job_sample_end = ws.job_end;
+    ws.wf.total_samples = ws.scalars;
+    ws.wf.sample_offset = ws.scalars + 1;
+    ws.wf.n_jobs = ws.scalars + 2;
+    ws.wf.scenes = ws.scenes;
+    ws.qcap = qcap;
+    ws.jobcap = njobs;
+    ctx->graphs.clear();   // captured graphs point into the old workspace
+    return RT_OK;
+}
+
+// ---- jobs ---------------------------------------------------------------------------------------------------
+int make_job(rt_ctx *ctx, const SceneDev &sc, FrameDev &f, const rt_render_desc *rd, int scene_slot, DevJob &J,
+             long long &samples)
+{
+    if (!rd) return ctx_fail(ctx, RT_ERR_INVALID, "render desc is NULL");
+    const rt_camera &cam = rd->camera ? *rd->camera : sc.camera;
+    const int W = rd->width > 0 ? rd->width : cam.width, H = rd->height > 0 ? rd->height : cam.height;
+    if (W != f.w || H != f.h) return ctx_fail(ctx, RT_ERR_INVALID, "frame is %dx%d but the render is %dx%d", f.w, f.h, W, H);
+    if (rd->spp < 1 || rd->spp > 1024) return ctx_fail(ctx, RT_ERR_INVALID, "spp %d outside [1,1024]", rd->spp);
+    if (rd->max_level < 0 || rd->max_level > 4) return ctx_fail(ctx, RT_ERR_INVALID, "max_level %d outside [0,4]", rd->max_level);
+    if (rd->mode != RT_MODE_RAYTRACE && rd->mode != RT_MODE_REFRACT)
+        return ctx_fail(ctx, RT_ERR_INVALID, "render mode 0x%x is not supported", rd->mode);
+    if (!(cam.fovy > 0 && cam.fovy < 180) || !finite3(cam.position) || !finite3(cam.n))
+        return ctx_fail(ctx, RT_ERR_INVALID, "camera is not valid");
+    J = DevJob{};
+    J.scene = scene_slot;
+    J.width = W, J.height = H, J.spp = rd->spp;
+    J.max_level = rd->max_level, J.flags = rd->flags, J.mode = rd->mode;
+    J.xlim = (rd->flags & RT_FLAG_REF_TILES) ? (W / 64) * 64 : W;
+    J.ylim = (rd->flags & RT_FLAG_REF_TILES) ? (H / 64) * 64 : H;
+    J.acc = f.fb.acc;
+    if (rd->flags & RT_FLAG_HIT_PLANES) {
+        J.plane_obj = f.fb.plane_obj, J.plane_prim = f.fb.plane_prim, J.plane_t = f.fb.plane_t;
+    }
+    for (int k = 0; k < 3; ++k) {
+        J.cam_pos[k] = cam.position[k], J.cam_u[k] = cam.u[k], J.cam_v[k] = cam.v[k], J.cam_n[k] = cam.n[k];
+    }
+    const double PIr = 3.1415926535897932384;
+    J.dp = std::tan(cam.fovy * PIr / 360) / (H / 2);
+    J.znear = cam.znear;
+    J.zfar = (float)(std::sqrt(2.0) * (double)cam.zfar);
+    J.seed = rd->seed;
+    J.slot = -1;
+    samples = (long long)J.xlim * J.ylim * J.spp;
+    return RT_OK;
+}
+
+// enqueue the level loop of one wave whose jobs are already in the workspace
+void enqueue_levels(rt_ctx *ctx, Workspace &ws, int max_level, const Tuning &t, cudaStream_t s)
+{
+    (void)ctx;
+    const int raygen_grid = sm_count() * 8;
+    launch_raygen(ws.wf, raygen_grid, 256, s);
+    for (int level = 0; level <= max_level; ++level) {
+        const int sel = level & 1;
+        launch_extend(ws.wf, sel, level, t, s);
+        launch_shade(ws.wf, sel, level, t, s);
+        launch_shadow(ws.wf, level, t, s);
+    }
+}
+
+static int render_once(rt_ctx *ctx, SceneDev &sc, FrameDev &f, const rt_render_desc *rd, long long qcap)
+{
+    DevJob J;
+    long long samples = 0;
+    int rc = make_job(ctx, sc, f, rd, 0, J, samples);
+    if (rc) return rc;
+    if (qcap <= 0) qcap = std::max<long long>(2 * samples, 4096);
+    rc = ws_ensure(ctx, ctx->ws, qcap, 1);
+    if (rc) return rc;
+    Workspace &ws = ctx->ws;
+    cudaStream_t s = ctx->stream;
+    ws.wf.cancel = ctx->cancel_dev;
+    *ctx->cancel_host = 0;
+    ctx->h_scalars[0] = samples;
+    ctx->h_scalars[1] = 0;
+    ctx->h_scalars[2] = 1;
+    ctx->h_job_end[0] = samples;
+    CK(ctx, cudaEventRecord(ctx->ev_start, s));
+    CK(ctx, cudaMemcpyAsync(ws.scenes, &sc.hdr, sizeof(DevScene), cudaMemcpyHostToDevice, s));
+    CK(ctx, cudaMemcpyAsync(ws.jobs, &J, sizeof(DevJob), cudaMemcpyHostToDevice, s));
+    CK(ctx, cudaMemcpyAsync(ws.job_end, ctx->h_job_end, 8, cudaMemcpyHostToDevice, s));
+    CK(ctx, cudaMemcpyAsync(ws.scalars, ctx->h_scalars, 24, cudaMemcpyHostToDevice, s));
+    CK(ctx, cudaMemsetAsync(ws.wf.C, 0, sizeof(Counters), s));
+    CK(ctx, cudaMemsetAsync(f.fb.acc, 0, 24 * (size_t)f.w * f.h, s));
+    if (rd->flags & RT_FLAG_HIT_PLANES) launch_plane_init(f.fb, (long long)f.w * f.h, s);
+    Tuning t = ctx->plain_tuning;
+    t.count = (rd->flags & RT_FLAG_COUNT_WORK) != 0;
+    enqueue_levels(ctx, ws, rd->max_level, t, s);
+    launch_resolve(f.fb, f.w, f.h, rd->spp, s);
+    CK(ctx, cudaGetLastError());
+    CK(ctx, cudaMemcpyAsync(ctx->counters_host, ws.wf.C, sizeof(Counters), cudaMemcpyDeviceToHost, s));
+    CK(ctx, cudaEventRecord(ctx->ev_stop, s));
+    return RT_OK;
+}
+
+extern "C" int rt_render(rt_ctx *ctx, int32_t scene_id, int32_t frame_id, const rt_render_desc *rd)
+{
+    if (!ctx) return RT_ERR_INVALID;
+    auto si = ctx->scenes.find(scene_id);
+    if (si == ctx->scenes.end()) return ctx_fail(ctx, RT_ERR_NOT_FOUND, "unknown scene %d", scene_id);
+    auto fi = ctx->frames.find(frame_id);
+    if (fi == ctx->frames.end()) return ctx_fail(ctx, RT_ERR_NOT_FOUND, "unknown frame %d", frame_id);
+    CK(ctx, cudaSetDevice(ctx->device));
+    ctx->pending = Pending{scene_id, frame_id, rd ? *rd : rt_render_desc{}, true, 0};
+    int rc = render_once(ctx, *si->second, *fi->second, rd, 0);
+    if (rc) ctx->pending.active = false;
+    return rc;
+}
+
+extern "C" int rt_render_wait(rt_ctx *ctx, rt_render_stats *stats)
+{
+    if (!ctx) return RT_ERR_INVALID;
+    CK(ctx, cudaEventSynchronize(ctx->ev_stop));
+    int retries = 0;
+    while (ctx->pending.active && ctx->counters_host->overflow) {
+        if (++retries > 4) return ctx_fail(ctx, RT_ERR_OVERFLOW, "ray queues overflowed after %d retries", retries - 1);
+        auto si = ctx->scenes.find(ctx->pending.scene);
+        auto fi = ctx->frames.find(ctx->pending.frame);
+        if (si == ctx->scenes.end() || fi == ctx->frames.end()) return ctx_fail(ctx, RT_ERR_NOT_FOUND, "render target released");
+        int rc = render_once(ctx, *si->second, *fi->second, &ctx->pending.rd, ctx->ws.qcap * 2);
+        if (rc) return rc;
+        CK(ctx, cudaEventSynchronize(ctx->ev_stop));
+    }
+    ctx->pending.retries = retries;
+    const bool was_cancelled = *ctx->cancel_host != 0;
+    *ctx->cancel_host = 0;
+    if (stats) {
+        const Counters &C = *ctx->counters_host;
+        stats->rays_primary = (int64_t)C.rays_primary;
+        stats->rays_secondary = (int64_t)C.rays_secondary;
+        stats->rays_shadow = (int64_t)C.rays_shadow;
+        stats->nodes_visited = (int64_t)C.nodes;
+        stats->tris_tested = (int64_t)C.tris;
+        stats->spheres_tested = (int64_t)C.spheres;
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, ctx->ev_start, ctx->ev_stop);
+        stats->ms = ms;
+        stats->overflow_retries = retries;
+    }
+    ctx->pending.active = false;
+    if (was_cancelled) return ctx_fail(ctx, RT_ERR_CANCELLED, "render cancelled");
+    if (ctx->counters_host->error)
+        return ctx_fail(ctx, RT_ERR_CUDA, "traversal stopped on a corrupt LBVH (flags 0x%x)", ctx->counters_host->error);
+    return RT_OK;
+}
+
+extern "C" int rt_cancel(rt_ctx *ctx)
+{
+    if (!ctx) return RT_ERR_INVALID;
+    *ctx->cancel_host = 1;
+    return RT_OK;
+}
+
+extern "C" int rt_poll(rt_ctx *ctx)
+{
+    if (!ctx) return RT_ERR_INVALID;
+    cudaError_t e = cudaEventQuery(ctx->ev_stop);
+    if (e == cudaErrorNotReady) return 0;
+    if (e != cudaSuccess) return ctx_fail(ctx, RT_ERR_CUDA, "%s", cudaGetErrorString(e));
+    return 1;
+}
+
+extern "C" int rt_render_host(rt_ctx *ctx, const rt_scene_desc *desc, const rt_render_desc *rd, uint8_t *out_rgb8,
+                              float *out_rgb, rt_render_stats *stats)
+{
+    if (!ctx || !desc || !rd) return RT_ERR_INVALID;
+    int32_t sid = -1, fid = -1;
+    int rc = rt_scene_upload(ctx, desc, &sid);
+    if (rc) return rc;
+    const rt_camera &cam = rd->camera ? *rd->camera : desc->camera;
+    const int W = rd->width > 0 ? rd->width : cam.width, H = rd->height > 0 ? rd->height : cam.height;
+    rc = rt_frame_create(ctx, W, H, &fid);
+    if (!rc) rc = rt_render(ctx, sid, fid, rd);
+    if (!rc) rc = rt_render_wait(ctx, stats);
+    if (!rc) rc = rt_frame_download(ctx, fid, out_rgb, out_rgb8, nullptr, nullptr, nullptr);
+    if (fid >= 0) rt_frame_release(ctx, fid);
+    rt_scene_release(ctx, sid);
+    return rc;
+}
+
+// ---- LBVH test hooks ------------------------------------------------------------------------------------------
+extern "C" int rt_morton_sort(rt_ctx *ctx, const float *tri_p, int64_t n, uint32_t *codes, uint32_t *perm)
+{
+    if (!ctx || (n > 0 && (!tri_p || !codes || !perm)) || n < 0 || n >= (1ll << 30)) return RT_ERR_INVALID;
+    if (n == 0) return RT_OK;
+    CK(ctx, cudaSetDevice(ctx->device));
+    DevBuf buf;
+    const size_t o_p = 0, o_o = a256(36 * (size_t)n), o_pos = o_o + a256(4 * (size_t)n), o_c = o_pos + 256,
+                 o_pm = o_c + a256(4 * (size_t)n), end = o_pm + a256(4 * (size_t)n);
+    CK(ctx, buf.ensure(end));
+    CK(ctx, ctx->lbvh_scratch.ensure(lbvh_scratch_bytes((int)n)));
+    char *b = (char *)buf.p;
+    cudaStream_t s = ctx->stream;
+    CK(ctx, cudaMemcpyAsync(b + o_p, tri_p, 36 * (size_t)n, cudaMemcpyHostToDevice, s));
+    CK(ctx, cudaMemsetAsync(b + o_o, 0, 4 * (size_t)n, s));
+    CK(ctx, cudaMemsetAsync(b + o_pos, 0, 256, s));
+    LbvhInput in{};
+    in.tri_p = (const float *)(b + o_p);
+    in.tri_obj = (const int *)(b + o_o);
+    in.obj_pos = (const float *)(b + o_pos);
+    in.n = (int)n;
+    CK(ctx, lbvh_morton_sort(in, (uint32_t *)(b + o_c), (uint32_t *)(b + o_pm), ctx->lbvh_scratch.p, s));
+    CK(ctx, cudaMemcpyAsync(codes, b + o_c, 4 * (size_t)n, cudaMemcpyDeviceToHost, s));
+    CK(ctx, cudaMemcpyAsync(perm, b + o_pm, 4 * (size_t)n, cudaMemcpyDeviceToHost, s));
+    CK(ctx, cudaStreamSynchronize(s));
+    return RT_OK;
+}
+
+extern "C" int rt_scene_bvh_download(rt_ctx *ctx, int32_t id, float *nodes, uint32_t *perm, int64_t *n_nodes)
+{
+    if (!ctx) return RT_ERR_INVALID;
+    auto it = ctx->scenes.find(id);
+    if (it == ctx->scenes.end()) return ctx_fail(ctx, RT_ERR_NOT_FOUND, "unknown scene %d", id);
+    SceneDev &sc = *it->second;
+    const int64_t n = sc.n_tris, nn = n > 0 ? 2 * n - 1 : 0;
+    if (n_nodes) *n_nodes = nn;
+    cudaStream_t s = ctx->stream;
+    if (nodes && nn) CK(ctx, cudaMemcpyAsync(nodes, sc.out.nodes, 32 * (size_t)nn, cudaMemcpyDeviceToHost, s));
+    if (perm && n) {   // original triangle order = reported id is not unique, so read p0.w of each slot
+        std::vector<float4> tri((size_t)n * 3);
+        CK(ctx, cudaMemcpyAsync(tri.data(), sc.out.tri, 48 * (size_t)n, cudaMemcpyDeviceToHost, s));
+        CK(ctx, cudaStreamSynchronize(s));
+        for (int64_t k = 0; k < n; ++k) {
+            float w = tri[(size_t)k * 3].w;
+            int32_t id32;
+            std::memcpy(&id32, &w, 4);
+            perm[k] = (uint32_t)id32;
+        }
+    }
+    CK(ctx, cudaStreamSynchronize(s));
+    return RT_OK;
+}

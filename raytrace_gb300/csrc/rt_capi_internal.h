@@ -1,0 +1,107 @@
+// rt_capi_internal.h — host-side objects behind the C ABI handles.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <map>
+#include <memory>
+#include <string>
+
+#include "../../include/rt_gb300.h"
+#include "rt_kernels.cuh"
+#include "rt_lbvh.cuh"
+
+// one device allocation that only grows
+struct DevBuf {
+    void *p = nullptr;
+    size_t bytes = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf &) = delete;
+    DevBuf &operator=(const DevBuf &) = delete;
+    DevBuf(DevBuf &&o) noexcept : p(o.p), bytes(o.bytes) { o.p = nullptr, o.bytes = 0; }
+    DevBuf &operator=(DevBuf &&o) noexcept
+    {
+        if (this != &o) {
+            release();
+            p = o.p, bytes = o.bytes;
+            o.p = nullptr, o.bytes = 0;
+        }
+        return *this;
+    }
+    ~DevBuf();
+    void release();
+    cudaError_t ensure(size_t need);
+};
+
+struct SceneDev {
+    DevBuf mem;                  // tables, triangle inputs, LBVH
+    rtg::DevScene hdr{};         // header with device pointers (host copy)
+    rtg::DevScene *d_hdr = nullptr;
+    rtg::LbvhInput in{};
+    rtg::LbvhOutput out{};
+    rt_camera camera{};
+    int n_tris = 0;
+    int64_t bytes = 0;
+    float build_ms = 0.0f;
+};
+
+struct FrameDev {
+    DevBuf mem;
+    rtg::FrameBufs fb{};
+    int w = 0, h = 0;
+    int64_t bytes = 0;
+};
+
+// ray queues, shadow queue, hit buffers, counters and job tables of one wavefront
+struct Workspace {
+    DevBuf mem;
+    rtg::Wavefront wf{};
+    rtg::DevJob *jobs = nullptr;
+    long long *job_end = nullptr;
+    long long *scalars = nullptr;   // [0] samples in the wave, [1] first sample, [2] jobs
+    rtg::DevScene *scenes = nullptr;
+    long long qcap = 0;
+    int jobcap = 0;
+};
+
+struct Pending {
+    int scene = -1, frame = -1;
+    rt_render_desc rd{};
+    bool active = false;
+    int retries = 0;
+};
+
+struct GraphEntry {
+    cudaGraphExec_t exec = nullptr;
+    ~GraphEntry()
+    {
+        if (exec) cudaGraphExecDestroy(exec);
+    }
+};
+
+struct rt_ctx {
+    int device = 0;
+    cudaStream_t own_stream = nullptr, stream = nullptr;
+    cudaEvent_t ev_start = nullptr, ev_stop = nullptr;
+    std::string err;
+    std::map<int, std::unique_ptr<SceneDev>> scenes;
+    std::map<int, std::unique_ptr<FrameDev>> frames;
+    int next_scene = 0, next_frame = 0;
+    Workspace ws;
+    DevBuf lbvh_scratch;
+    volatile int *cancel_host = nullptr;
+    int *cancel_dev = nullptr;
+    rtg::Counters *counters_host = nullptr;
+    long long h_scalars[4] = {0, 0, 0, 0};
+    long long h_job_end[1] = {0};
+    Pending pending;
+    rtg::Tuning plain_tuning;
+    std::map<long long, std::unique_ptr<GraphEntry>> graphs;
+};
+
+int ctx_fail(rt_ctx *ctx, int code, const char *fmt, ...);
+int validate_desc(rt_ctx *ctx, const rt_scene_desc *d);
+int frame_alloc(rt_ctx *ctx, int32_t w, int32_t h, FrameDev &f);
+int ws_ensure(rt_ctx *ctx, Workspace &ws, long long qcap, int njobs);
+int make_job(rt_ctx *ctx, const SceneDev &sc, FrameDev &f, const rt_render_desc *rd, int scene_slot, rtg::DevJob &J,
+             long long &samples);
+void enqueue_levels(rt_ctx *ctx, Workspace &ws, int max_level, const rtg::Tuning &t, cudaStream_t s);

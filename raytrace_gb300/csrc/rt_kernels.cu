@@ -1,0 +1,602 @@
+// rt_kernels.cu — wavefront kernels of the GB300 renderer.
+//
+// One level of the reference's RTfrac recursion (RayTracer.cpp:450-596) is one pass:
+//   extend  closest hit of every ray in the queue                 (:458-465)
+//   shade   zNear/zFar cut, local ambient term, one shadow work item per hit, reflect and
+//           refract children appended to the next queue with warp ballot/popc compaction
+//                                                                 (:466-593)
+//   shadow  the per-light shadow rays of each hit (any-hit), diffuse and Blinn terms of the
+//           unblocked lights                                      (:474-545)
+// The recursion tree is flattened into per-ray RGB weights: a child's colour enters its
+// parent as r*(1-f)*C_R and f*(C_T (x) Beer), so every node adds weight (x) local colour to its
+// pixel. Pixels accumulate in 64-bit fixed point (2^-32) with integer atomics, which makes
+// the sum independent of the order in which rays finish: the same frame gives the same bits
+// alone or batched with other frames.
+#include <cstdio>
+
+#include "rt_kernels.cuh"
+#include "rt_trace.cuh"
+
+namespace rtg {
+
+constexpr unsigned kFull = 0xffffffffu;
+constexpr float kFix = 4294967296.0f;   // 2^32
+
+__device__ __forceinline__ void acc_add(long long *acc, int pix, V3 c)
+{
+    unsigned long long *a = reinterpret_cast<unsigned long long *>(acc + 3ll * pix);
+    if (c.x != 0.0f && c.x == c.x) atomicAdd(a + 0, (unsigned long long)__float2ll_rn(c.x * kFix));
+    if (c.y != 0.0f && c.y == c.y) atomicAdd(a + 1, (unsigned long long)__float2ll_rn(c.y * kFix));
+    if (c.z != 0.0f && c.z == c.z) atomicAdd(a + 2, (unsigned long long)__float2ll_rn(c.z * kFix));
+}
+
+// Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11)
+__device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint2 k)
+{
+    const unsigned M0 = 0xD2511F53u, M1 = 0xCD9E8D57u, W0 = 0x9E3779B9u, W1 = 0xBB67AE85u;
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        unsigned hi0 = __umulhi(M0, c.x), lo0 = M0 * c.x;
+        unsigned hi1 = __umulhi(M1, c.z), lo1 = M1 * c.z;
+        c = make_uint4(hi1 ^ c.y ^ k.x, lo1, hi0 ^ c.w ^ k.y, lo0);
+        k.x += W0;
+        k.y += W1;
+    }
+    return c;
+}
+
+// warp-uniform loop over the rays [0, n): static grid stride, or tiles pulled from a counter
+template <bool DYN, class F>
+__device__ __forceinline__ void for_each_ray(int n, int *work, int tile, F &&body)
+{
+    const int lane = threadIdx.x & 31;
+    if (!DYN) {
+        long long nw = (long long)gridDim.x * (blockDim.x >> 5);
+        long long w = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+        for (long long base = w * 32; base < n; base += nw * 32)
+            body((int)(base + lane), base + lane < n);
+    } else {
+        while (true) {
+            int start = 0;
+            if (lane == 0) start = atomicAdd(work, tile);
+            start = __shfl_sync(kFull, start, 0);
+            if (start >= n) break;
+            int end = min(start + tile, n);
+            for (int base = start; base < end; base += 32)
+                body(base + lane, base + lane < end);
+        }
+    }
+}
+
+__device__ __forceinline__ bool cancelled(const volatile int *cancel) { return cancel && *cancel; }
+
+// ---- ray generation (parallelRT, RayTracer.cpp:13-27) -------------------------------------
+__global__ void k_raygen(Wavefront wf)
+{
+    if (cancelled(wf.cancel)) return;
+    const long long total = *wf.total_samples, first = *wf.sample_offset;
+    const RayQueue q = wf.q[0];
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        wf.C->q_count[0] = (int)min(total, (long long)q.capacity);
+        wf.C->rays_primary = (unsigned long long)total;
+        if (total > q.capacity) atomicExch(&wf.C->overflow, 1);
+    }
+    for (long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x; g < total && g < q.capacity;
+         g += (long long)gridDim.x * blockDim.x) {
+        const long long gs = first + g;
+        int lo = 0, hi = (int)*wf.n_jobs - 1;
+        while (lo < hi) {
+            int mid = (lo + hi) >> 1;
+            if (wf.job_sample_end[mid] > gs) hi = mid;
+            else lo = mid + 1;
+        }
+        const DevJob &J = wf.jobs[lo];
+        long long local = gs - J.sample_base;
+        long long p = local / J.spp;
+        int s = (int)(local - p * J.spp);
+        int row = (int)(p / J.xlim), col = (int)(p - (long long)row * J.xlim);
+        int xcur = col - J.width / 2, ycur = row - J.height / 2;
+        float a, b;
+        if (J.spp > 1) {   // sub-pixel jitter in [0,1) from a per-pixel Philox stream
+            unsigned pix = (unsigned)(row * J.width + col);
+            uint4 r = philox4x32_10(make_uint4(pix, 0u, (unsigned)s, 0u),
+                                    make_uint2((unsigned)J.seed, (unsigned)(J.seed >> 32)));
+            double jx = (double)(r.x >> 8) * (1.0 / 16777216.0), jy = (double)(r.y >> 8) * (1.0 / 16777216.0);
+            a = __double2float_rn(((double)xcur + jx) * J.dp);
+            b = __double2float_rn(((double)ycur + jy) * J.dp);
+        } else {
+            a = __double2float_rn((double)xcur * J.dp);
+            b = __double2float_rn((double)ycur * J.dp);
+        }
+        V3 n = mk(J.cam_n[0], J.cam_n[1], J.cam_n[2]);
+        V3 u = mk(J.cam_u[0], J.cam_u[1], J.cam_u[2]);
+        V3 v = mk(J.cam_v[0], J.cam_v[1], J.cam_v[2]);
+        V3 dir = normalise(vadd(vadd(n, vscale(u, a)), vscale(v, b)));
+        int pixel = row * J.width + col;
+        q.o[g] = make_float4(J.cam_pos[0], J.cam_pos[1], J.cam_pos[2], 1.0f);
+        q.d[g] = make_float4(dir.x, dir.y, dir.z, 1.0f);
+        q.w[g] = make_float4(1.0f, 1.0f, 1.0f, __int_as_float(pixel));
+        q.m[g] = make_int4(-1, ray_flags(0, kRayBase, 0, s == 0 && J.plane_obj != nullptr), -1, lo);
+    }
+}
+
+// ---- extend: closest hit -------------------------------------------------------------------
+template <int STACK, bool DYN, bool COUNT>
+__global__ void __launch_bounds__(256) k_extend(Wavefront wf, int sel, int wslot, int tile)
+{
+    Counters *C = wf.C;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {   // the next queue and the shadow queue fill in shade
+        C->q_count[sel ^ 1] = 0;
+        C->s_count = 0;
+    }
+    if (cancelled(wf.cancel)) return;
+    const RayQueue q = wf.q[sel];
+    const int n = min(C->q_count[sel], q.capacity);
+    WorkCount wc{0, 0, 0, 0};
+    for_each_ray<DYN>(n, &C->work[wslot], tile, [&](int i, bool active) {
+        if (!active) return;
+        float4 o4 = q.o[i], d4 = q.d[i];
+        int4 m4 = q.m[i];
+        const DevScene &S = wf.scenes[wf.jobs[m4.w].scene];
+        Best best;
+        int newobj;
+        closest_hit<STACK, COUNT>(S, mk(o4), mk(d4), m4.x, ray_inside(m4.y) != 0, best, newobj, wc);
+        wf.hit[i] = make_float4(best.t, best.u, best.v, __int_as_float(best.key));
+        wf.newobj[i] = newobj;
+    });
+    if (wc.err) atomicOr(&C->error, wc.err);
+    if (COUNT) {
+        for (int off = 16; off > 0; off >>= 1) {
+            wc.nodes += __shfl_down_sync(kFull, wc.nodes, off);
+            wc.tris += __shfl_down_sync(kFull, wc.tris, off);
+            wc.spheres += __shfl_down_sync(kFull, wc.spheres, off);
+        }
+        if ((threadIdx.x & 31) == 0) {
+            atomicAdd(&C->nodes, (unsigned long long)wc.nodes);
+            atomicAdd(&C->tris, (unsigned long long)wc.tris);
+            atomicAdd(&C->spheres, (unsigned long long)wc.spheres);
+        }
+    }
+}
+
+// texture colour: nearest texel, wrapped, BGR bytes (Color(Texture*,Coord2D), 3DElement.cpp:430-450)
+__device__ V3 tex_color(const DevScene &S, int tex, float u, float v)
+{
+    const DevTexture T = S.tex[tex];
+    float ip;
+    float nu = modff(u, &ip), nv = modff(v, &ip);
+    if (nu < 0) nu = __fadd_rn(nu, 1.0f);
+    if (nv < 0) nv = __fadd_rn(nv, 1.0f);
+    float fx = __fmul_rn(nu, (float)T.w), fy = __fmul_rn(nv, (float)T.h);
+    int x = fx == fx ? (int)(short)(int)fx : 0, y = fy == fy ? (int)(short)(int)fy : 0;
+    long long off = ((long long)y * T.w + x) * 3, last = ((long long)T.w * T.h - 1) * 3;
+    off = off > last ? last : (off < 0 ? 0 : off);
+    const uint8_t *t = S.texels + T.offset + off;
+    return mk(__fdiv_rn((float)t[2], 255.0f), __fdiv_rn((float)t[1], 255.0f), __fdiv_rn((float)t[0], 255.0f));
+}
+
+// light terms of one light at P (RayTracer.cpp:482-503)
+struct LightTerm {
+    V3 p2l;
+    float dis, lum;
+    bool point;
+};
+__device__ __forceinline__ LightTerm light_term(const DevLight &L, V3 P)
+{
+    LightTerm r;
+    if (L.type == 2) {   // MY_LIGHT_POINT
+        V3 p2l_v = vsub(mk(L.pos[0], L.pos[1], L.pos[2]), P);
+        float d2 = dot3(p2l_v, p2l_v);
+        float step = __fadd_rn(L.att[0], __fmul_rn(L.att[2], d2));
+        r.dis = __fsqrt_rn(d2);
+        step = __fadd_rn(step, __fmul_rn(L.att[1], r.dis));
+        r.lum = __fdiv_rn(1.0f, step);
+        r.p2l = normalise(p2l_v);
+        r.point = true;
+    } else {
+        r.dis = 1e10f;
+        r.lum = 1.0f;
+        r.p2l = normalise(mk(L.pos[0], L.pos[1], L.pos[2]));
+        r.point = false;
+    }
+    return r;
+}
+
+// ---- shade ------------------------------------------------------------------------------------
+template <bool DYN>
+__global__ void __launch_bounds__(256) k_shade(Wavefront wf, int sel, int wslot, int tile)
+{
+    if (cancelled(wf.cancel)) return;
+    Counters *C = wf.C;
+    const RayQueue q = wf.q[sel], qo = wf.q[sel ^ 1];
+    const ShadowQueue sq = wf.sq;
+    const int n = min(C->q_count[sel], q.capacity);
+    const int lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1u;
+    for_each_ray<DYN>(n, &C->work[wslot], tile, [&](int i, bool active) {
+        bool emit = false;
+        int nchild = 0;
+        float4 c_o[2], c_d[2], c_w[2];
+        int4 c_m[2];
+        float4 s_p, s_n, s_v, s_wc, s_ws;
+        if (active) {
+            const float4 o4 = q.o[i], d4 = q.d[i], w4 = q.w[i];
+            const int4 m4 = q.m[i];
+            const float4 h4 = wf.hit[i];
+            const int nob = wf.newobj[i];
+            const DevJob &J = wf.jobs[m4.w];
+            const DevScene &S = wf.scenes[J.scene];
+            const int flags = m4.y, level = ray_level(flags), type = ray_type(flags), inside = ray_inside(flags);
+            const float t = h4.x;
+            const int key = __float_as_int(h4.w);
+            const int pix = __float_as_int(w4.w);
+            const bool is_tri = key >= 0 && (key & kTriFlag);
+            const DevPrim *pr = (key >= 0 && !is_tri) ? &S.prims[key] : nullptr;
+            const int tk = key & ~kTriFlag;
+            if (ray_plane(flags)) {
+                int obj = -1, prim = 0;
+                if (is_tri) {
+                    obj = __float_as_int(S.tri[3 * tk + 1].w);
+                    prim = __float_as_int(S.tri[3 * tk].w);
+                } else if (pr)
+                    obj = pr->obj, prim = pr->sub;
+                J.plane_obj[pix] = obj;
+                J.plane_prim[pix] = prim;
+                J.plane_t[pix] = key >= 0 ? t : kMiss;
+            }
+            const float znear = level == 0 ? J.znear : 0.0f;
+            if (key >= 0 && !(t > J.zfar || t < znear)) {
+                const V3 O = mk(o4), D = mk(d4);
+                const V3 P = vadd(O, vscale(D, t));
+                int mtl_id, tex = -1, hit_inside = 0;
+                float hit_rfr = 1.0f, tu = 0.0f, tv = 0.0f;
+                V3 N;
+                if (is_tri) {
+                    const float4 e2 = S.tri[3 * tk + 2];
+                    mtl_id = __float_as_int(e2.w);
+                    const float u = h4.y, v = h4.z, w = __fsub_rn(__fsub_rn(1.0f, u), v);
+                    V3 n0 = mk(S.trin[3 * tk]), n1 = mk(S.trin[3 * tk + 1]), n2 = mk(S.trin[3 * tk + 2]);
+                    N = normalise(vadd(vadd(vscale(n0, w), vscale(n1, u)), vscale(n2, v)));
+                    const DevMaterial &M = S.mtl[mtl_id];
+                    hit_rfr = M.rfr;
+                    tex = M.tex;
+                    if (tex >= 0 && S.triuv) {
+                        float2 a = S.triuv[3 * tk], b = S.triuv[3 * tk + 1], c = S.triuv[3 * tk + 2];
+                        tu = __fadd_rn(__fadd_rn(__fmul_rn(a.x, w), __fmul_rn(b.x, u)), __fmul_rn(c.x, v));
+                        tv = __fadd_rn(__fadd_rn(__fmul_rn(a.y, w), __fmul_rn(b.y, u)), __fmul_rn(c.y, v));
+                    }
+                } else {
+                    mtl_id = pr->mtl;
+                    const DevMaterial &M = S.mtl[mtl_id];
+                    if (pr->type == kPrimSphere) {
+                        const V3 Cc = mk(pr->a);
+                        if (key == m4.x) {   // own sphere from inside (the only way key == excl)
+                            N = normalise(vsub(Cc, P));
+                            hit_rfr = type == kRayRefract ? 1.0f : M.rfr;
+                        } else {
+                            N = normalise(vsub(P, Cc));
+                            hit_rfr = M.rfr;
+                        }
+                        hit_inside = inside ? 0 : 0xff;
+                    } else if (pr->type == kPrimPlane) {
+                        N = mk(pr->b);
+                        tex = pr->tex;
+                        if (tex >= 0) {
+                            const V3 ax = mk(pr->c), ay = mk(pr->d);
+                            const V3 p2r = vsub(O, mk(pr->a));
+                            const V3 tmp1 = cross3(D, ay);
+                            const float f = __fdiv_rn(__fdiv_rn(1.0f, dot3(ax, tmp1)), 5.0f);
+                            tu = __fmul_rn(dot3(p2r, tmp1), f);
+                            tv = __fmul_rn(dot3(D, cross3(p2r, ax)), f);
+                        }
+                    } else {   // box face normal (Basic3DObject.cpp:285-293)
+                        const V3 b2p = vsub(P, mk(pr->c)), mx = mk(pr->d);
+                        V3 pt = mk(0.0f, 0.0f, 0.0f);
+                        if (fabsf(__fsub_rn(fabsf(b2p.z), mx.z)) <= kEps6) pt.z = b2p.z > 0 ? 1.0f : -1.0f;
+                        if (fabsf(__fsub_rn(fabsf(b2p.y), mx.y)) <= kEps6) pt.y = b2p.y > 0 ? 1.0f : -1.0f;
+                        if (fabsf(__fsub_rn(fabsf(b2p.x), mx.x)) <= kEps6) pt.x = b2p.x > 0 ? 1.0f : -1.0f;
+                        N = normalise(pt);
+                    }
+                }
+                const DevMaterial &M = S.mtl[mtl_id];
+                const V3 vc = tex >= 0 ? tex_color(S, tex, tu, tv) : mk(1.0f, 1.0f, 1.0f);
+                V3 W = mk(w4);
+                if (m4.z >= 0) {   // Beer factor of a refracted parent that entered a sphere
+                    const DevMaterial &B = S.mtl[m4.z];
+                    W.x = __fmul_rn(W.x, expf(__fmul_rn(__fmul_rn(B.kd[0], 0.15f), -t)));
+                    W.y = __fmul_rn(W.y, expf(__fmul_rn(__fmul_rn(B.kd[1], 0.15f), -t)));
+                    W.z = __fmul_rn(W.z, expf(__fmul_rn(__fmul_rn(B.kd[2], 0.15f), -t)));
+                }
+                const bool refl = M.reflect > 0.01f, refr = M.refract > 0.01f;
+                const float a1 = refl ? __fsub_rn(1.0f, M.reflect) : 1.0f;
+                const float a2 = refr ? __fsub_rn(1.0f, M.refract) : 1.0f;
+                const V3 Wl = vscale(W, __fmul_rn(a1, a2));
+                // ambient: environment plus every switched-on light, shadowed or not
+                const V3 ka = mk(M.ka[0], M.ka[1], M.ka[2]);
+                V3 mix_va = vmul(ka, mk(S.env[0], S.env[1], S.env[2]));
+                int lights_on = 0;
+                for (int l = 0; l < S.n_lights; ++l) {
+                    const DevLight &L = S.lights[l];
+                    if (!L.on) continue;
+                    ++lights_on;
+                    float lum = 1.0f;
+                    if (L.type == 2) lum = light_term(L, P).lum;
+                    const V3 la = L.type == 2 ? vscale(mk(L.amb[0], L.amb[1], L.amb[2]), lum) : mk(L.amb[0], L.amb[1], L.amb[2]);
+                    mix_va = vadd(mix_va, vmul(ka, la));
+                }
+                const V3 Wc = vmul(Wl, vc);
+                acc_add(J.acc, pix, vmul(Wc, mix_va));
+                if (lights_on > 0) {
+                    emit = true;
+                    s_p = make_float4(P.x, P.y, P.z, __int_as_float(pix));
+                    s_n = make_float4(N.x, N.y, N.z, __int_as_float(mtl_id));
+                    s_v = make_float4(D.x, D.y, D.z, __int_as_float(nob));
+                    s_wc = make_float4(Wc.x, Wc.y, Wc.z, __int_as_float(m4.w));
+                    s_ws = make_float4(Wl.x, Wl.y, Wl.z, 0.0f);
+                }
+                const float bwc = o4.w;
+                if (refl && level + 1 <= J.max_level) {
+                    const float r = M.reflect, bc = __fmul_rn(bwc, r);
+                    if (!(bc < 1e-5f)) {
+                        const float nn = __fmul_rn(2.0f, dot3(D, N));
+                        const V3 R = normalise(vsub(D, vscale(N, nn)));
+                        const V3 Wr = vscale(W, __fmul_rn(r, a2));
+                        c_o[nchild] = make_float4(P.x, P.y, P.z, bc);
+                        c_d[nchild] = make_float4(R.x, R.y, R.z, 1.0f);
+                        c_w[nchild] = make_float4(Wr.x, Wr.y, Wr.z, __int_as_float(pix));
+                        c_m[nchild] = make_int4(nob, ray_flags(level + 1, kRayReflect, 0, 0), -1, m4.w);
+                        ++nchild;
+                    }
+                }
+                if (refr && level + 1 <= J.max_level) {
+                    const float f = M.refract;
+                    const float eta = __fdiv_rn(d4.w, hit_rfr);
+                    const float cosIn = -dot3(D, N);
+                    const float cosOut2 =
+                        __fsub_rn(1.0f, __fmul_rn(__fmul_rn(eta, eta), __fsub_rn(1.0f, __fmul_rn(cosIn, cosIn))));
+                    const float bc = __fmul_rn(bwc, f);
+                    if (!(cosOut2 < 0.0f) && !(bc < 1e-5f)) {
+                        const V3 l2 = vscale(D, eta);
+                        const V3 l1 = vscale(N, __fsub_rn(__fmul_rn(eta, cosIn), __fsqrt_rn(cosOut2)));
+                        const V3 T = normalise(vadd(l1, l2));
+                        const V3 Wt = vscale(W, f);
+                        c_o[nchild] = make_float4(P.x, P.y, P.z, bc);
+                        c_d[nchild] = make_float4(T.x, T.y, T.z, hit_rfr);
+                        c_w[nchild] = make_float4(Wt.x, Wt.y, Wt.z, __int_as_float(pix));
+                        c_m[nchild] = make_int4(nob, ray_flags(level + 1, kRayRefract, hit_inside, 0), hit_inside ? mtl_id : -1,
+                                                m4.w);
+                        ++nchild;
+                    }
+                }
+            }
+        }
+        // warp-aggregated appends: one atomic per warp for the shadow queue and one for the rays
+        const unsigned bs = __ballot_sync(kFull, emit);
+        if (bs) {
+            int base = 0;
+            if (lane == 0) base = atomicAdd(&C->s_count, __popc(bs));
+            base = __shfl_sync(kFull, base, 0);
+            if (emit) {
+                const int slot = base + __popc(bs & lt);
+                if (slot < sq.capacity) {
+                    sq.p[slot] = s_p;
+                    sq.n[slot] = s_n;
+                    sq.v[slot] = s_v;
+                    sq.wc[slot] = s_wc;
+                    sq.ws[slot] = s_ws;
+                } else
+                    atomicExch(&C->overflow, 1);
+            }
+        }
+        const unsigned b1 = __ballot_sync(kFull, nchild >= 1), b2 = __ballot_sync(kFull, nchild == 2);
+        const int tot = __popc(b1) + __popc(b2);
+        if (tot) {
+            int base = 0;
+            if (lane == 0) {
+                base = atomicAdd(&C->q_count[sel ^ 1], tot);
+                atomicAdd(&C->rays_secondary, (unsigned long long)tot);
+            }
+            base = __shfl_sync(kFull, base, 0);
+            const int off = base + __popc(b1 & lt) + __popc(b2 & lt);
+            for (int c = 0; c < nchild; ++c) {
+                const int slot = off + c;
+                if (slot < qo.capacity) {
+                    qo.o[slot] = c_o[c];
+                    qo.d[slot] = c_d[c];
+                    qo.w[slot] = c_w[c];
+                    qo.m[slot] = c_m[c];
+                } else
+                    atomicExch(&C->overflow, 1);
+            }
+        }
+    });
+}
+
+// ---- shadow: per-light any-hit + direct light ---------------------------------------------------
+template <int STACK, bool DYN, bool COUNT>
+__global__ void __launch_bounds__(256) k_shadow(Wavefront wf, int wslot, int tile)
+{
+    if (cancelled(wf.cancel)) return;
+    Counters *C = wf.C;
+    const ShadowQueue sq = wf.sq;
+    const int n = min(C->s_count, sq.capacity);
+    WorkCount wc{0, 0, 0, 0};
+    unsigned long long rays = 0;
+    for_each_ray<DYN>(n, &C->work[wslot], tile, [&](int i, bool active) {
+        if (!active) return;
+        const float4 p4 = sq.p[i], n4 = sq.n[i], v4 = sq.v[i], wc4 = sq.wc[i], ws4 = sq.ws[i];
+        const DevJob &J = wf.jobs[__float_as_int(wc4.w)];
+        const DevScene &S = wf.scenes[J.scene];
+        const DevMaterial &M = S.mtl[__float_as_int(n4.w)];
+        const V3 P = mk(p4), N = mk(n4), D = mk(v4), Wc = mk(wc4), Ws = mk(ws4);
+        const int excl = __float_as_int(v4.w);
+        V3 sum = mk(0.0f, 0.0f, 0.0f);
+        for (int l = 0; l < S.n_lights; ++l) {
+            const DevLight &L = S.lights[l];
+            if (!L.on) continue;
+            ++rays;
+            const LightTerm lt = light_term(L, P);
+            if (any_hit<STACK, COUNT>(S, P, lt.p2l, lt.dis, excl, wc)) continue;
+            V3 ld = mk(L.dif[0], L.dif[1], L.dif[2]), ls = mk(L.spec[0], L.spec[1], L.spec[2]);
+            if (lt.point) ld = vscale(ld, lt.lum), ls = vscale(ls, lt.lum);
+            float nn = dot3(N, lt.p2l);
+            if (nn > 0) sum = vadd(sum, vmul(Wc, vscale(vmul(mk(M.kd[0], M.kd[1], M.kd[2]), ld), nn)));
+            const V3 h = normalise(vsub(lt.p2l, D));
+            nn = dot3(N, h);
+            if (nn > 0) sum = vadd(sum, vmul(Ws, vscale(vmul(mk(M.ks[0], M.ks[1], M.ks[2]), ls), powf(nn, M.shininess))));
+        }
+        acc_add(J.acc, __float_as_int(p4.w), sum);
+    });
+    if (wc.err) atomicOr(&C->error, wc.err);
+    for (int off = 16; off > 0; off >>= 1) rays += __shfl_down_sync(kFull, rays, off);
+    if ((threadIdx.x & 31) == 0 && rays) atomicAdd(&C->rays_shadow, rays);
+    if (COUNT) {
+        for (int off = 16; off > 0; off >>= 1) {
+            wc.nodes += __shfl_down_sync(kFull, wc.nodes, off);
+            wc.tris += __shfl_down_sync(kFull, wc.tris, off);
+            wc.spheres += __shfl_down_sync(kFull, wc.spheres, off);
+        }
+        if ((threadIdx.x & 31) == 0) {
+            atomicAdd(&C->nodes, (unsigned long long)wc.nodes);
+            atomicAdd(&C->tris, (unsigned long long)wc.tris);
+            atomicAdd(&C->spheres, (unsigned long long)wc.spheres);
+        }
+    }
+}
+
+// ---- resolve: fixed point -> float rgb and Color::put bytes ---------------------------------------
+__device__ __forceinline__ uint8_t put_channel(float c)
+{
+    if (c > 1.0f) return 255;
+    if (c < 0.0f || c != c) return 0;
+    return (uint8_t)(int)(c * 255);
+}
+__global__ void k_resolve(FrameBufs fb, long long npix, int spp)
+{
+    const double scale = 1.0 / 4294967296.0 / (double)spp;
+    for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < npix; p += (long long)gridDim.x * blockDim.x) {
+        float c[3];
+        for (int k = 0; k < 3; ++k) c[k] = (float)((double)fb.acc[3 * p + k] * scale);
+        if (fb.rgb) {
+            fb.rgb[3 * p] = c[0];
+            fb.rgb[3 * p + 1] = c[1];
+            fb.rgb[3 * p + 2] = c[2];
+        }
+        if (fb.rgb8) {
+            fb.rgb8[3 * p] = put_channel(c[0]);
+            fb.rgb8[3 * p + 1] = put_channel(c[1]);
+            fb.rgb8[3 * p + 2] = put_channel(c[2]);
+        }
+    }
+}
+
+__global__ void k_plane_init(FrameBufs fb, long long npix)
+{
+    for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < npix; p += (long long)gridDim.x * blockDim.x) {
+        fb.plane_obj[p] = -1;
+        fb.plane_prim[p] = 0;
+        fb.plane_t[p] = kMiss;
+    }
+}
+
+// ---- launchers ------------------------------------------------------------------------------------
+int sm_count()
+{
+    static int n = 0;
+    if (!n) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        if (n <= 0) n = 1;
+    }
+    return n;
+}
+
+static int grid_for(const Tuning &t, const void *kernel)
+{
+    if (t.grid > 0) return t.grid;
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, t.block, 0);
+    if (per_sm <= 0) per_sm = 1;
+    return sm_count() * per_sm;
+}
+
+void launch_raygen(const Wavefront &wf, int grid, int block, cudaStream_t s)
+{
+    k_raygen<<<grid, block, 0, s>>>(wf);
+}
+
+template <int STACK>
+static void extend_stack(const Wavefront &wf, int sel, int wslot, const Tuning &t, cudaStream_t s)
+{
+#define RT_EXT(DYN, CNT)                                                                                          \
+    {                                                                                                             \
+        auto k = k_extend<STACK, DYN, CNT>;                                                                       \
+        k<<<grid_for(t, (const void *)k), t.block, 0, s>>>(wf, sel, wslot, t.tile);                              \
+    }
+    if (t.dynamic) {
+        if (t.count) RT_EXT(true, true) else RT_EXT(true, false)
+    } else {
+        if (t.count) RT_EXT(false, true) else RT_EXT(false, false)
+    }
+#undef RT_EXT
+}
+
+void launch_extend(const Wavefront &wf, int sel, int level, const Tuning &t, cudaStream_t s)
+{
+    const int wslot = 3 * level;
+    if (t.stack <= 32) extend_stack<32>(wf, sel, wslot, t, s);
+    else extend_stack<64>(wf, sel, wslot, t, s);
+}
+
+void launch_shade(const Wavefront &wf, int sel, int level, const Tuning &t, cudaStream_t s)
+{
+    const int wslot = 3 * level + 1;
+    if (t.dynamic) {
+        auto k = k_shade<true>;
+        k<<<grid_for(t, (const void *)k), t.block, 0, s>>>(wf, sel, wslot, t.tile);
+    } else {
+        auto k = k_shade<false>;
+        k<<<grid_for(t, (const void *)k), t.block, 0, s>>>(wf, sel, wslot, t.tile);
+    }
+}
+
+template <int STACK>
+static void shadow_stack(const Wavefront &wf, int wslot, const Tuning &t, cudaStream_t s)
+{
+#define RT_SHD(DYN, CNT)                                                                                          \
+    {                                                                                                             \
+        auto k = k_shadow<STACK, DYN, CNT>;                                                                       \
+        k<<<grid_for(t, (const void *)k), t.block, 0, s>>>(wf, wslot, t.tile);                                   \
+    }
+    if (t.dynamic) {
+        if (t.count) RT_SHD(true, true) else RT_SHD(true, false)
+    } else {
+        if (t.count) RT_SHD(false, true) else RT_SHD(false, false)
+    }
+#undef RT_SHD
+}
+
+void launch_shadow(const Wavefront &wf, int level, const Tuning &t, cudaStream_t s)
+{
+    const int wslot = 3 * level + 2;
+    if (t.stack <= 32) shadow_stack<32>(wf, wslot, t, s);
+    else shadow_stack<64>(wf, wslot, t, s);
+}
+
+void launch_resolve(const FrameBufs &fb, int width, int height, int spp, cudaStream_t s)
+{
+    long long npix = (long long)width * height;
+    int grid = (int)std::min<long long>((npix + 255) / 256, (long long)sm_count() * 8);
+    if (grid < 1) grid = 1;
+    k_resolve<<<grid, 256, 0, s>>>(fb, npix, spp);
+}
+
+void launch_plane_init(const FrameBufs &fb, long long npix, cudaStream_t s)
+{
+    int grid = (int)std::min<long long>((npix + 255) / 256, (long long)sm_count() * 8);
+    if (grid < 1) grid = 1;
+    k_plane_init<<<grid, 256, 0, s>>>(fb, npix);
+}
+
+} // namespace rtg

@@ -1,0 +1,53 @@
+// rt_kernels.cuh — launch interface of the wavefront kernels (rt_kernels.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+#include "rt_device.cuh"
+
+namespace rtg {
+
+// per-frame device buffers
+struct FrameBufs {
+    long long *acc;     // 3 x int64 fixed point (2^-32) per pixel
+    float *rgb;         // 3 floats per pixel
+    uint8_t *rgb8;      // 3 bytes per pixel
+    int *plane_obj;     // primary hit object, sample 0
+    int *plane_prim;
+    float *plane_t;
+};
+
+// everything one wavefront pass needs
+struct Wavefront {
+    const DevScene *scenes;
+    const DevJob *jobs;
+    const long long *job_sample_end;  // inclusive prefix of samples per job (device)
+    const long long *total_samples;   // device scalar: samples in this wave
+    const long long *sample_offset;   // device scalar: global index of the wave's first sample
+    const long long *n_jobs;          // device scalar: jobs in the job table
+    RayQueue q[2];
+    ShadowQueue sq;
+    float4 *hit;
+    int *newobj;
+    Counters *C;
+    const volatile int *cancel;       // host-mapped cancel flag (may be NULL)
+};
+
+struct Tuning {
+    int block = 128;     // threads per block of the traversal kernels
+    int tile = 256;      // rays per dynamic work fetch (multiple of 32)
+    int stack = 64;      // traversal stack entries
+    bool dynamic = false;// persistent grid pulling tiles from a global counter
+    bool count = false;  // count BVH nodes / triangles / spheres
+    int grid = 0;        // blocks (0 = derived from the SM count)
+};
+
+int sm_count();
+// kernels of one level; `sel` picks the input ray queue
+void launch_raygen(const Wavefront &wf, int grid, int block, cudaStream_t s);
+void launch_extend(const Wavefront &wf, int sel, int level, const Tuning &t, cudaStream_t s);
+void launch_shade(const Wavefront &wf, int sel, int level, const Tuning &t, cudaStream_t s);
+void launch_shadow(const Wavefront &wf, int level, const Tuning &t, cudaStream_t s);
+void launch_resolve(const FrameBufs &fb, int width, int height, int spp, cudaStream_t s);
+void launch_plane_init(const FrameBufs &fb, long long npix, cudaStream_t s);
+
+} // namespace rtg

@@ -1,0 +1,397 @@
+// rt_lbvh.cu — device-built LBVH, replacing the reference's per-frame octant binning
+// (Model::RTPrepare, Model.cpp:402-480) and its brute-force octant lists (Model.cpp:748-811).
+//
+//   1. prep     per-triangle world box (p0+position, p0+e1, p0+e2) and centroid; the scene
+//               box of all triangles by a block-reduced atomic min/max on order-preserving ints
+//   2. morton   30-bit codes: 10 bits per axis of the centroid inside the scene box
+//   3. sort     stable LSD radix sort of (code, index), 8-bit digits, 4 passes; each pass is a
+//               per-tile digit histogram, one exclusive scan over (digit, tile), and a scatter
+//               that ranks keys inside a tile with __match_any_sync so equal digits keep order
+//   4. gather   triangles reordered to Morton order (p0|id, e1|obj, e2|mtl) and padded leaf boxes
+//   5. karras   hierarchy from the sorted codes (Karras 2012), ties broken by index
+//   6. refit    bottom-up boxes: the second child to arrive at a node (atomic counter) writes
+//               the union of its children and moves up
+// Nodes are 32 bytes: float4(min.xyz, left) and float4(max.xyz, right); internal nodes are
+// 0..n-2, leaf k is node n-1+k.
+#include <algorithm>
+
+#include "rt_lbvh.cuh"
+
+namespace rtg {
+
+namespace {
+
+constexpr int kTileKeys = 2048;   // keys per radix tile (256 threads x 8)
+constexpr int kSortThreads = 256;
+
+__device__ __forceinline__ unsigned f2ord(float f)
+{
+    unsigned u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float ord2f(unsigned u)
+{
+    return __uint_as_float((u & 0x80000000u) ? (u & 0x7fffffffu) : ~u);
+}
+
+struct TriWorld {
+    float p0[3], e1[3], e2[3], mn[3], mx[3];
+};
+
+__device__ __forceinline__ TriWorld tri_world(const LbvhInput &in, int i)
+{
+    TriWorld w;
+    const float *p = in.tri_p + 9ll * i;
+    const float *pos = in.obj_pos + 3ll * in.tri_obj[i];
+    for (int k = 0; k < 3; ++k) {
+        w.p0[k] = __fadd_rn(p[k], pos[k]);           // clTri::p0 = p0 + position
+        w.e1[k] = __fsub_rn(p[3 + k], p[k]);          // axisu = p1 - p0 (model space)
+        w.e2[k] = __fsub_rn(p[6 + k], p[k]);          // axisv = p2 - p0
+        float a = w.p0[k], b = __fadd_rn(w.p0[k], w.e1[k]), c = __fadd_rn(w.p0[k], w.e2[k]);
+        w.mn[k] = fminf(a, fminf(b, c));
+        w.mx[k] = fmaxf(a, fmaxf(b, c));
+    }
+    return w;
+}
+
+__global__ void k_prep(LbvhInput in, float4 *centroid, unsigned *box)
+{
+    __shared__ unsigned smn[3], smx[3];
+    if (threadIdx.x < 3) smn[threadIdx.x] = 0xffffffffu, smx[threadIdx.x] = 0u;
+    __syncthreads();
+    unsigned lmn[3] = {0xffffffffu, 0xffffffffu, 0xffffffffu}, lmx[3] = {0u, 0u, 0u};
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < in.n; i += gridDim.x * blockDim.x) {
+        TriWorld w = tri_world(in, i);
+        float c[3];
+        for (int k = 0; k < 3; ++k) {
+            c[k] = __fmul_rn(__fadd_rn(w.mn[k], w.mx[k]), 0.5f);
+            lmn[k] = min(lmn[k], f2ord(w.mn[k]));
+            lmx[k] = max(lmx[k], f2ord(w.mx[k]));
+        }
+        centroid[i] = make_float4(c[0], c[1], c[2], 0.0f);
+    }
+    for (int k = 0; k < 3; ++k) {
+        for (int off = 16; off > 0; off >>= 1) {
+            lmn[k] = min(lmn[k], __shfl_xor_sync(0xffffffffu, lmn[k], off));
+            lmx[k] = max(lmx[k], __shfl_xor_sync(0xffffffffu, lmx[k], off));
+        }
+        if ((threadIdx.x & 31) == 0) {
+            atomicMin(&smn[k], lmn[k]);
+            atomicMax(&smx[k], lmx[k]);
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < 3) {
+        atomicMin(&box[threadIdx.x], smn[threadIdx.x]);
+        atomicMax(&box[3 + threadIdx.x], smx[threadIdx.x]);
+    }
+}
+
+__device__ __forceinline__ unsigned expand10(unsigned v)
+{
+    v &= 0x3ffu;
+    v = (v * 0x00010001u) & 0xFF0000FFu;
+    v = (v * 0x00000101u) & 0x0F00F00Fu;
+    v = (v * 0x00000011u) & 0xC30C30C3u;
+    v = (v * 0x00000005u) & 0x49249249u;
+    return v;
+}
+
+__global__ void k_morton(int n, const float4 *centroid, const unsigned *box, unsigned *codes, unsigned *idx)
+{
+    float mn[3], scale[3];
+    for (int k = 0; k < 3; ++k) {
+        mn[k] = ord2f(box[k]);
+        float ext = __fsub_rn(ord2f(box[3 + k]), mn[k]);
+        scale[k] = ext > 0.0f ? __fdiv_rn(1024.0f, ext) : 0.0f;
+    }
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        float4 c = centroid[i];
+        float cc[3] = {c.x, c.y, c.z};
+        unsigned q[3];
+        for (int k = 0; k < 3; ++k) {
+            float f = __fmul_rn(__fsub_rn(cc[k], mn[k]), scale[k]);
+            int qi = (int)f;
+            q[k] = (unsigned)min(max(qi, 0), 1023);
+        }
+        codes[i] = (expand10(q[0]) << 2) | (expand10(q[1]) << 1) | expand10(q[2]);
+        idx[i] = (unsigned)i;
+    }
+}
+
+// ---- radix sort --------------------------------------------------------------------------------
+__global__ void __launch_bounds__(kSortThreads) k_hist(int n, const unsigned *keys, int shift, unsigned *hist, int tiles)
+{
+    __shared__ unsigned h[256];
+    h[threadIdx.x] = 0;
+    __syncthreads();
+    const int tile = blockIdx.x;
+    const int start = tile * kTileKeys;
+    for (int r = 0; r < kTileKeys / kSortThreads; ++r) {
+        int i = start + r * kSortThreads + threadIdx.x;
+        if (i < n) atomicAdd(&h[(keys[i] >> shift) & 0xffu], 1u);
+    }
+    __syncthreads();
+    hist[threadIdx.x * tiles + tile] = h[threadIdx.x];
+}
+
+// exclusive scan of m values in one block of 1024 threads (chunked)
+__global__ void __launch_bounds__(1024) k_scan(unsigned *a, int m)
+{
+    __shared__ unsigned sums[1024];
+    const int per = (m + 1023) / 1024;
+    const int b = threadIdx.x * per, e = min(b + per, m);
+    unsigned s = 0;
+    for (int i = b; i < e; ++i) s += a[i];
+    sums[threadIdx.x] = s;
+    __syncthreads();
+    for (int off = 1; off < 1024; off <<= 1) {
+        unsigned v = threadIdx.x >= off ? sums[threadIdx.x - off] : 0u;
+        __syncthreads();
+        sums[threadIdx.x] += v;
+        __syncthreads();
+    }
+    unsigned run = sums[threadIdx.x] - s;
+    for (int i = b; i < e; ++i) {
+        unsigned v = a[i];
+        a[i] = run;
+        run += v;
+    }
+}
+
+__global__ void __launch_bounds__(kSortThreads) k_scatter(int n, const unsigned *kin, const unsigned *vin, unsigned *kout,
+                                                          unsigned *vout, int shift, const unsigned *hist, int tiles)
+{
+    __shared__ unsigned wcount[kSortThreads / 32][257];
+    __shared__ unsigned base[256];
+    __shared__ unsigned round_total[256];
+    const int tile = blockIdx.x, start = tile * kTileKeys;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1u;
+    base[threadIdx.x] = hist[threadIdx.x * tiles + tile];
+    for (int w = 0; w < kSortThreads / 32; ++w) wcount[w][threadIdx.x] = 0;
+    if (threadIdx.x == 0)
+        for (int w = 0; w < kSortThreads / 32; ++w) wcount[w][256] = 0;
+    __syncthreads();
+    for (int r = 0; r < kTileKeys / kSortThreads; ++r) {
+        const int i = start + r * kSortThreads + threadIdx.x;
+        const bool ok = i < n;
+        unsigned key = 0, val = 0, d = 256;
+        if (ok) {
+            key = kin[i];
+            val = vin[i];
+            d = (key >> shift) & 0xffu;
+        }
+        const unsigned peers = __match_any_sync(0xffffffffu, d);
+        const unsigned wrank = __popc(peers & lt);
+        if (wrank == 0) wcount[warp][d] = __popc(peers);
+        __syncthreads();
+        {   // exclusive prefix over warps for each digit
+            unsigned run = 0;
+            for (int w = 0; w < kSortThreads / 32; ++w) {
+                unsigned c = wcount[w][threadIdx.x];
+                wcount[w][threadIdx.x] = run;
+                run += c;
+            }
+            round_total[threadIdx.x] = run;
+        }
+        __syncthreads();
+        if (ok) {
+            const unsigned dst = base[d] + wcount[warp][d] + wrank;
+            kout[dst] = key;
+            vout[dst] = val;
+        }
+        __syncthreads();
+        base[threadIdx.x] += round_total[threadIdx.x];
+        for (int w = 0; w < kSortThreads / 32; ++w) wcount[w][threadIdx.x] = 0;
+        __syncthreads();
+    }
+}
+
+// ---- gather, hierarchy, refit -------------------------------------------------------------------
+__global__ void k_gather(LbvhInput in, LbvhOutput out, const unsigned *perm, const unsigned *box)
+{
+    const int n = in.n;
+    // absolute padding from the scene size: 2^-20 of its largest coordinate magnitude
+    float scene_mag = 0.0f;
+    for (int k = 0; k < 6; ++k) scene_mag = fmaxf(scene_mag, fabsf(ord2f(box[k])));
+    const float pad_abs = scene_mag * (1.0f / 1048576.0f);
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        const int i = (int)perm[k];
+        TriWorld w = tri_world(in, i);
+        out.tri[3ll * k] = make_float4(w.p0[0], w.p0[1], w.p0[2], __int_as_float(in.tri_id[i]));
+        out.tri[3ll * k + 1] = make_float4(w.e1[0], w.e1[1], w.e1[2], __int_as_float(in.tri_obj[i]));
+        out.tri[3ll * k + 2] = make_float4(w.e2[0], w.e2[1], w.e2[2], __int_as_float(in.tri_mtl[i]));
+        const float *nn = in.tri_n + 9ll * i;
+        for (int j = 0; j < 3; ++j) out.trin[3ll * k + j] = make_float4(nn[3 * j], nn[3 * j + 1], nn[3 * j + 2], 0.0f);
+        if (out.triuv) {
+            const float *uv = in.tri_uv ? in.tri_uv + 6ll * i : nullptr;
+            for (int j = 0; j < 3; ++j) out.triuv[3ll * k + j] = uv ? make_float2(uv[2 * j], uv[2 * j + 1]) : make_float2(0, 0);
+        }
+        // padded leaf box: the exact triangle test may accept a hit a few ulps outside
+        float mag = 0.0f, ext = 0.0f;
+        for (int j = 0; j < 3; ++j) {
+            mag = fmaxf(mag, fmaxf(fabsf(w.mn[j]), fabsf(w.mx[j])));
+            ext = fmaxf(ext, w.mx[j] - w.mn[j]);
+        }
+        const float pad = (mag + ext) * (1.0f / 65536.0f) + pad_abs;
+        const long long node = (long long)(n - 1) + k;
+        out.nodes[2 * node] = make_float4(w.mn[0] - pad, w.mn[1] - pad, w.mn[2] - pad, __int_as_float(-1));
+        out.nodes[2 * node + 1] = make_float4(w.mx[0] + pad, w.mx[1] + pad, w.mx[2] + pad, __int_as_float(-1));
+    }
+}
+
+__device__ __forceinline__ int delta(const unsigned *codes, int n, int i, int j)
+{
+    if (j < 0 || j >= n) return -1;
+    const unsigned a = codes[i], b = codes[j];
+    if (a != b) return __clz(a ^ b);
+    return 32 + __clz((unsigned)i ^ (unsigned)j);
+}
+
+__global__ void k_karras(int n, const unsigned *codes, float4 *nodes, int *parent)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n - 1; i += gridDim.x * blockDim.x) {
+        const int d = (delta(codes, n, i, i + 1) - delta(codes, n, i, i - 1)) >= 0 ? 1 : -1;
+        const int dmin = delta(codes, n, i, i - d);
+        int lmax = 2;
+        while (delta(codes, n, i, i + lmax * d) > dmin) lmax <<= 1;
+        int l = 0;
+        for (int t = lmax >> 1; t >= 1; t >>= 1)
+            if (delta(codes, n, i, i + (l + t) * d) > dmin) l += t;
+        const int j = i + l * d;
+        const int dnode = delta(codes, n, i, j);
+        int s = 0;
+        for (int div = 2;; div <<= 1) {
+            const int t = (l + div - 1) / div;
+            if (delta(codes, n, i, i + (s + t) * d) > dnode) s += t;
+            if (t <= 1) break;
+        }
+        const int gamma = i + s * d + min(d, 0);
+        const int left = (min(i, j) == gamma) ? (n - 1) + gamma : gamma;
+        const int right = (max(i, j) == gamma + 1) ? (n - 1) + gamma + 1 : gamma + 1;
+        nodes[2ll * i].w = __int_as_float(left);
+        nodes[2ll * i + 1].w = __int_as_float(right);
+        parent[left] = i;
+        parent[right] = i;
+        if (i == 0) parent[0] = -1;
+    }
+}
+
+__global__ void k_refit(int n, float4 *nodes, const int *parent, int *flags)
+{
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        int node = (n - 1) + k;
+        int p = parent[node];
+        for (int depth = 0; p >= 0 && p < n - 1 && depth < 128; ++depth) {
+            __threadfence();
+            if (atomicAdd(&flags[p], 1) == 0) break;   // first child: the sibling finishes the node
+            const float4 lo = nodes[2ll * p], hi = nodes[2ll * p + 1];
+            const int c0 = __float_as_int(lo.w), c1 = __float_as_int(hi.w);
+            const float4 a0 = __ldcg(&nodes[2ll * c0]), a1 = __ldcg(&nodes[2ll * c0 + 1]);
+            const float4 b0 = __ldcg(&nodes[2ll * c1]), b1 = __ldcg(&nodes[2ll * c1 + 1]);
+            __stcg(&nodes[2ll * p], make_float4(fminf(a0.x, b0.x), fminf(a0.y, b0.y), fminf(a0.z, b0.z), lo.w));
+            __stcg(&nodes[2ll * p + 1], make_float4(fmaxf(a1.x, b1.x), fmaxf(a1.y, b1.y), fmaxf(a1.z, b1.z), hi.w));
+            node = p;
+            p = parent[p];
+        }
+    }
+}
+
+struct Scratch {
+    unsigned *box;        // 8
+    float4 *centroid;     // n
+    unsigned *codes[2];   // n each
+    unsigned *idx[2];     // n each
+    unsigned *hist;       // 256 * tiles
+    int *parent;          // 2n - 1
+    int *flags;           // n - 1
+};
+
+size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+Scratch carve(void *base, int n)
+{
+    const int tiles = (n + kTileKeys - 1) / kTileKeys;
+    char *p = (char *)base;
+    Scratch s;
+    s.box = (unsigned *)p;
+    p += 256;
+    s.centroid = (float4 *)p;
+    p += align256(sizeof(float4) * (size_t)n);
+    for (int k = 0; k < 2; ++k) {
+        s.codes[k] = (unsigned *)p;
+        p += align256(4 * (size_t)n);
+        s.idx[k] = (unsigned *)p;
+        p += align256(4 * (size_t)n);
+    }
+    s.hist = (unsigned *)p;
+    p += align256(4 * 256 * (size_t)tiles);
+    s.parent = (int *)p;
+    p += align256(4 * (size_t)(2 * n));
+    s.flags = (int *)p;
+    return s;
+}
+
+int grid_of(long long n, int block)
+{
+    long long g = (n + block - 1) / block;
+    return (int)std::max<long long>(1, std::min<long long>(g, 65535));
+}
+
+// sorted codes end in codes[0] / idx[0] after an even number of passes
+cudaError_t morton_and_sort(const LbvhInput &in, const Scratch &sc, cudaStream_t s)
+{
+    const int n = in.n;
+    const int tiles = (n + kTileKeys - 1) / kTileKeys;
+    cudaMemsetAsync(sc.box, 0xff, 12, s);
+    cudaMemsetAsync(sc.box + 3, 0, 12, s);
+    k_prep<<<grid_of(n, 256), 256, 0, s>>>(in, sc.centroid, sc.box);
+    k_morton<<<grid_of(n, 256), 256, 0, s>>>(n, sc.centroid, sc.box, sc.codes[0], sc.idx[0]);
+    for (int pass = 0; pass < 4; ++pass) {
+        const int src = pass & 1, dst = src ^ 1;
+        k_hist<<<tiles, kSortThreads, 0, s>>>(n, sc.codes[src], 8 * pass, sc.hist, tiles);
+        k_scan<<<1, 1024, 0, s>>>(sc.hist, 256 * tiles);
+        k_scatter<<<tiles, kSortThreads, 0, s>>>(n, sc.codes[src], sc.idx[src], sc.codes[dst], sc.idx[dst], 8 * pass,
+                                                 sc.hist, tiles);
+    }
+    return cudaGetLastError();
+}
+
+} // namespace
+
+size_t lbvh_scratch_bytes(int n)
+{
+    const int tiles = (n + kTileKeys - 1) / kTileKeys;
+    return 256 + align256(sizeof(float4) * (size_t)n) + 4 * align256(4 * (size_t)n) + align256(4 * 256 * (size_t)tiles) +
+           align256(4 * (size_t)(2 * n)) + align256(4 * (size_t)n) + 256;
+}
+
+cudaError_t lbvh_morton_sort(const LbvhInput &in, uint32_t *codes_out, uint32_t *perm_out, void *scratch, cudaStream_t s)
+{
+    if (in.n <= 0) return cudaSuccess;
+    Scratch sc = carve(scratch, in.n);
+    cudaError_t e = morton_and_sort(in, sc, s);
+    if (e != cudaSuccess) return e;
+    cudaMemcpyAsync(codes_out, sc.codes[0], 4 * (size_t)in.n, cudaMemcpyDeviceToDevice, s);
+    cudaMemcpyAsync(perm_out, sc.idx[0], 4 * (size_t)in.n, cudaMemcpyDeviceToDevice, s);
+    return cudaGetLastError();
+}
+
+cudaError_t lbvh_build(const LbvhInput &in, const LbvhOutput &out, void *scratch, cudaStream_t s)
+{
+    const int n = in.n;
+    if (n <= 0) return cudaSuccess;
+    Scratch sc = carve(scratch, n);
+    cudaError_t e = morton_and_sort(in, sc, s);
+    if (e != cudaSuccess) return e;
+    k_gather<<<grid_of(n, 256), 256, 0, s>>>(in, out, sc.idx[0], sc.box);
+    if (n > 1) {
+        k_karras<<<grid_of(n - 1, 256), 256, 0, s>>>(n, sc.codes[0], out.nodes, sc.parent);
+        cudaMemsetAsync(sc.flags, 0, 4 * (size_t)(n - 1), s);
+        k_refit<<<grid_of(n, 256), 256, 0, s>>>(n, out.nodes, sc.parent, sc.flags);
+    }
+    return cudaGetLastError();
+}
+
+} // namespace rtg
