@@ -67,6 +67,16 @@ extern "C" {
                                       (W and H floored to multiples of 64, RayTracer.cpp:13) */
 #define RT_FLAG_HIT_PLANES   0x2   /* also write per-pixel primary hit id / distance planes   */
 #define RT_FLAG_COUNT_WORK   0x4   /* count BVH nodes visited and primitives tested (slower)  */
+#define RT_FLAG_PROFILE      0x8   /* time every kernel with CUDA events (rt_render_stats.kernel_ms) */
+
+/* kernel kinds of rt_render_stats.kernel_ms / kernel_launches */
+#define RT_KERNEL_RAYGEN     0
+#define RT_KERNEL_EXTEND     1
+#define RT_KERNEL_SHADE      2
+#define RT_KERNEL_SHADOW     3
+#define RT_KERNEL_RESOLVE    4
+#define RT_KERNEL_OTHER      5
+#define RT_KERNEL_KINDS      6
 
 typedef struct rt_camera {
     float position[3];
@@ -145,11 +155,16 @@ typedef struct rt_render_stats {
     int64_t rays_primary;        /* W*H*spp rays generated */
     int64_t rays_secondary;      /* reflect + refract rays traced */
     int64_t rays_shadow;         /* shadow rays traced */
-    int64_t nodes_visited;       /* with RT_FLAG_COUNT_WORK */
-    int64_t tris_tested;         /* with RT_FLAG_COUNT_WORK */
+    int64_t nodes_visited;       /* with RT_FLAG_COUNT_WORK: BVH node boxes tested by extend */
+    int64_t tris_tested;         /* with RT_FLAG_COUNT_WORK: by extend */
     int64_t spheres_tested;      /* with RT_FLAG_COUNT_WORK */
+    int64_t shadow_nodes_visited;   /* the same three counts for the shadow (any-hit) kernels */
+    int64_t shadow_tris_tested;
+    int64_t shadow_spheres_tested;
     float   ms;                  /* device time of the last render (CUDA events) */
     int32_t overflow_retries;
+    float   kernel_ms[RT_KERNEL_KINDS];       /* with RT_FLAG_PROFILE: device time per kernel kind */
+    int32_t kernel_launches[RT_KERNEL_KINDS]; /* kernels launched per kind (always filled) */
 } rt_render_stats;
 
 typedef struct rt_ctx rt_ctx;
@@ -302,6 +317,10 @@ const rt_scene_desc *rt_scene_host_desc(const rt_scene_host *s);
 int  rt_scene_host_render_params(const rt_scene_host *s, int32_t *spp, int32_t *max_level,
                                  uint64_t *seed);
 int  rt_scene_host_save(const rt_scene_host *s, const char *path);
+/* page-lock the scene's host arrays so uploads run at full link speed (0 = pinned) */
+int  rt_scene_host_pin(rt_scene_host *s);
+/* bytes of the scene's host arrays that an upload copies to the device */
+int64_t rt_scene_host_bytes(const rt_scene_host *s);
 int  rt_scene_host_load(const char *path, rt_scene_host **out);
 void rt_scene_host_free(rt_scene_host *s);
 

@@ -21,7 +21,8 @@ RT_OBJECT_SPHERE, RT_OBJECT_CUBE, RT_OBJECT_MODEL, RT_OBJECT_PLANE, RT_OBJECT_BA
 RT_LIGHT_PARALLEL, RT_LIGHT_POINT, RT_LIGHT_SPOT = 1, 2, 3
 RT_MODE_CHECK, RT_MODE_DEPTH, RT_MODE_NORMAL, RT_MODE_TEXTURE = 0x1, 0x2, 0x3, 0x4
 RT_MODE_MATERIAL, RT_MODE_SHADOW, RT_MODE_REFLECT, RT_MODE_REFRACT, RT_MODE_RAYTRACE = 0x5, 0x6, 0x7, 0x8, 0x80
-RT_FLAG_REF_TILES, RT_FLAG_HIT_PLANES, RT_FLAG_COUNT_WORK = 0x1, 0x2, 0x4
+RT_FLAG_REF_TILES, RT_FLAG_HIT_PLANES, RT_FLAG_COUNT_WORK, RT_FLAG_PROFILE = 0x1, 0x2, 0x4, 0x8
+KERNEL_KINDS = ("raygen", "extend", "shade", "shadow", "resolve", "other")
 
 F3 = C.c_float * 3
 
@@ -70,13 +71,18 @@ class RenderDesc(C.Structure):
 class RenderStats(C.Structure):
     _fields_ = [("rays_primary", C.c_int64), ("rays_secondary", C.c_int64), ("rays_shadow", C.c_int64),
                 ("nodes_visited", C.c_int64), ("tris_tested", C.c_int64), ("spheres_tested", C.c_int64),
-                ("ms", C.c_float), ("overflow_retries", C.c_int32)]
+                ("shadow_nodes_visited", C.c_int64), ("shadow_tris_tested", C.c_int64),
+                ("shadow_spheres_tested", C.c_int64), ("ms", C.c_float), ("overflow_retries", C.c_int32),
+                ("kernel_ms", C.c_float * 6), ("kernel_launches", C.c_int32 * 6)]
 
     def total_rays(self) -> int:
         return int(self.rays_primary + self.rays_secondary + self.rays_shadow)
 
     def as_dict(self) -> dict:
-        return {k: getattr(self, k) for k, _ in self._fields_}
+        d = {k: getattr(self, k) for k, _ in self._fields_}
+        d["kernel_ms"] = dict(zip(KERNEL_KINDS, list(self.kernel_ms)))
+        d["kernel_launches"] = dict(zip(KERNEL_KINDS, list(self.kernel_launches)))
+        return d
 
 
 class BatchTuning(C.Structure):
@@ -153,6 +159,8 @@ _SIGS = {
     "rt_scene_host_desc": (C.POINTER(SceneDesc), [P]),
     "rt_scene_host_render_params": (C.c_int, [P, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_uint64)]),
     "rt_scene_host_save": (C.c_int, [P, C.c_char_p]),
+    "rt_scene_host_pin": (C.c_int, [P]),
+    "rt_scene_host_bytes": (C.c_int64, [P]),
     "rt_scene_host_load": (C.c_int, [C.c_char_p, C.POINTER(P)]),
     "rt_scene_host_free": (None, [P]),
 }
@@ -237,6 +245,15 @@ class SceneHost:
         if rc:
             raise RTError(rc, f"rt_scene_host_load({path})")
         return cls(h)
+
+    def pin(self) -> None:
+        rc = lib.rt_scene_host_pin(self._h)
+        if rc:
+            raise RTError(rc, "rt_scene_host_pin")
+
+    @property
+    def nbytes(self) -> int:
+        return int(lib.rt_scene_host_bytes(self._h))
 
     def save(self, path: str) -> None:
         rc = lib.rt_scene_host_save(self._h, path.encode())
@@ -348,9 +365,10 @@ class Context:
             out.update(obj=obj, prim=prim, t=t)
         return out
 
-    def render_host(self, scene: SceneHost, rd: RenderDesc, w: int, h: int):
-        rgb8 = np.empty((h, w, 3), np.uint8)
-        rgb = np.empty((h, w, 3), np.float32)
+    def render_host(self, scene: SceneHost, rd: RenderDesc, w: int, h: int, want_rgb: bool = True,
+                    rgb8: np.ndarray | None = None):
+        rgb8 = np.empty((h, w, 3), np.uint8) if rgb8 is None else rgb8
+        rgb = np.empty((h, w, 3), np.float32) if want_rgb else None
         st = RenderStats()
         self._ck(lib.rt_render_host(self._h, scene.desc_ptr(), C.byref(rd), _ptr(rgb8), _ptr(rgb), C.byref(st)),
                  "rt_render_host")

@@ -15,6 +15,8 @@
 #include <string>
 #include <vector>
 
+#include <cuda_runtime_api.h>
+
 #include "../../include/rt_gb300.h"
 #include "Flatten.h"
 #include "Scene.h"
@@ -269,6 +271,11 @@ struct rt_scene_host {
     FlatScene flat;
     int32_t spp = 1, max_level = 3;
     uint64_t seed = 0;
+    std::vector<void *> pinned;
+    ~rt_scene_host()
+    {
+        for (void *p : pinned) cudaHostUnregister(p);
+    }
 };
 
 static rt_scene_host *finish(Scene &sc, int spp, int max_level, uint64_t seed)
@@ -437,6 +444,37 @@ extern "C" int rt_scene_host_render_params(const rt_scene_host *s, int32_t *spp,
 }
 
 extern "C" void rt_scene_host_free(rt_scene_host *s) { delete s; }
+
+extern "C" int64_t rt_scene_host_bytes(const rt_scene_host *s)
+{
+    if (!s) return 0;
+    const FlatScene &f = s->flat;
+    int64_t b = (int64_t)(f.tri_p.size() + f.tri_n.size() + f.tri_uv.size()) * 4 +
+                (int64_t)(f.tri_mtl.size() + f.tri_id.size()) * 4 + (int64_t)f.objects.size() * (int64_t)sizeof(rt_object) +
+                (int64_t)f.materials.size() * (int64_t)sizeof(rt_material) + (int64_t)f.lights.size() * (int64_t)sizeof(rt_light);
+    for (auto &t : f.texels) b += (int64_t)t.size();
+    return b;
+}
+
+extern "C" int rt_scene_host_pin(rt_scene_host *s)
+{
+    if (!s) return RT_ERR_INVALID;
+    if (!s->pinned.empty()) return RT_OK;
+    FlatScene &f = s->flat;
+    auto pin = [&](void *p, size_t bytes) -> bool {
+        if (!p || !bytes) return true;
+        if (cudaHostRegister(p, bytes, cudaHostRegisterDefault) != cudaSuccess) {
+            cudaGetLastError();
+            return false;
+        }
+        s->pinned.push_back(p);
+        return true;
+    };
+    bool ok = pin(f.tri_p.data(), f.tri_p.size() * 4) && pin(f.tri_n.data(), f.tri_n.size() * 4) &&
+              pin(f.tri_uv.data(), f.tri_uv.size() * 4) && pin(f.tri_mtl.data(), f.tri_mtl.size() * 4) &&
+              pin(f.tri_id.data(), f.tri_id.size() * 4);
+    return ok ? RT_OK : RT_ERR_CUDA;
+}
 
 // ---- binary scene file: "RTSC", version, fixed-size records, then arrays ------------------
 namespace {

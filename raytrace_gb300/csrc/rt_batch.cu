@@ -102,7 +102,7 @@ static int batch_core(rt_ctx *ctx, int32_t n, const int32_t *scene_ids, const in
             cudaGraph_t g;
             cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
             cudaMemsetAsync(ws.wf.C, 0, sizeof(Counters), cap);
-            enqueue_levels(ctx, ws, plan.max_level, t, cap);
+            enqueue_levels(ctx, ws, plan.max_level, t, cap, nullptr);
             cudaError_t e = cudaStreamEndCapture(cap, &g);
             cudaStreamDestroy(cap);
             if (e != cudaSuccess) return ctx_fail(ctx, RT_ERR_CUDA, "graph capture: %s", cudaGetErrorString(e));
@@ -126,7 +126,7 @@ static int batch_core(rt_ctx *ctx, int32_t n, const int32_t *scene_ids, const in
             cudaGraphLaunch(exec, s);
         else {
             cudaMemsetAsync(ws.wf.C, 0, sizeof(Counters), s);
-            enqueue_levels(ctx, ws, plan.max_level, t, s);
+            enqueue_levels(ctx, ws, plan.max_level, t, s, nullptr);
         }
         cudaMemcpyAsync(ctx->counters_host, ws.wf.C, sizeof(Counters), cudaMemcpyDeviceToHost, s);
         if (cudaStreamSynchronize(s) != cudaSuccess) return ctx_fail(ctx, RT_ERR_CUDA, "batch wave failed");

@@ -308,6 +308,7 @@ extern "C" int rt_scene_upload(rt_ctx *ctx, const rt_scene_desc *d, int32_t *sce
     const size_t o_tp = take(sizeof(float) * 9 * (size_t)n), o_tn = take(sizeof(float) * 9 * (size_t)n);
     const size_t o_tuv = has_uv ? take(sizeof(float) * 6 * (size_t)n) : 0;
     const size_t o_tm = take(sizeof(int) * (size_t)n), o_ti = take(sizeof(int) * (size_t)n), o_to = take(sizeof(int) * (size_t)n);
+    const size_t o_rng = take(sizeof(int) * 3 * std::max<size_t>(1, h.tri_ranges.size()));
     const size_t o_nodes = take(sizeof(float4) * 2 * (size_t)std::max<int64_t>(1, 2 * n - 1));
     const size_t o_tri = take(sizeof(float4) * 3 * (size_t)n), o_trin = take(sizeof(float4) * 3 * (size_t)n);
     const size_t o_triuv = has_uv ? take(sizeof(float2) * 3 * (size_t)n) : 0;
@@ -315,23 +316,58 @@ extern "C" int rt_scene_upload(rt_ctx *ctx, const rt_scene_desc *d, int32_t *sce
     CK(ctx, sc->mem.ensure(off));
     char *base = (char *)sc->mem.p;
     cudaStream_t s = ctx->stream;
-    // staging copies of the compacted triangle inputs
-    std::vector<float> tp((size_t)n * 9), tn((size_t)n * 9), tuv(has_uv ? (size_t)n * 6 : 0);
-    std::vector<int> tm((size_t)n), ti((size_t)n), to((size_t)n);
+    // triangle inputs: straight from the caller's arrays when the shown models cover them in
+    // order (the usual case, and the fast path for page-locked host memory); otherwise
+    // compacted through staging copies
+    bool direct = true;
     {
-        size_t w = 0;
-        for (size_t r = 0; r < h.tri_ranges.size(); ++r) {
-            const int64_t first = h.tri_ranges[r].first, cnt = h.tri_ranges[r].second;
-            std::memcpy(&tp[w * 9], d->tri_p + first * 9, sizeof(float) * 9 * (size_t)cnt);
-            std::memcpy(&tn[w * 9], d->tri_n + first * 9, sizeof(float) * 9 * (size_t)cnt);
-            if (has_uv) std::memcpy(&tuv[w * 6], d->tri_uv + first * 6, sizeof(float) * 6 * (size_t)cnt);
-            for (int64_t i = 0; i < cnt; ++i) {
-                tm[w + i] = d->tri_mtl[first + i];
-                ti[w + i] = d->tri_id ? d->tri_id[first + i] : (int)i;
-                to[w + i] = h.tri_range_obj[r];
-            }
-            w += (size_t)cnt;
+        int64_t expect = 0;
+        for (auto &r : h.tri_ranges) {
+            if (r.first != expect) direct = false;
+            expect = r.first + r.second;
         }
+        if (expect != d->n_tris) direct = false;
+    }
+    std::vector<int> range_tab;   // (first, count, obj) per shown model, in the compacted numbering
+    {
+        int64_t w = 0;
+        for (size_t r = 0; r < h.tri_ranges.size(); ++r) {
+            range_tab.insert(range_tab.end(), {(int)w, (int)h.tri_ranges[r].second, h.tri_range_obj[r]});
+            w += h.tri_ranges[r].second;
+        }
+    }
+    if (n > 0) {
+        if (direct) {
+            CK(ctx, cudaMemcpyAsync(base + o_tp, d->tri_p, sizeof(float) * 9 * (size_t)n, cudaMemcpyHostToDevice, s));
+            CK(ctx, cudaMemcpyAsync(base + o_tn, d->tri_n, sizeof(float) * 9 * (size_t)n, cudaMemcpyHostToDevice, s));
+            if (has_uv) CK(ctx, cudaMemcpyAsync(base + o_tuv, d->tri_uv, sizeof(float) * 6 * (size_t)n, cudaMemcpyHostToDevice, s));
+            CK(ctx, cudaMemcpyAsync(base + o_tm, d->tri_mtl, sizeof(int) * (size_t)n, cudaMemcpyHostToDevice, s));
+            if (d->tri_id) CK(ctx, cudaMemcpyAsync(base + o_ti, d->tri_id, sizeof(int) * (size_t)n, cudaMemcpyHostToDevice, s));
+        } else {
+            std::vector<float> tp((size_t)n * 9), tn((size_t)n * 9), tuv(has_uv ? (size_t)n * 6 : 0);
+            std::vector<int> tm((size_t)n), ti((size_t)n);
+            size_t w = 0;
+            for (size_t r = 0; r < h.tri_ranges.size(); ++r) {
+                const int64_t first = h.tri_ranges[r].first, cnt = h.tri_ranges[r].second;
+                std::memcpy(&tp[w * 9], d->tri_p + first * 9, sizeof(float) * 9 * (size_t)cnt);
+                std::memcpy(&tn[w * 9], d->tri_n + first * 9, sizeof(float) * 9 * (size_t)cnt);
+                if (has_uv) std::memcpy(&tuv[w * 6], d->tri_uv + first * 6, sizeof(float) * 6 * (size_t)cnt);
+                for (int64_t i = 0; i < cnt; ++i) {
+                    tm[w + i] = d->tri_mtl[first + i];
+                    ti[w + i] = d->tri_id ? d->tri_id[first + i] : (int)i;
+                }
+                w += (size_t)cnt;
+            }
+            CK(ctx, cudaMemcpyAsync(base + o_tp, tp.data(), sizeof(float) * tp.size(), cudaMemcpyHostToDevice, s));
+            CK(ctx, cudaMemcpyAsync(base + o_tn, tn.data(), sizeof(float) * tn.size(), cudaMemcpyHostToDevice, s));
+            if (has_uv) CK(ctx, cudaMemcpyAsync(base + o_tuv, tuv.data(), sizeof(float) * tuv.size(), cudaMemcpyHostToDevice, s));
+            CK(ctx, cudaMemcpyAsync(base + o_tm, tm.data(), sizeof(int) * (size_t)n, cudaMemcpyHostToDevice, s));
+            CK(ctx, cudaMemcpyAsync(base + o_ti, ti.data(), sizeof(int) * (size_t)n, cudaMemcpyHostToDevice, s));
+            CK(ctx, cudaStreamSynchronize(s));   // the staging vectors go out of scope
+        }
+        CK(ctx, cudaMemcpyAsync(base + o_rng, range_tab.data(), sizeof(int) * range_tab.size(), cudaMemcpyHostToDevice, s));
+        launch_tri_objects((const int *)(base + o_rng), (int)h.tri_ranges.size(), (int)n, (int *)(base + o_to),
+                           (direct && !d->tri_id) ? (int *)(base + o_ti) : nullptr, s);
     }
     CK(ctx, cudaMemcpyAsync(base + o_prims, h.prims.data(), sizeof(DevPrim) * h.prims.size(), cudaMemcpyHostToDevice, s));
     CK(ctx, cudaMemcpyAsync(base + o_mtl, h.mtl.data(), sizeof(DevMaterial) * h.mtl.size(), cudaMemcpyHostToDevice, s));
@@ -339,14 +375,6 @@ extern "C" int rt_scene_upload(rt_ctx *ctx, const rt_scene_desc *d, int32_t *sce
     CK(ctx, cudaMemcpyAsync(base + o_tex, h.tex.data(), sizeof(DevTexture) * h.tex.size(), cudaMemcpyHostToDevice, s));
     CK(ctx, cudaMemcpyAsync(base + o_texels, h.texels.data(), h.texels.size(), cudaMemcpyHostToDevice, s));
     CK(ctx, cudaMemcpyAsync(base + o_objpos, h.obj_pos.data(), sizeof(float) * h.obj_pos.size(), cudaMemcpyHostToDevice, s));
-    if (n > 0) {
-        CK(ctx, cudaMemcpyAsync(base + o_tp, tp.data(), sizeof(float) * tp.size(), cudaMemcpyHostToDevice, s));
-        CK(ctx, cudaMemcpyAsync(base + o_tn, tn.data(), sizeof(float) * tn.size(), cudaMemcpyHostToDevice, s));
-        if (has_uv) CK(ctx, cudaMemcpyAsync(base + o_tuv, tuv.data(), sizeof(float) * tuv.size(), cudaMemcpyHostToDevice, s));
-        CK(ctx, cudaMemcpyAsync(base + o_tm, tm.data(), sizeof(int) * (size_t)n, cudaMemcpyHostToDevice, s));
-        CK(ctx, cudaMemcpyAsync(base + o_ti, ti.data(), sizeof(int) * (size_t)n, cudaMemcpyHostToDevice, s));
-        CK(ctx, cudaMemcpyAsync(base + o_to, to.data(), sizeof(int) * (size_t)n, cudaMemcpyHostToDevice, s));
-    }
     DevScene &H = sc->hdr;
     H.prims = (const DevPrim *)(base + o_prims);
     H.n_prims = (int)h.prims.size();
@@ -626,16 +654,30 @@ int make_job(rt_ctx *ctx, const SceneDev &sc, FrameDev &f, const rt_render_desc 
 }
 
 // enqueue the level loop of one wave whose jobs are already in the workspace
-void enqueue_levels(rt_ctx *ctx, Workspace &ws, int max_level, const Tuning &t, cudaStream_t s)
+void enqueue_levels(rt_ctx *ctx, Workspace &ws, int max_level, const Tuning &t, cudaStream_t s, KernelProfiler *prof)
 {
     (void)ctx;
+    auto B = [&](int kind) {
+        if (prof) prof->begin(kind, s);
+    };
+    auto E = [&]() {
+        if (prof) prof->end(s);
+    };
     const int raygen_grid = sm_count() * 8;
+    B(RT_KERNEL_RAYGEN);
     launch_raygen(ws.wf, raygen_grid, 256, s);
+    E();
     for (int level = 0; level <= max_level; ++level) {
         const int sel = level & 1;
+        B(RT_KERNEL_EXTEND);
         launch_extend(ws.wf, sel, level, t, s);
+        E();
+        B(RT_KERNEL_SHADE);
         launch_shade(ws.wf, sel, level, t, s);
+        E();
+        B(RT_KERNEL_SHADOW);
         launch_shadow(ws.wf, level, t, s);
+        E();
     }
 }
 
@@ -663,11 +705,19 @@ static int render_once(rt_ctx *ctx, SceneDev &sc, FrameDev &f, const rt_render_d
     CK(ctx, cudaMemcpyAsync(ws.scalars, ctx->h_scalars, 24, cudaMemcpyHostToDevice, s));
     CK(ctx, cudaMemsetAsync(ws.wf.C, 0, sizeof(Counters), s));
     CK(ctx, cudaMemsetAsync(f.fb.acc, 0, 24 * (size_t)f.w * f.h, s));
-    if (rd->flags & RT_FLAG_HIT_PLANES) launch_plane_init(f.fb, (long long)f.w * f.h, s);
+    KernelProfiler &P = ctx->prof;
+    P.reset((rd->flags & RT_FLAG_PROFILE) != 0);
+    if (rd->flags & RT_FLAG_HIT_PLANES) {
+        P.begin(RT_KERNEL_OTHER, s);
+        launch_plane_init(f.fb, (long long)f.w * f.h, s);
+        P.end(s);
+    }
     Tuning t = ctx->plain_tuning;
     t.count = (rd->flags & RT_FLAG_COUNT_WORK) != 0;
-    enqueue_levels(ctx, ws, rd->max_level, t, s);
+    enqueue_levels(ctx, ws, rd->max_level, t, s, &P);
+    P.begin(RT_KERNEL_RESOLVE, s);
     launch_resolve(f.fb, f.w, f.h, rd->spp, s);
+    P.end(s);
     CK(ctx, cudaGetLastError());
     CK(ctx, cudaMemcpyAsync(ctx->counters_host, ws.wf.C, sizeof(Counters), cudaMemcpyDeviceToHost, s));
     CK(ctx, cudaEventRecord(ctx->ev_stop, s));
@@ -713,10 +763,15 @@ extern "C" int rt_render_wait(rt_ctx *ctx, rt_render_stats *stats)
         stats->nodes_visited = (int64_t)C.nodes;
         stats->tris_tested = (int64_t)C.tris;
         stats->spheres_tested = (int64_t)C.spheres;
+        stats->shadow_nodes_visited = (int64_t)C.s_nodes;
+        stats->shadow_tris_tested = (int64_t)C.s_tris;
+        stats->shadow_spheres_tested = (int64_t)C.s_spheres;
         float ms = 0.0f;
         cudaEventElapsedTime(&ms, ctx->ev_start, ctx->ev_stop);
         stats->ms = ms;
         stats->overflow_retries = retries;
+        ctx->prof.collect(stats->kernel_ms);
+        for (int k = 0; k < RT_KERNEL_KINDS; ++k) stats->kernel_launches[k] = ctx->prof.launches[k];
     }
     ctx->pending.active = false;
     if (was_cancelled) return ctx_fail(ctx, RT_ERR_CANCELLED, "render cancelled");

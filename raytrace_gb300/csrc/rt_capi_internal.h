@@ -5,6 +5,7 @@
 #include <map>
 #include <memory>
 #include <string>
+#include <vector>
 
 #include "../../include/rt_gb300.h"
 #include "rt_kernels.cuh"
@@ -70,6 +71,59 @@ struct Pending {
     int retries = 0;
 };
 
+// CUDA events around each kernel launch of a render (RT_FLAG_PROFILE)
+struct KernelProfiler {
+    std::vector<cudaEvent_t> pool;
+    std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> marks;
+    size_t used = 0;
+    bool on = false;
+    int launches[RT_KERNEL_KINDS] = {0};
+    void reset(bool enable)
+    {
+        on = enable;
+        used = 0;
+        marks.clear();
+        for (int &l : launches) l = 0;
+    }
+    cudaEvent_t next()
+    {
+        if (used == pool.size()) {
+            cudaEvent_t e;
+            cudaEventCreate(&e);
+            pool.push_back(e);
+        }
+        return pool[used++];
+    }
+    // bracket one launch of `kind` (call begin before and end after it)
+    void begin(int kind, cudaStream_t s)
+    {
+        launches[kind]++;
+        if (!on) return;
+        cudaEvent_t a = next();
+        cudaEventRecord(a, s);
+        marks.push_back({kind, {a, nullptr}});
+    }
+    void end(cudaStream_t s)
+    {
+        if (!on || marks.empty()) return;
+        cudaEvent_t b = next();
+        cudaEventRecord(b, s);
+        marks.back().second.second = b;
+    }
+    void collect(float *ms) const
+    {
+        for (int k = 0; k < RT_KERNEL_KINDS; ++k) ms[k] = 0.0f;
+        for (auto &m : marks) {
+            float t = 0.0f;
+            if (m.second.second && cudaEventElapsedTime(&t, m.second.first, m.second.second) == cudaSuccess) ms[m.first] += t;
+        }
+    }
+    ~KernelProfiler()
+    {
+        for (cudaEvent_t e : pool) cudaEventDestroy(e);
+    }
+};
+
 struct GraphEntry {
     cudaGraphExec_t exec = nullptr;
     ~GraphEntry()
@@ -95,6 +149,7 @@ struct rt_ctx {
     long long h_job_end[1] = {0};
     Pending pending;
     rtg::Tuning plain_tuning;
+    KernelProfiler prof;
     std::map<long long, std::unique_ptr<GraphEntry>> graphs;
 };
 
@@ -104,4 +159,6 @@ int frame_alloc(rt_ctx *ctx, int32_t w, int32_t h, FrameDev &f);
 int ws_ensure(rt_ctx *ctx, Workspace &ws, long long qcap, int njobs);
 int make_job(rt_ctx *ctx, const SceneDev &sc, FrameDev &f, const rt_render_desc *rd, int scene_slot, rtg::DevJob &J,
              long long &samples);
-void enqueue_levels(rt_ctx *ctx, Workspace &ws, int max_level, const rtg::Tuning &t, cudaStream_t s);
+// raygen + (extend, shade, shadow) per level; `prof` (may be NULL) brackets every launch
+void enqueue_levels(rt_ctx *ctx, Workspace &ws, int max_level, const rtg::Tuning &t, cudaStream_t s,
+                    KernelProfiler *prof);

@@ -161,7 +161,8 @@ struct Counters {
     int overflow;                         // a queue ran out of space
     int work[16];                         // dynamic work counters (reset per pass)
     unsigned long long rays_primary, rays_secondary, rays_shadow;
-    unsigned long long nodes, tris, spheres;
+    unsigned long long nodes, tris, spheres;            // extend kernels (closest hit)
+    unsigned long long s_nodes, s_tris, s_spheres;      // shadow kernels (any hit)
     int error;
     int pad[3];
 };

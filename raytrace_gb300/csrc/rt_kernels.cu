@@ -457,9 +457,9 @@ __global__ void __launch_bounds__(256) k_shadow(Wavefront wf, int wslot, int til
             wc.spheres += __shfl_down_sync(kFull, wc.spheres, off);
         }
         if ((threadIdx.x & 31) == 0) {
-            atomicAdd(&C->nodes, (unsigned long long)wc.nodes);
-            atomicAdd(&C->tris, (unsigned long long)wc.tris);
-            atomicAdd(&C->spheres, (unsigned long long)wc.spheres);
+            atomicAdd(&C->s_nodes, (unsigned long long)wc.nodes);
+            atomicAdd(&C->s_tris, (unsigned long long)wc.tris);
+            atomicAdd(&C->s_spheres, (unsigned long long)wc.spheres);
         }
     }
 }

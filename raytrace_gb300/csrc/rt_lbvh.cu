@@ -360,6 +360,26 @@ cudaError_t morton_and_sort(const LbvhInput &in, const Scratch &sc, cudaStream_t
 
 } // namespace
 
+__global__ void k_tri_objects(const int *ranges, int n_ranges, int n, int *obj, int *ids)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        int lo = 0, hi = n_ranges - 1;
+        while (lo < hi) {   // last range whose first <= i
+            const int mid = (lo + hi + 1) >> 1;
+            if (ranges[3 * mid] <= i) lo = mid;
+            else hi = mid - 1;
+        }
+        obj[i] = ranges[3 * lo + 2];
+        if (ids) ids[i] = i - ranges[3 * lo];
+    }
+}
+
+void launch_tri_objects(const int *ranges, int n_ranges, int n, int *obj, int *ids, cudaStream_t s)
+{
+    if (n <= 0 || n_ranges <= 0) return;
+    k_tri_objects<<<grid_of(n, 256), 256, 0, s>>>(ranges, n_ranges, n, obj, ids);
+}
+
 size_t lbvh_scratch_bytes(int n)
 {
     const int tiles = (n + kTileKeys - 1) / kTileKeys;

@@ -31,4 +31,8 @@ cudaError_t lbvh_build(const LbvhInput &in, const LbvhOutput &out, void *scratch
 cudaError_t lbvh_morton_sort(const LbvhInput &in, uint32_t *codes_out, uint32_t *perm_out, void *scratch,
                              cudaStream_t s);
 
+// per-triangle object index (and, when `ids` is not NULL, the index inside its model) from a
+// table of (first, count, object) triples, one per shown model
+void launch_tri_objects(const int *ranges, int n_ranges, int n, int *obj, int *ids, cudaStream_t s);
+
 } // namespace rtg

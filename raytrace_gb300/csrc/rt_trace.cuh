@@ -147,9 +147,11 @@ constexpr unsigned kMaxVisits = 1u << 22;
 template <int STACK, bool COUNT>
 __device__ void closest_hit(const DevScene &S, V3 O, V3 D, int excl, bool inside, Best &best, int &newobj, WorkCount &wc)
 {
+    // "no hit" sits at 1e20 with order -1: a primitive must be strictly closer to replace it,
+    // as the reference's `t < hr.distance` (BorderTest reports a box miss as exactly 1e20)
     best.t = kMiss;
     best.key = -1;
-    best.ord = 0x7fffffff;
+    best.ord = -1;
     best.u = best.v = 0.0f;
     // the ray's own sphere uses the inside branch; if it wins, newobj is the best hit among
     // the objects before it (the reference updates newobj only for keys != excl)
@@ -162,7 +164,7 @@ __device__ void closest_hit(const DevScene &S, V3 O, V3 D, int excl, bool inside
     Best before;
     before.t = kMiss;
     before.key = -1;
-    before.ord = 0x7fffffff;
+    before.ord = -1;
 
     for (int p = 0; p < S.n_prims; ++p) {
         const DevPrim &P = S.prims[p];

@@ -1,0 +1,203 @@
+"""GPU renderer parity: against the reference's own outputs (golden fixtures) and against the
+CPU oracle. Hit object / primitive ids must match exactly and colours within 1e-4 (absolute,
+per FP32 channel, before Color::put) on every pixel the oracle does not mark ambiguous."""
+import os
+import subprocess
+import tempfile
+
+import numpy as np
+import pytest
+
+import raytrace_gb300 as rt
+from conftest import ROOT, golden_names, load_golden
+from oracle import port
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-4
+
+
+def gpu_render(ctx, scene, w, h, spp, lvl, seed, ref_tiles=True):
+    sid = ctx.upload(scene)
+    fid = ctx.frame(w, h)
+    flags = rt.RT_FLAG_HIT_PLANES | (rt.RT_FLAG_REF_TILES if ref_tiles else 0)
+    st = ctx.render(sid, fid, ctx.render_desc(w, h, spp, lvl, flags=flags, seed=seed))
+    out = ctx.download(fid, w, h)
+    ctx.release_frame(fid)
+    ctx.release_scene(sid)
+    return out, st
+
+
+def compare(out, ref, amb, region):
+    o, r, a = (x[region] for x in (out, ref, amb))
+    id_bad = ((o["obj"] != r["obj"]) | (o["prim"] != r["prim"])) if False else None
+    return id_bad
+
+
+def check_parity(out, ref, amb, h, w, max_rgb8_lsb=1):
+    rh, rw = (h // 64) * 64, (w // 64) * 64
+    sl = (slice(0, rh), slice(0, rw))
+    a = amb[sl]
+    ids_equal = (out["obj"][sl] == ref["obj"][sl]) & (out["prim"][sl] == ref["prim"][sl])
+    bad_ids = ~ids_equal & ~a
+    assert not bad_ids.any(), f"{int(bad_ids.sum())} unambiguous pixels hit another primitive"
+    same = ids_equal & (ref["obj"][sl] >= 0)
+    np.testing.assert_array_equal(out["t"][sl][same].view(np.uint32), ref["t"][sl][same].view(np.uint32))
+    d = np.abs(out["rgb"][sl] - ref["rgb"][sl]).max(axis=2)
+    bad = (d > TOL) & ~a
+    assert not bad.any(), f"{int(bad.sum())} unambiguous pixels differ by more than {TOL} (max {d[~a].max():.3g})"
+    lsb = np.abs(out["rgb8"][sl].astype(int) - ref["rgb8"][sl].astype(int)).max(axis=2)
+    assert lsb[~a].max() <= max_rgb8_lsb
+    return {"ambiguous": int(a.sum()), "max_rgb_diff": float(d[~a].max()) if (~a).any() else 0.0}
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_gpu_matches_reference_fixture(ctx, name):
+    g, meta, scene = load_golden(name)
+    w, h = meta["width"], meta["height"]
+    out, st = gpu_render(ctx, scene, w, h, meta["spp"], meta["max_level"], meta["seed"])
+    check_parity(out, g, g["ambiguous"], h, w)
+
+
+@pytest.mark.parametrize("seed,n_spheres,ico,refr", [(1, 8, 0, 0), (2, 12, 6, 3), (3, 5, 10, 2), (4, 16, 3, 4)])
+def test_gpu_matches_oracle_small(ctx, seed, n_spheres, ico, refr):
+    w, h = 96, 80
+    scene = rt.SceneHost.small(seed, n_spheres, ico, w, h, refr)
+    out, _ = gpu_render(ctx, scene, w, h, 1, 3, seed, ref_tiles=False)
+    ref = port.render(scene, w, h, 1, 3, seed, ref_tiles=False, check=True)
+    # full frame (not only the 64x64 tiles): compare every pixel
+    a = ref["ambiguous"]
+    ids_equal = (out["obj"] == ref["obj"]) & (out["prim"] == ref["prim"])
+    assert not (~ids_equal & ~a).any()
+    d = np.abs(out["rgb"] - ref["rgb"]).max(axis=2)
+    assert not ((d > TOL) & ~a).any(), d[~a].max()
+
+
+def test_gpu_matches_oracle_jitter_depth4(ctx):
+    w, h = 64, 64
+    scene = rt.SceneHost.small(21, 14, 5, w, h, 2)
+    out, st = gpu_render(ctx, scene, w, h, 4, 4, 77)
+    ref = port.render(scene, w, h, 4, 4, 77, ref_tiles=True, check=True)
+    check_parity(out, ref, ref["ambiguous"], h, w)
+    assert st.rays_primary == w * h * 4
+    got = np.array([st.rays_primary, st.rays_secondary, st.rays_shadow])
+    if ref["ambiguous"].any():   # a near-tie may change the ray tree below that pixel
+        assert np.all(np.abs(got - ref["counts"]) <= 1e-3 * ref["counts"] + 64)
+    else:
+        np.testing.assert_array_equal(ref["counts"], got)
+
+
+def test_ray_counts_match_oracle(ctx):
+    w, h = 128, 128
+    scene = rt.SceneHost.config(0).with_camera(w, h)
+    _, st = gpu_render(ctx, scene, w, h, 1, 3, 0, ref_tiles=False)
+    ref = port.render(scene, w, h, 1, 3, 0, check=False)
+    assert [st.rays_primary, st.rays_secondary, st.rays_shadow] == ref["counts"].tolist()
+
+
+def test_config1_full_frame(ctx):
+    """81,920-triangle mesh at 1024x768: every mismatch must be a pixel the oracle marks."""
+    scene = rt.SceneHost.config(1)
+    w, h = 1024, 768
+    out, _ = gpu_render(ctx, scene, w, h, 1, 3, 1)
+    ref = port.render(scene, w, h, 1, 3, 1, ref_tiles=True, check=False)
+    d = np.abs(out["rgb"] - ref["rgb"]).max(axis=2)
+    bad = (d > TOL) | (out["obj"] != ref["obj"]) | (out["prim"] != ref["prim"])
+    assert bad.mean() < 1e-3, bad.sum()
+    ys, xs = np.nonzero(bad)
+    tiles = sorted({(y // 64) * (w // 64) + x // 64 for y, x in zip(ys, xs)})
+    if tiles:
+        chk = port.render(scene, w, h, 1, 3, 1, ref_tiles=True, check=True, tiles=tiles)
+        unexplained = bad & ~chk["ambiguous"]
+        assert not unexplained.any(), list(zip(*np.nonzero(unexplained)))[:10]
+
+
+def test_deterministic_and_order_independent(ctx):
+    scene = rt.SceneHost.config(1).with_camera(256, 192)
+    a, _ = gpu_render(ctx, scene, 256, 192, 1, 3, 1)
+    b, _ = gpu_render(ctx, scene, 256, 192, 1, 3, 1)
+    np.testing.assert_array_equal(a["rgb"].view(np.uint32), b["rgb"].view(np.uint32))
+
+
+def test_render_host_equals_device_path(ctx):
+    scene = rt.SceneHost.small(31, 10, 6, 128, 96, 3)
+    out, _ = gpu_render(ctx, scene, 128, 96, 1, 3, 0, ref_tiles=False)
+    rgb, rgb8, st = ctx.render_host(scene, ctx.render_desc(128, 96, 1, 3), 128, 96)
+    np.testing.assert_array_equal(rgb.view(np.uint32), out["rgb"].view(np.uint32))
+    np.testing.assert_array_equal(rgb8, out["rgb8"])
+
+
+def test_invalid_requests_fail_cleanly(ctx):
+    scene = rt.SceneHost.small(3, 4, 0, 64, 64)
+    sid = ctx.upload(scene)
+    fid = ctx.frame(32, 32)
+    with pytest.raises(rt.RTError) as e:
+        ctx.render(sid, fid, ctx.render_desc(64, 64, 1, 3))   # frame size mismatch
+    assert e.value.code == rt.RT_ERR_INVALID
+    with pytest.raises(rt.RTError):
+        ctx.render(sid, fid, ctx.render_desc(32, 32, 1, 9))   # depth outside 0..4
+    with pytest.raises(rt.RTError) as e:
+        ctx.render(sid + 1000, fid, ctx.render_desc(32, 32, 1, 3))
+    assert e.value.code == rt.RT_ERR_NOT_FOUND
+    ctx.release_frame(fid)
+    ctx.release_scene(sid)
+
+
+def test_dropin_cpp_api(ctx):
+    """Scene / RayTracer C++ API: RayTracer::start output equals the C ABI render of the
+    flattened scene, and matches the oracle within one uint8 step off ambiguous pixels."""
+    lib_dir = os.path.dirname(rt.LIB_PATH)
+    with tempfile.TemporaryDirectory() as d:
+        exe = os.path.join(d, "dropin_test")
+        subprocess.run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", os.path.join(ROOT, "tests", "cpp", "dropin_test.cpp"),
+                        "-o", exe, f"-L{lib_dir}", "-lrt_gb300", f"-Wl,-rpath,{lib_dir}", "-pthread"], check=True)
+        img_p, scn_p = os.path.join(d, "out.rgb8"), os.path.join(d, "s.rtsc")
+        subprocess.run([exe, img_p, scn_p], check=True, capture_output=True)
+        w, h = 192, 128
+        img = np.fromfile(img_p, np.uint8).reshape(h, w, 3)
+        scene = rt.SceneHost.load(scn_p)
+    out, _ = gpu_render(ctx, scene, w, h, 1, 3, 0)
+    np.testing.assert_array_equal(img[:128, :192], out["rgb8"][:128, :192])
+    ref = port.render(scene, w, h, 1, 3, 0, ref_tiles=True, check=True)
+    check_parity(out, ref, ref["ambiguous"], h, w)
+    assert scene.desc.objects[4].show == 0
+
+
+def test_morton_sort_bit_exact(ctx):
+    scene = rt.SceneHost.config(1)
+    tri = scene.tri_points()
+    for data in (tri, np.repeat(tri[:1000], 3, axis=0), np.random.default_rng(5).normal(size=(200000, 9)).astype(np.float32)):
+        c_gpu, p_gpu = ctx.morton_sort(data)
+        c_cpu, p_cpu = port.morton_sort(data)
+        np.testing.assert_array_equal(c_gpu, c_cpu)
+        np.testing.assert_array_equal(p_gpu, p_cpu)
+
+
+def test_lbvh_invariants(ctx):
+    scene = rt.SceneHost.config(3, 5)
+    sid = ctx.upload(scene)
+    nodes, perm = ctx.bvh(sid)
+    ctx.release_scene(sid)
+    n = scene.desc.n_tris
+    assert nodes.shape[0] == 2 * n - 1
+    assert sorted(perm.tolist()) == list(range(n))   # single model: ids are 0..n-1
+    lo, hi = nodes[:, :3], nodes[:, 4:7]
+    left = nodes[:, 3].view(np.int32)
+    right = nodes[:, 7].view(np.int32)
+    seen = np.zeros(2 * n - 1, np.int32)
+    stack = [0]
+    depth = {0: 0}
+    while stack:
+        k = stack.pop()
+        seen[k] += 1
+        if k >= n - 1:
+            continue
+        for c in (left[k], right[k]):
+            assert 0 <= c < 2 * n - 1
+            assert np.all(lo[c] >= lo[k]) and np.all(hi[c] <= hi[k])
+            depth[c] = depth[k] + 1
+            stack.append(c)
+    assert np.all(seen == 1), "every node reachable exactly once"
+    assert max(depth.values()) <= 64
+    tri = scene.tri_points().reshape(-1, 3, 3)[perm]
+    leaf_lo, leaf_hi = lo[n - 1:], hi[n - 1:]
+    assert np.all(tri.min(axis=1) >= leaf_lo) and np.all(tri.max(axis=1) <= leaf_hi)
