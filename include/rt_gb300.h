@@ -39,6 +39,7 @@ extern "C" {
 #define RT_ERR_BUDGET      -7   /* the serving HBM budget cannot admit the request */
 #define RT_ERR_NOT_FOUND   -8   /* unknown scene / frame / request id              */
 #define RT_ERR_BUSY        -9   /* the object is in use by an unfinished render    */
+#define RT_ERR_TOO_LARGE  -10   /* the request exceeds a fixed capacity            */
 
 /* ---- scene vocabulary (values match the reference's macros) --------------------- */
 #define RT_OBJECT_SPHERE     0x1   /* MY_OBJECT_SPHERE     3DElement.h:4  */
@@ -296,6 +297,19 @@ int    rt_server_run_poisson(rt_server *srv, double lambda_per_s, double duratio
 /* 30-bit Morton codes of triangle centroids over the AABB of the centroids, radix-sorted
    (stable): codes[i] and perm[i] are the i-th smallest code and its triangle index */
 int rt_morton_sort(rt_ctx *ctx, const float *tri_p, int64_t n_tris, uint32_t *codes, uint32_t *perm);
+/*
+ * rt_morton_sort on device buffers with no device allocation, for callers that cannot
+ * allocate (a plugin whose host application owns the device memory, a latency-bound path
+ * where cudaMalloc would block). d_tri_p, d_codes and d_perm are device pointers the caller
+ * owns; the working memory is one fixed static device array sized for RT_NOALLOC_MAX_TRIS
+ * triangles (about 7.5 MB, held by every GPU that loads the library). Larger inputs return
+ * RT_ERR_TOO_LARGE. Runs on cuda_stream (NULL = default stream) and returns after enqueueing.
+ * The first call on a device sets up the array's address; make it before any stream capture.
+ * Calls that overlap on the GPU share the array and race. No counterpart in the reference.
+ */
+#define RT_NOALLOC_MAX_TRIS (1 << 18)
+int rt_morton_sort_noalloc(const float *d_tri_p, int64_t n_tris, uint32_t *d_codes, uint32_t *d_perm,
+                           void *cuda_stream);
 /* download the LBVH of a scene: nodes float[(2n-1)*8] (min xyz, left | max xyz, right) and
    the sorted triangle order perm[n] */
 int rt_scene_bvh_download(rt_ctx *ctx, int32_t scene_id, float *nodes, uint32_t *perm,

@@ -17,6 +17,8 @@ LIB_PATH = os.path.join(_HERE, "_build", "librt_gb300.so")
 
 RT_OK, RT_ERR_INVALID, RT_ERR_CUDA, RT_ERR_OOM, RT_ERR_CANCELLED = 0, -1, -2, -3, -4
 RT_ERR_OVERFLOW, RT_ERR_TIMEOUT, RT_ERR_BUDGET, RT_ERR_NOT_FOUND, RT_ERR_BUSY = -5, -6, -7, -8, -9
+RT_ERR_TOO_LARGE = -10
+RT_NOALLOC_MAX_TRIS = 1 << 18
 RT_OBJECT_SPHERE, RT_OBJECT_CUBE, RT_OBJECT_MODEL, RT_OBJECT_PLANE, RT_OBJECT_BALLPLANE = 1, 2, 3, 4, 5
 RT_LIGHT_PARALLEL, RT_LIGHT_POINT, RT_LIGHT_SPOT = 1, 2, 3
 RT_MODE_CHECK, RT_MODE_DEPTH, RT_MODE_NORMAL, RT_MODE_TEXTURE = 0x1, 0x2, 0x3, 0x4
@@ -151,6 +153,7 @@ _SIGS = {
     "rt_server_now": (C.c_double, [P]),
     "rt_server_run_poisson": (C.c_int, [P, C.c_double, C.c_double, C.c_uint64, C.POINTER(ServeStats)]),
     "rt_morton_sort": (C.c_int, [P, P, C.c_int64, P, P]),
+    "rt_morton_sort_noalloc": (C.c_int, [P, C.c_int64, P, P, P]),
     "rt_scene_bvh_download": (C.c_int, [P, C.c_int32, P, P, C.POINTER(C.c_int64)]),
     "rt_scenegen": (C.c_int, [C.c_int32, C.c_int32, C.POINTER(P)]),
     "rt_scenegen_small": (C.c_int, [C.c_uint64, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.POINTER(P)]),

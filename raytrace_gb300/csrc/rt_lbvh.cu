@@ -415,3 +415,89 @@ cudaError_t lbvh_build(const LbvhInput &in, const LbvhOutput &out, void *scratch
 }
 
 } // namespace rtg
+
+// ---- allocation-free Morton sort -------------------------------------------------------------
+// Working memory of rt_morton_sort_noalloc: one fixed array in device memory, sized for
+// RT_NOALLOC_MAX_TRIS triangles (centroids 16 B, second sort buffer 8 B and zero object ids
+// 4 B per triangle, digit histograms 1 KB per 2048 triangles, the scene box and a zero object
+// position). Every GPU that loads the library holds it until the process exits.
+#include <cstdio>
+#include <mutex>
+
+#include "../../include/rt_gb300.h"
+
+namespace rtg {
+namespace {
+
+constexpr size_t kNoAllocN = (size_t)RT_NOALLOC_MAX_TRIS;
+constexpr size_t kNoAllocTiles = (kNoAllocN + kTileKeys - 1) / kTileKeys;
+constexpr size_t kNoAllocBytes = 256 + 256 + 16 * kNoAllocN + 4 * kNoAllocN + 4 * kNoAllocN + 4 * kNoAllocN +
+                                 1024 * kNoAllocTiles;
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+constexpr int kNoAllocMaxDevices = 64;
+void *g_noalloc_ptr[kNoAllocMaxDevices];
+std::mutex g_noalloc_mu;
+
+} // namespace
+} // namespace rtg
+
+// Callers that cannot allocate device memory: a plugin inside a host application whose
+// device memory is owned and budgeted by that application, or code on a latency-bound path
+// where cudaMalloc / cudaFree would block on the device. They pass device buffers they
+// already own; this entry point uses only the fixed array above (no cudaMalloc, cudaFree or
+// allocating library call). The first call on a device looks up the array's device address
+// for that device (cudaGetSymbolAddress, with the device current); make that first call
+// before any stream capture. All calls share the one array, which keeps the last call's
+// contents: calls that overlap on the GPU (two streams, two threads) race and corrupt each
+// other's results, so serialise them.
+extern "C" int rt_morton_sort_noalloc(const float *d_tri_p, int64_t n_tris, uint32_t *d_codes, uint32_t *d_perm,
+                                      void *cuda_stream)
+{
+    using namespace rtg;
+    if (n_tris < 0 || (n_tris > 0 && (!d_tri_p || !d_codes || !d_perm))) return RT_ERR_INVALID;
+    if (n_tris > (int64_t)RT_NOALLOC_MAX_TRIS) {
+        std::fprintf(stderr, "rt_morton_sort_noalloc: %lld triangles exceed the fixed capacity of %d\n",
+                     (long long)n_tris, RT_NOALLOC_MAX_TRIS);
+        return RT_ERR_TOO_LARGE;
+    }
+    if (n_tris == 0) return RT_OK;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kNoAllocMaxDevices) return RT_ERR_CUDA;
+    void *base = nullptr;
+    {
+        std::lock_guard<std::mutex> lk(g_noalloc_mu);
+        if (!g_noalloc_ptr[dev]) {
+            void *p = nullptr;
+            if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) {
+                cudaGetLastError();
+                return RT_ERR_CUDA;
+            }
+            g_noalloc_ptr[dev] = p;
+        }
+        base = g_noalloc_ptr[dev];
+    }
+    const int n = (int)n_tris;
+    cudaStream_t s = (cudaStream_t)cuda_stream;
+    char *p = (char *)base;
+    Scratch sc{};
+    sc.box = (unsigned *)p;
+    float *obj_pos = (float *)(p + 256);
+    sc.centroid = (float4 *)(p + 512);
+    int *tri_obj = (int *)(p + 512 + 16 * kNoAllocN);
+    sc.codes[1] = (unsigned *)(p + 512 + 20 * kNoAllocN);
+    sc.idx[1] = (unsigned *)(p + 512 + 24 * kNoAllocN);
+    sc.hist = (unsigned *)(p + 512 + 28 * kNoAllocN);
+    sc.codes[0] = d_codes;   // the caller's outputs are the other sort buffer: 4 passes end there
+    sc.idx[0] = d_perm;
+    // the array keeps the previous call's bytes: zero the object table this call reads
+    if (cudaMemsetAsync(obj_pos, 0, 256, s) != cudaSuccess || cudaMemsetAsync(tri_obj, 0, 4 * (size_t)n, s) != cudaSuccess)
+        return RT_ERR_CUDA;
+    LbvhInput in{};
+    in.tri_p = d_tri_p;
+    in.tri_obj = tri_obj;
+    in.obj_pos = obj_pos;
+    in.n = n;
+    if (morton_and_sort(in, sc, s) != cudaSuccess) return RT_ERR_CUDA;
+    return RT_OK;
+}
