@@ -240,9 +240,10 @@ def run_gpu(args) -> None:
     dominant = max(("extend", "shadow", "shade"), key=lambda k: km[k])
     shadow_items = cnt.rays_shadow / 4           # one work item per hit, 4 lights
     alg = {
-        # queue record 80 B + 24 B fixed-point accumulate, then per light: 64 B per internal node
-        # visited (its two 32-B children), 36 B per triangle tested, 16 B per sphere tested
-        "shadow": shadow_items * (80 + 24) + 64 * cnt.shadow_nodes_visited + 36 * cnt.shadow_tris_tested
+        # per shadow ray (one thread per hit and light): the 80-B hit record and a 24-B
+        # fixed-point accumulate, then 64 B per internal node visited (the two 32-B child
+        # records of the pair), 36 B per triangle tested, 16 B per sphere tested
+        "shadow": cnt.rays_shadow * (80 + 24) + 64 * cnt.shadow_nodes_visited + 36 * cnt.shadow_tris_tested
         + 16 * cnt.shadow_spheres_tested,
         # ray 48 B read, hit 20 B written, then the traversal as above
         "extend": (cnt.rays_primary + cnt.rays_secondary) * (48 + 20) + 64 * cnt.nodes_visited

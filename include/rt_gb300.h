@@ -225,11 +225,17 @@ int rt_render_host(rt_ctx *ctx, const rt_scene_desc *desc, const rt_render_desc 
 
 /* ---- batched multi-scene rendering (persistent wavefront kernel + CUDA graph) ------------ */
 typedef struct rt_batch_tuning {
-    int32_t block;               /* threads per block of the traversal kernels (0 = autotune) */
-    int32_t tile;                /* rays taken per work-counter fetch (0 = autotune) */
-    int32_t stack;               /* traversal stack depth (0 = autotune) */
+    int32_t block;               /* threads per block of the traversal kernels (0 = default) */
+    int32_t tile;                /* rays taken per work-counter fetch (0 = default) */
+    int32_t stack;               /* traversal stack entries; 64 holds any LBVH (0 = default) */
     int32_t use_graph;           /* capture the per-bounce launch sequence as a CUDA graph */
+    int32_t min_blocks;          /* 0, 6, 8, 10 or 12: resident 128-thread blocks per SM the register
+                                    budget of the traversal kernels must allow (0 = compiler's) */
+    int32_t dynamic;             /* plain path: pull ray tiles from a counter (1) or stride (0) */
 } rt_batch_tuning;
+
+/* kernel tuning of the plain per-scene path (rt_render); NULL restores the defaults */
+int rt_ctx_set_tuning(rt_ctx *ctx, const rt_batch_tuning *tuning);
 
 /* render n (scene, frame, desc) jobs as one wavefront; returns after enqueueing */
 int rt_batch_render(rt_ctx *ctx, int32_t n, const int32_t *scene_ids, const int32_t *frame_ids,
@@ -310,8 +316,9 @@ int rt_morton_sort(rt_ctx *ctx, const float *tri_p, int64_t n_tris, uint32_t *co
 #define RT_NOALLOC_MAX_TRIS (1 << 18)
 int rt_morton_sort_noalloc(const float *d_tri_p, int64_t n_tris, uint32_t *d_codes, uint32_t *d_perm,
                            void *cuda_stream);
-/* download the LBVH of a scene: nodes float[(2n-1)*8] (min xyz, left | max xyz, right) and
-   the sorted triangle order perm[n] */
+/* download the LBVH of a scene with L leaves (triangles and spheres): nodes float[(2L-1)*8]
+   (min xyz, left | max xyz, right; leaf k is node L-1+k) and perm[L], the leaf order: the
+   reported id of a triangle leaf, 0x80000000 | primitive index of a sphere leaf */
 int rt_scene_bvh_download(rt_ctx *ctx, int32_t scene_id, float *nodes, uint32_t *perm,
                           int64_t *n_nodes);
 

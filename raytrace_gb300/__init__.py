@@ -88,7 +88,11 @@ class RenderStats(C.Structure):
 
 
 class BatchTuning(C.Structure):
-    _fields_ = [("block", C.c_int32), ("tile", C.c_int32), ("stack", C.c_int32), ("use_graph", C.c_int32)]
+    _fields_ = [("block", C.c_int32), ("tile", C.c_int32), ("stack", C.c_int32), ("use_graph", C.c_int32),
+                ("min_blocks", C.c_int32), ("dynamic", C.c_int32)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
 
 
 class ServerConfig(C.Structure):
@@ -139,6 +143,7 @@ _SIGS = {
     "rt_cancel": (C.c_int, [P]),
     "rt_poll": (C.c_int, [P]),
     "rt_render_host": (C.c_int, [P, C.POINTER(SceneDesc), C.POINTER(RenderDesc), P, P, C.POINTER(RenderStats)]),
+    "rt_ctx_set_tuning": (C.c_int, [P, C.POINTER(BatchTuning)]),
     "rt_batch_render": (C.c_int, [P, C.c_int32, P, P, P, C.POINTER(BatchTuning)]),
     "rt_batch_render_plain": (C.c_int, [P, C.c_int32, P, P, P]),
     "rt_batch_autotune": (C.c_int, [P, C.c_int32, P, P, P, C.POINTER(BatchTuning)]),
@@ -396,6 +401,9 @@ class Context:
         t = BatchTuning()
         self._ck(lib.rt_batch_autotune(self._h, n, _ptr(s), _ptr(f), C.cast(arr, P), C.byref(t)), "rt_batch_autotune")
         return t
+
+    def set_tuning(self, tuning: BatchTuning | None) -> None:
+        self._ck(lib.rt_ctx_set_tuning(self._h, C.byref(tuning) if tuning is not None else None), "rt_ctx_set_tuning")
 
     def synchronize(self) -> None:
         self._ck(lib.rt_ctx_synchronize(self._h), "rt_ctx_synchronize")

@@ -1,0 +1,74 @@
+"""Headless renderer CLI: render a seeded benchmark scene and write the image.
+
+Replaces the reference's window + glDrawPixels blit (main.cpp:197-208) with files: a binary
+PPM of the uint8 image (Color::put, bottom-up rows flipped to top-down for viewers) and
+optionally a PFM of the float colour.
+
+    python -m raytrace_gb300.cli --config 2 --width 960 --height 540 --out frame.ppm
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import sys
+
+import numpy as np
+
+from . import RT_FLAG_PROFILE, RT_FLAG_REF_TILES, Context, SceneHost
+
+
+def write_ppm(path: str, rgb8: np.ndarray) -> None:
+    h, w, _ = rgb8.shape
+    with open(path, "wb") as f:
+        f.write(f"P6\n{w} {h}\n255\n".encode())
+        f.write(np.ascontiguousarray(rgb8[::-1]).tobytes())
+
+
+def write_pfm(path: str, rgb: np.ndarray) -> None:
+    h, w, _ = rgb.shape
+    with open(path, "wb") as f:
+        f.write(f"PF\n{w} {h}\n-1.0\n".encode())   # little endian, rows bottom-up as stored
+        f.write(np.ascontiguousarray(rgb, "<f4").tobytes())
+
+
+def main(argv: list[str] | None = None) -> int:
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--config", type=int, default=0, help="benchmark scene 0..4")
+    ap.add_argument("--index", type=int, default=0, help="scene number inside configs 3 and 4")
+    ap.add_argument("--width", type=int, default=0)
+    ap.add_argument("--height", type=int, default=0)
+    ap.add_argument("--spp", type=int, default=0)
+    ap.add_argument("--level", type=int, default=-1)
+    ap.add_argument("--repeat", type=int, default=1)
+    ap.add_argument("--ref-tiles", action="store_true", help="only the reference's 64x64-tile region")
+    ap.add_argument("--out", default="")
+    ap.add_argument("--pfm", default="")
+    a = ap.parse_args(argv)
+    scene = SceneHost.config(a.config, a.index)
+    spp, lvl, seed = scene.params
+    cam = scene.desc.camera
+    w, h = a.width or cam.width, a.height or cam.height
+    if (w, h) != (cam.width, cam.height):
+        scene = scene.with_camera(w, h)
+    spp = a.spp or spp
+    lvl = lvl if a.level < 0 else a.level
+    with Context(0) as ctx:
+        sid = ctx.upload(scene)
+        fid = ctx.frame(w, h)
+        flags = RT_FLAG_PROFILE | (RT_FLAG_REF_TILES if a.ref_tiles else 0)
+        st = None
+        for _ in range(max(1, a.repeat)):
+            st = ctx.render(sid, fid, ctx.render_desc(w, h, spp, lvl, flags=flags, seed=seed))
+        out = ctx.download(fid, w, h, planes=False)
+        info = {"config": a.config, "width": w, "height": h, "spp": spp, "max_level": lvl,
+                "build_ms": ctx.build_ms(sid), **st.as_dict()}
+    if a.out:
+        write_ppm(a.out, out["rgb8"])
+    if a.pfm:
+        write_pfm(a.pfm, out["rgb"])
+    print(json.dumps(info))
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -92,7 +92,7 @@ static int batch_core(rt_ctx *ctx, int32_t n, const int32_t *scene_ids, const in
         if (plan.jobs[i].plane_obj) launch_plane_init(plan.frames[i]->fb, (long long)plan.frames[i]->w * plan.frames[i]->h, s);
     // per-wave sequence; captured once per (max_level, tuning) and replayed
     const long long key = ((long long)plan.max_level << 40) ^ ((long long)t.block << 24) ^ ((long long)t.tile << 8) ^
-                          (long long)t.stack ^ ((long long)t.dynamic << 50);
+                          (long long)t.stack ^ ((long long)t.dynamic << 50) ^ ((long long)t.min_blocks << 52);
     cudaGraphExec_t exec = nullptr;
     if (use_graph) {
         auto it = ctx->graphs.find(key);
@@ -121,7 +121,10 @@ static int batch_core(rt_ctx *ctx, int32_t n, const int32_t *scene_ids, const in
         ctx->h_scalars[0] = std::min(wave, total - first);
         ctx->h_scalars[1] = first;
         ctx->h_scalars[2] = (long long)plan.jobs.size();
-        cudaMemcpyAsync(ws.scalars, ctx->h_scalars, 24, cudaMemcpyHostToDevice, s);
+        long long ml = 0;
+        for (const DevScene &hd : hdrs) ml = std::max<long long>(ml, hd.n_lights);
+        ctx->h_scalars[3] = ml;
+        cudaMemcpyAsync(ws.scalars, ctx->h_scalars, 32, cudaMemcpyHostToDevice, s);
         if (exec)
             cudaGraphLaunch(exec, s);
         else {
@@ -151,20 +154,13 @@ extern "C" int rt_batch_render(rt_ctx *ctx, int32_t n, const int32_t *scene_ids,
                                const rt_render_desc *rds, const rt_batch_tuning *tuning)
 {
     if (!ctx) return RT_ERR_INVALID;
-    Tuning t;
-    t.dynamic = true;
-    t.block = 128;
-    t.tile = 256;
-    t.stack = 64;
+    Tuning t;   // defaults: persistent grid, 32-ray tiles, 128-thread blocks capped at 64 registers
     bool graph = true;
     if (tuning) {
-        if (tuning->block) t.block = tuning->block;
-        if (tuning->tile) t.tile = tuning->tile;
-        if (tuning->stack) t.stack = tuning->stack;
+        int rc = tuning_from(ctx, tuning, t);
+        if (rc) return rc;
         graph = tuning->use_graph != 0;
     }
-    if (t.block % 32 || t.block < 32 || t.block > 256 || t.tile % 32 || t.tile <= 0)
-        return ctx_fail(ctx, RT_ERR_INVALID, "tuning block %d / tile %d not supported", t.block, t.tile);
     return batch_core(ctx, n, scene_ids, frame_ids, rds, t, graph);
 }
 
@@ -192,13 +188,15 @@ extern "C" int rt_batch_autotune(rt_ctx *ctx, int32_t n, const int32_t *scene_id
                                  const rt_render_desc *rds, rt_batch_tuning *out)
 {
     if (!ctx || !out) return RT_ERR_INVALID;
-    const int blocks[] = {64, 128, 256};
-    const int tiles[] = {64, 256, 1024};
+    // (threads per block, register cap as resident blocks per SM) x rays per tile fetch; the
+    // stack stays at 64 entries, the depth bound of a 30-bit Morton LBVH with index tie-breaks
+    const int shapes[][2] = {{128, 8}, {128, 6}, {64, 8}, {256, 0}};
+    const int tiles[] = {32, 64, 128, 256};
     double best = 1e30;
-    rt_batch_tuning best_t{128, 256, 64, 1};
-    for (int b : blocks)
+    rt_batch_tuning best_t{128, 32, 64, 1, 8, 1};
+    for (const auto &sh : shapes)
         for (int tl : tiles) {
-            rt_batch_tuning t{b, tl, 64, 1};
+            rt_batch_tuning t{sh[0], tl, 64, 1, sh[1], 1};
             int rc = rt_batch_render(ctx, n, scene_ids, frame_ids, rds, &t);   // warm (captures the graph)
             if (rc) return rc;
             auto t0 = std::chrono::steady_clock::now();

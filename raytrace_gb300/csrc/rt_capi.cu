@@ -182,6 +182,7 @@ struct HostTables {
     std::vector<std::pair<int64_t, int64_t>> tri_ranges;   // (first, count) per shown model
     std::vector<int> tri_range_obj;
     int64_t n_tris = 0;
+    int n_linear = 0;   // prims before this index are planes / boxes, the rest spheres
 };
 
 static void build_tables(const rt_scene_desc *d, HostTables &h)
@@ -277,6 +278,12 @@ static void build_tables(const rt_scene_desc *d, HostTables &h)
             break;
         }
     }
+    // planes and boxes first (tested linearly per ray), spheres after them (LBVH leaves);
+    // the order among primitives does not matter: ties resolve by object index
+    std::stable_partition(h.prims.begin(), h.prims.end(), [](const DevPrim &p) { return p.type != kPrimSphere; });
+    h.n_linear = 0;
+    for (const DevPrim &p : h.prims)
+        if (p.type != kPrimSphere) ++h.n_linear;
 }
 
 extern "C" int rt_scene_upload(rt_ctx *ctx, const rt_scene_desc *d, int32_t *scene_id)
@@ -291,6 +298,7 @@ extern "C" int rt_scene_upload(rt_ctx *ctx, const rt_scene_desc *d, int32_t *sce
     sc->camera = d->camera;
     const int64_t n = h.n_tris;
     sc->n_tris = (int)n;
+    sc->n_leaves = (int)(n + (int64_t)h.prims.size() - h.n_linear);
     // one allocation for tables, triangle inputs and the LBVH
     size_t off = 0;
     auto take = [&](size_t bytes) {
@@ -309,9 +317,14 @@ extern "C" int rt_scene_upload(rt_ctx *ctx, const rt_scene_desc *d, int32_t *sce
     const size_t o_tuv = has_uv ? take(sizeof(float) * 6 * (size_t)n) : 0;
     const size_t o_tm = take(sizeof(int) * (size_t)n), o_ti = take(sizeof(int) * (size_t)n), o_to = take(sizeof(int) * (size_t)n);
     const size_t o_rng = take(sizeof(int) * 3 * std::max<size_t>(1, h.tri_ranges.size()));
-    const size_t o_nodes = take(sizeof(float4) * 2 * (size_t)std::max<int64_t>(1, 2 * n - 1));
-    const size_t o_tri = take(sizeof(float4) * 3 * (size_t)n), o_trin = take(sizeof(float4) * 3 * (size_t)n);
-    const size_t o_triuv = has_uv ? take(sizeof(float2) * 3 * (size_t)n) : 0;
+    const int n_sph = (int)h.prims.size() - h.n_linear;
+    const int64_t L = n + n_sph;   // LBVH leaves
+    const size_t o_sph = take(sizeof(float4) * (size_t)std::max(1, n_sph)), o_sphr = take(sizeof(float) * (size_t)std::max(1, n_sph));
+    const size_t o_sphp = take(sizeof(int) * (size_t)std::max(1, n_sph)), o_spho = take(sizeof(int) * (size_t)std::max(1, n_sph));
+    const size_t o_nodes = take(sizeof(float4) * 2 * (size_t)std::max<int64_t>(1, 2 * L - 1));
+    const size_t o_pairs = take(sizeof(float4) * 4 * (size_t)std::max<int64_t>(1, L - 1));
+    const size_t o_tri = take(sizeof(float4) * 3 * (size_t)L), o_trin = take(sizeof(float4) * 3 * (size_t)L);
+    const size_t o_triuv = has_uv ? take(sizeof(float2) * 3 * (size_t)L) : 0;
     const size_t o_hdr = take(sizeof(DevScene));
     CK(ctx, sc->mem.ensure(off));
     char *base = (char *)sc->mem.p;
@@ -375,11 +388,31 @@ extern "C" int rt_scene_upload(rt_ctx *ctx, const rt_scene_desc *d, int32_t *sce
     CK(ctx, cudaMemcpyAsync(base + o_tex, h.tex.data(), sizeof(DevTexture) * h.tex.size(), cudaMemcpyHostToDevice, s));
     CK(ctx, cudaMemcpyAsync(base + o_texels, h.texels.data(), h.texels.size(), cudaMemcpyHostToDevice, s));
     CK(ctx, cudaMemcpyAsync(base + o_objpos, h.obj_pos.data(), sizeof(float) * h.obj_pos.size(), cudaMemcpyHostToDevice, s));
+    if (n_sph > 0) {
+        std::vector<float4> sph((size_t)n_sph);
+        std::vector<float> sphr((size_t)n_sph);
+        std::vector<int> sphp((size_t)n_sph), spho((size_t)n_sph);
+        for (int j = 0; j < n_sph; ++j) {
+            const DevPrim &p = h.prims[(size_t)(h.n_linear + j)];
+            sph[(size_t)j] = p.a;
+            sphr[(size_t)j] = p.b.x;
+            sphp[(size_t)j] = h.n_linear + j;
+            spho[(size_t)j] = p.obj;
+        }
+        CK(ctx, cudaMemcpyAsync(base + o_sph, sph.data(), sizeof(float4) * sph.size(), cudaMemcpyHostToDevice, s));
+        CK(ctx, cudaMemcpyAsync(base + o_sphr, sphr.data(), sizeof(float) * sphr.size(), cudaMemcpyHostToDevice, s));
+        CK(ctx, cudaMemcpyAsync(base + o_sphp, sphp.data(), sizeof(int) * sphp.size(), cudaMemcpyHostToDevice, s));
+        CK(ctx, cudaMemcpyAsync(base + o_spho, spho.data(), sizeof(int) * spho.size(), cudaMemcpyHostToDevice, s));
+        CK(ctx, cudaStreamSynchronize(s));   // the staging vectors go out of scope
+    }
     DevScene &H = sc->hdr;
     H.prims = (const DevPrim *)(base + o_prims);
     H.n_prims = (int)h.prims.size();
+    H.n_linear = h.n_linear;
     H.n_tris = (int)n;
+    H.n_leaves = (int)L;
     H.nodes = (const float4 *)(base + o_nodes);
+    H.pairs = (const float4 *)(base + o_pairs);
     H.tri = (const float4 *)(base + o_tri);
     H.trin = (const float4 *)(base + o_trin);
     H.triuv = has_uv ? (const float2 *)(base + o_triuv) : nullptr;
@@ -400,7 +433,13 @@ extern "C" int rt_scene_upload(rt_ctx *ctx, const rt_scene_desc *d, int32_t *sce
     sc->in.tri_obj = (const int *)(base + o_to);
     sc->in.obj_pos = (const float *)(base + o_objpos);
     sc->in.n = (int)n;
+    sc->in.sph = (const float4 *)(base + o_sph);
+    sc->in.sph_r = (const float *)(base + o_sphr);
+    sc->in.sph_prim = (const int *)(base + o_sphp);
+    sc->in.sph_obj = (const int *)(base + o_spho);
+    sc->in.n_sph = n_sph;
     sc->out.nodes = (float4 *)(base + o_nodes);
+    sc->out.pairs = (float4 *)(base + o_pairs);
     sc->out.tri = (float4 *)(base + o_tri);
     sc->out.trin = (float4 *)(base + o_trin);
     sc->out.triuv = has_uv ? (float2 *)(base + o_triuv) : nullptr;
@@ -422,11 +461,11 @@ extern "C" int rt_scene_rebuild(rt_ctx *ctx, int32_t id)
     auto it = ctx->scenes.find(id);
     if (it == ctx->scenes.end()) return ctx_fail(ctx, RT_ERR_NOT_FOUND, "unknown scene %d", id);
     SceneDev &sc = *it->second;
-    if (sc.n_tris <= 0) {
+    if (sc.n_leaves <= 0) {
         sc.build_ms = 0.0f;
         return RT_OK;
     }
-    CK(ctx, ctx->lbvh_scratch.ensure(lbvh_scratch_bytes(sc.n_tris)));
+    CK(ctx, ctx->lbvh_scratch.ensure(lbvh_scratch_bytes(sc.n_leaves)));
     cudaEvent_t a, b;
     CK(ctx, cudaEventCreate(&a));
     CK(ctx, cudaEventCreate(&b));
@@ -562,7 +601,8 @@ extern "C" int rt_frame_download(rt_ctx *ctx, int32_t id, float *rgb, uint8_t *r
 // ---- workspace --------------------------------------------------------------------------------------------
 int ws_ensure(rt_ctx *ctx, Workspace &ws, long long qcap, int njobs)
 {
-    if (qcap > (1ll << 30)) return ctx_fail(ctx, RT_ERR_OOM, "ray queue of %lld rays is too large", qcap);
+    // queue capacity x 8 lights must fit the shadow kernel's int work index
+    if (qcap > (1ll << 27)) return ctx_fail(ctx, RT_ERR_OOM, "ray queue of %lld rays is too large", qcap);
     if (qcap <= ws.qcap && njobs <= ws.jobcap && ws.mem.p) return RT_OK;
     qcap = std::max(qcap, ws.qcap);
     njobs = std::max(njobs, ws.jobcap);
@@ -609,6 +649,7 @@ int ws_ensure(rt_ctx *ctx, Workspace &ws, long long qcap, int njobs)
     ws.wf.total_samples = ws.scalars;
     ws.wf.sample_offset = ws.scalars + 1;
     ws.wf.n_jobs = ws.scalars + 2;
+    ws.wf.max_lights = ws.scalars + 3;
     ws.wf.scenes = ws.scenes;
     ws.qcap = qcap;
     ws.jobcap = njobs;
@@ -697,12 +738,13 @@ static int render_once(rt_ctx *ctx, SceneDev &sc, FrameDev &f, const rt_render_d
     ctx->h_scalars[0] = samples;
     ctx->h_scalars[1] = 0;
     ctx->h_scalars[2] = 1;
+    ctx->h_scalars[3] = sc.hdr.n_lights;
     ctx->h_job_end[0] = samples;
     CK(ctx, cudaEventRecord(ctx->ev_start, s));
     CK(ctx, cudaMemcpyAsync(ws.scenes, &sc.hdr, sizeof(DevScene), cudaMemcpyHostToDevice, s));
     CK(ctx, cudaMemcpyAsync(ws.jobs, &J, sizeof(DevJob), cudaMemcpyHostToDevice, s));
     CK(ctx, cudaMemcpyAsync(ws.job_end, ctx->h_job_end, 8, cudaMemcpyHostToDevice, s));
-    CK(ctx, cudaMemcpyAsync(ws.scalars, ctx->h_scalars, 24, cudaMemcpyHostToDevice, s));
+    CK(ctx, cudaMemcpyAsync(ws.scalars, ctx->h_scalars, 32, cudaMemcpyHostToDevice, s));
     CK(ctx, cudaMemsetAsync(ws.wf.C, 0, sizeof(Counters), s));
     CK(ctx, cudaMemsetAsync(f.fb.acc, 0, 24 * (size_t)f.w * f.h, s));
     KernelProfiler &P = ctx->prof;
@@ -780,6 +822,36 @@ extern "C" int rt_render_wait(rt_ctx *ctx, rt_render_stats *stats)
     return RT_OK;
 }
 
+// shared by the plain path and the batch path: tuning values a kernel launch accepts
+int tuning_from(rt_ctx *ctx, const rt_batch_tuning *in, Tuning &t)
+{
+    if (!in) return RT_OK;
+    if (in->block) t.block = in->block;
+    if (in->tile) t.tile = in->tile;
+    if (in->stack) t.stack = in->stack;
+    t.min_blocks = in->min_blocks;
+    if (t.block % 32 || t.block < 32 || t.block > 256 || t.tile % 32 || t.tile <= 0)
+        return ctx_fail(ctx, RT_ERR_INVALID, "tuning block %d / tile %d not supported", t.block, t.tile);
+    if (t.min_blocks != 0 && t.min_blocks != 6 && t.min_blocks != 8 && t.min_blocks != 10 && t.min_blocks != 12)
+        return ctx_fail(ctx, RT_ERR_INVALID, "min_blocks %d: use 0, 6, 8, 10 or 12", t.min_blocks);
+    if (t.min_blocks && t.block > 128) return ctx_fail(ctx, RT_ERR_INVALID, "min_blocks needs blocks of at most 128 threads");
+    if (t.stack != 64) return ctx_fail(ctx, RT_ERR_INVALID, "stack %d: the traversal needs 64 entries", t.stack);
+    return RT_OK;
+}
+
+extern "C" int rt_ctx_set_tuning(rt_ctx *ctx, const rt_batch_tuning *tuning)
+{
+    if (!ctx) return RT_ERR_INVALID;
+    Tuning t;
+    if (tuning) {
+        int rc = tuning_from(ctx, tuning, t);
+        if (rc) return rc;
+        t.dynamic = tuning->dynamic != 0;
+    }
+    ctx->plain_tuning = t;
+    return RT_OK;
+}
+
 extern "C" int rt_cancel(rt_ctx *ctx)
 {
     if (!ctx) return RT_ERR_INVALID;
@@ -848,7 +920,7 @@ extern "C" int rt_scene_bvh_download(rt_ctx *ctx, int32_t id, float *nodes, uint
     auto it = ctx->scenes.find(id);
     if (it == ctx->scenes.end()) return ctx_fail(ctx, RT_ERR_NOT_FOUND, "unknown scene %d", id);
     SceneDev &sc = *it->second;
-    const int64_t n = sc.n_tris, nn = n > 0 ? 2 * n - 1 : 0;
+    const int64_t n = sc.n_leaves, nn = n > 0 ? 2 * n - 1 : 0;
     if (n_nodes) *n_nodes = nn;
     cudaStream_t s = ctx->stream;
     if (nodes && nn) CK(ctx, cudaMemcpyAsync(nodes, sc.out.nodes, 32 * (size_t)nn, cudaMemcpyDeviceToHost, s));
@@ -856,11 +928,11 @@ extern "C" int rt_scene_bvh_download(rt_ctx *ctx, int32_t id, float *nodes, uint
         std::vector<float4> tri((size_t)n * 3);
         CK(ctx, cudaMemcpyAsync(tri.data(), sc.out.tri, 48 * (size_t)n, cudaMemcpyDeviceToHost, s));
         CK(ctx, cudaStreamSynchronize(s));
-        for (int64_t k = 0; k < n; ++k) {
-            float w = tri[(size_t)k * 3].w;
-            int32_t id32;
-            std::memcpy(&id32, &w, 4);
-            perm[k] = (uint32_t)id32;
+        for (int64_t k = 0; k < n; ++k) {   // triangle: its reported id; sphere: 0x80000000 | primitive
+            int32_t id32, tag;
+            std::memcpy(&id32, &tri[(size_t)k * 3].w, 4);
+            std::memcpy(&tag, &tri[(size_t)k * 3 + 2].w, 4);
+            perm[k] = tag >= 0 ? (uint32_t)id32 : (0x80000000u | (uint32_t)(-1 - tag));
         }
     }
     CK(ctx, cudaStreamSynchronize(s));

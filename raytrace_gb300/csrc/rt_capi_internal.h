@@ -41,6 +41,7 @@ struct SceneDev {
     rtg::LbvhOutput out{};
     rt_camera camera{};
     int n_tris = 0;
+    int n_leaves = 0;   // triangles + spheres in the LBVH
     int64_t bytes = 0;
     float build_ms = 0.0f;
 };
@@ -160,5 +161,6 @@ int ws_ensure(rt_ctx *ctx, Workspace &ws, long long qcap, int njobs);
 int make_job(rt_ctx *ctx, const SceneDev &sc, FrameDev &f, const rt_render_desc *rd, int scene_slot, rtg::DevJob &J,
              long long &samples);
 // raygen + (extend, shade, shadow) per level; `prof` (may be NULL) brackets every launch
+int tuning_from(rt_ctx *ctx, const rt_batch_tuning *in, rtg::Tuning &t);
 void enqueue_levels(rt_ctx *ctx, Workspace &ws, int max_level, const rtg::Tuning &t, cudaStream_t s,
                     KernelProfiler *prof);

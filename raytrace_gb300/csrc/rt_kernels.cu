@@ -121,8 +121,9 @@ __global__ void k_raygen(Wavefront wf)
 }
 
 // ---- extend: closest hit -------------------------------------------------------------------
-template <int STACK, bool DYN, bool COUNT>
-__global__ void __launch_bounds__(256) k_extend(Wavefront wf, int sel, int wslot, int tile)
+// MINB > 0 caps registers so MINB blocks of 128 threads fit on an SM
+template <int STACK, bool DYN, bool COUNT, int MINB>
+__global__ void __launch_bounds__(MINB ? 128 : 256, MINB ? MINB : 1) k_extend(Wavefront wf, int sel, int wslot, int tile)
 {
     Counters *C = wf.C;
     if (blockIdx.x == 0 && threadIdx.x == 0) {   // the next queue and the shadow queue fill in shade
@@ -413,38 +414,43 @@ __global__ void __launch_bounds__(256) k_shade(Wavefront wf, int sel, int wslot,
 }
 
 // ---- shadow: per-light any-hit + direct light ---------------------------------------------------
-template <int STACK, bool DYN, bool COUNT>
-__global__ void __launch_bounds__(256) k_shadow(Wavefront wf, int wslot, int tile)
+template <int STACK, bool DYN, bool COUNT, int MINB>
+__global__ void __launch_bounds__(MINB ? 128 : 256, MINB ? MINB : 1) k_shadow(Wavefront wf, int wslot, int tile)
 {
     if (cancelled(wf.cancel)) return;
     Counters *C = wf.C;
     const ShadowQueue sq = wf.sq;
     const int n = min(C->s_count, sq.capacity);
+    const int nl = (int)*wf.max_lights;
     WorkCount wc{0, 0, 0, 0};
     unsigned long long rays = 0;
-    for_each_ray<DYN>(n, &C->work[wslot], tile, [&](int i, bool active) {
+    // one thread per (hit, light), light-major: neighbouring threads aim at the same light
+    // from neighbouring hit points, so their traversals stay coherent
+    for_each_ray<DYN>(n * nl, &C->work[wslot], tile, [&](int w, bool active) {
         if (!active) return;
-        const float4 p4 = sq.p[i], n4 = sq.n[i], v4 = sq.v[i], wc4 = sq.wc[i], ws4 = sq.ws[i];
+        const int l = w / n, i = w - l * n;
+        const float4 wc4 = sq.wc[i];
         const DevJob &J = wf.jobs[__float_as_int(wc4.w)];
         const DevScene &S = wf.scenes[J.scene];
+        if (l >= S.n_lights) return;
+        const DevLight &L = S.lights[l];
+        if (!L.on) return;
+        ++rays;
+        const float4 p4 = sq.p[i], v4 = sq.v[i];
+        const V3 P = mk(p4), D = mk(v4);
+        const LightTerm lt = light_term(L, P);
+        if (any_hit<STACK, COUNT>(S, P, lt.p2l, lt.dis, __float_as_int(v4.w), wc)) return;
+        const float4 n4 = sq.n[i], ws4 = sq.ws[i];
         const DevMaterial &M = S.mtl[__float_as_int(n4.w)];
-        const V3 P = mk(p4), N = mk(n4), D = mk(v4), Wc = mk(wc4), Ws = mk(ws4);
-        const int excl = __float_as_int(v4.w);
+        const V3 N = mk(n4), Wc = mk(wc4), Ws = mk(ws4);
+        V3 ld = mk(L.dif[0], L.dif[1], L.dif[2]), ls = mk(L.spec[0], L.spec[1], L.spec[2]);
+        if (lt.point) ld = vscale(ld, lt.lum), ls = vscale(ls, lt.lum);
         V3 sum = mk(0.0f, 0.0f, 0.0f);
-        for (int l = 0; l < S.n_lights; ++l) {
-            const DevLight &L = S.lights[l];
-            if (!L.on) continue;
-            ++rays;
-            const LightTerm lt = light_term(L, P);
-            if (any_hit<STACK, COUNT>(S, P, lt.p2l, lt.dis, excl, wc)) continue;
-            V3 ld = mk(L.dif[0], L.dif[1], L.dif[2]), ls = mk(L.spec[0], L.spec[1], L.spec[2]);
-            if (lt.point) ld = vscale(ld, lt.lum), ls = vscale(ls, lt.lum);
-            float nn = dot3(N, lt.p2l);
-            if (nn > 0) sum = vadd(sum, vmul(Wc, vscale(vmul(mk(M.kd[0], M.kd[1], M.kd[2]), ld), nn)));
-            const V3 h = normalise(vsub(lt.p2l, D));
-            nn = dot3(N, h);
-            if (nn > 0) sum = vadd(sum, vmul(Ws, vscale(vmul(mk(M.ks[0], M.ks[1], M.ks[2]), ls), powf(nn, M.shininess))));
-        }
+        float nn = dot3(N, lt.p2l);
+        if (nn > 0) sum = vmul(Wc, vscale(vmul(mk(M.kd[0], M.kd[1], M.kd[2]), ld), nn));
+        const V3 h = normalise(vsub(lt.p2l, D));
+        nn = dot3(N, h);
+        if (nn > 0) sum = vadd(sum, vmul(Ws, vscale(vmul(mk(M.ks[0], M.ks[1], M.ks[2]), ls), powf(nn, M.shininess))));
         acc_add(J.acc, __float_as_int(p4.w), sum);
     });
     if (wc.err) atomicOr(&C->error, wc.err);
@@ -526,27 +532,29 @@ void launch_raygen(const Wavefront &wf, int grid, int block, cudaStream_t s)
     k_raygen<<<grid, block, 0, s>>>(wf);
 }
 
-template <int STACK>
-static void extend_stack(const Wavefront &wf, int sel, int wslot, const Tuning &t, cudaStream_t s)
+template <bool DYN, bool CNT>
+static void extend_launch(const Wavefront &wf, int sel, int wslot, const Tuning &t, cudaStream_t s)
 {
-#define RT_EXT(DYN, CNT)                                                                                          \
+#define RT_EXT(MB)                                                                                                \
     {                                                                                                             \
-        auto k = k_extend<STACK, DYN, CNT>;                                                                       \
+        auto k = k_extend<64, DYN, CNT, MB>;                                                                      \
         k<<<grid_for(t, (const void *)k), t.block, 0, s>>>(wf, sel, wslot, t.tile);                              \
     }
-    if (t.dynamic) {
-        if (t.count) RT_EXT(true, true) else RT_EXT(true, false)
-    } else {
-        if (t.count) RT_EXT(false, true) else RT_EXT(false, false)
-    }
+    if (t.min_blocks == 8) RT_EXT(8) else if (t.min_blocks == 6) RT_EXT(6) else if (t.min_blocks == 10) RT_EXT(10)
+    else if (t.min_blocks == 12) RT_EXT(12) else RT_EXT(0)
 #undef RT_EXT
 }
 
 void launch_extend(const Wavefront &wf, int sel, int level, const Tuning &t, cudaStream_t s)
 {
     const int wslot = 3 * level;
-    if (t.stack <= 32) extend_stack<32>(wf, sel, wslot, t, s);
-    else extend_stack<64>(wf, sel, wslot, t, s);
+    if (t.dynamic) {
+        if (t.count) extend_launch<true, true>(wf, sel, wslot, t, s);
+        else extend_launch<true, false>(wf, sel, wslot, t, s);
+    } else {
+        if (t.count) extend_launch<false, true>(wf, sel, wslot, t, s);
+        else extend_launch<false, false>(wf, sel, wslot, t, s);
+    }
 }
 
 void launch_shade(const Wavefront &wf, int sel, int level, const Tuning &t, cudaStream_t s)
@@ -561,27 +569,29 @@ void launch_shade(const Wavefront &wf, int sel, int level, const Tuning &t, cuda
     }
 }
 
-template <int STACK>
-static void shadow_stack(const Wavefront &wf, int wslot, const Tuning &t, cudaStream_t s)
+template <bool DYN, bool CNT>
+static void shadow_launch(const Wavefront &wf, int wslot, const Tuning &t, cudaStream_t s)
 {
-#define RT_SHD(DYN, CNT)                                                                                          \
+#define RT_SHD(MB)                                                                                                \
     {                                                                                                             \
-        auto k = k_shadow<STACK, DYN, CNT>;                                                                       \
+        auto k = k_shadow<64, DYN, CNT, MB>;                                                                      \
         k<<<grid_for(t, (const void *)k), t.block, 0, s>>>(wf, wslot, t.tile);                                   \
     }
-    if (t.dynamic) {
-        if (t.count) RT_SHD(true, true) else RT_SHD(true, false)
-    } else {
-        if (t.count) RT_SHD(false, true) else RT_SHD(false, false)
-    }
+    if (t.min_blocks == 8) RT_SHD(8) else if (t.min_blocks == 6) RT_SHD(6) else if (t.min_blocks == 10) RT_SHD(10)
+    else if (t.min_blocks == 12) RT_SHD(12) else RT_SHD(0)
 #undef RT_SHD
 }
 
 void launch_shadow(const Wavefront &wf, int level, const Tuning &t, cudaStream_t s)
 {
     const int wslot = 3 * level + 2;
-    if (t.stack <= 32) shadow_stack<32>(wf, wslot, t, s);
-    else shadow_stack<64>(wf, wslot, t, s);
+    if (t.dynamic) {
+        if (t.count) shadow_launch<true, true>(wf, wslot, t, s);
+        else shadow_launch<true, false>(wf, wslot, t, s);
+    } else {
+        if (t.count) shadow_launch<false, true>(wf, wslot, t, s);
+        else shadow_launch<false, false>(wf, wslot, t, s);
+    }
 }
 
 void launch_resolve(const FrameBufs &fb, int width, int height, int spp, cudaStream_t s)

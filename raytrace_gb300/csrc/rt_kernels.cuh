@@ -24,6 +24,7 @@ struct Wavefront {
     const long long *total_samples;   // device scalar: samples in this wave
     const long long *sample_offset;   // device scalar: global index of the wave's first sample
     const long long *n_jobs;          // device scalar: jobs in the job table
+    const long long *max_lights;      // device scalar: most lights of any scene in the wave
     RayQueue q[2];
     ShadowQueue sq;
     float4 *hit;
@@ -34,11 +35,12 @@ struct Wavefront {
 
 struct Tuning {
     int block = 128;     // threads per block of the traversal kernels
-    int tile = 256;      // rays per dynamic work fetch (multiple of 32)
+    int tile = 32;       // rays per dynamic work fetch (multiple of 32)
     int stack = 64;      // traversal stack entries
-    bool dynamic = false;// persistent grid pulling tiles from a global counter
+    bool dynamic = true; // persistent grid pulling tiles from a global counter
     bool count = false;  // count BVH nodes / triangles / spheres
     int grid = 0;        // blocks (0 = derived from the SM count)
+    int min_blocks = 8;  // 0, 6, 8, 10 or 12: register cap of the traversal kernels (128-thread blocks)
 };
 
 int sm_count();

@@ -38,9 +38,21 @@ struct TriWorld {
     float p0[3], e1[3], e2[3], mn[3], mx[3];
 };
 
-__device__ __forceinline__ TriWorld tri_world(const LbvhInput &in, int i)
+__device__ __forceinline__ TriWorld leaf_world(const LbvhInput &in, int i)
 {
     TriWorld w;
+    if (i >= in.n) {   // sphere leaf: box = centre +- radius
+        const int s = i - in.n;
+        const float4 c = in.sph[s];
+        const float r = in.sph_r[s];
+        const float cc[3] = {c.x, c.y, c.z};
+        for (int k = 0; k < 3; ++k) {
+            w.p0[k] = cc[k], w.e1[k] = 0.0f, w.e2[k] = 0.0f;
+            w.mn[k] = __fsub_rn(cc[k], r);
+            w.mx[k] = __fadd_rn(cc[k], r);
+        }
+        return w;
+    }
     const float *p = in.tri_p + 9ll * i;
     const float *pos = in.obj_pos + 3ll * in.tri_obj[i];
     for (int k = 0; k < 3; ++k) {
@@ -60,8 +72,9 @@ __global__ void k_prep(LbvhInput in, float4 *centroid, unsigned *box)
     if (threadIdx.x < 3) smn[threadIdx.x] = 0xffffffffu, smx[threadIdx.x] = 0u;
     __syncthreads();
     unsigned lmn[3] = {0xffffffffu, 0xffffffffu, 0xffffffffu}, lmx[3] = {0u, 0u, 0u};
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < in.n; i += gridDim.x * blockDim.x) {
-        TriWorld w = tri_world(in, i);
+    const int total = in.n + in.n_sph;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+        TriWorld w = leaf_world(in, i);
         float c[3];
         for (int k = 0; k < 3; ++k) {
             c[k] = __fmul_rn(__fadd_rn(w.mn[k], w.mx[k]), 0.5f);
@@ -211,22 +224,32 @@ __global__ void __launch_bounds__(kSortThreads) k_scatter(int n, const unsigned 
 // ---- gather, hierarchy, refit -------------------------------------------------------------------
 __global__ void k_gather(LbvhInput in, LbvhOutput out, const unsigned *perm, const unsigned *box)
 {
-    const int n = in.n;
+    const int n = in.n + in.n_sph;
     // absolute padding from the scene size: 2^-20 of its largest coordinate magnitude
     float scene_mag = 0.0f;
     for (int k = 0; k < 6; ++k) scene_mag = fmaxf(scene_mag, fabsf(ord2f(box[k])));
     const float pad_abs = scene_mag * (1.0f / 1048576.0f);
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
         const int i = (int)perm[k];
-        TriWorld w = tri_world(in, i);
-        out.tri[3ll * k] = make_float4(w.p0[0], w.p0[1], w.p0[2], __int_as_float(in.tri_id[i]));
-        out.tri[3ll * k + 1] = make_float4(w.e1[0], w.e1[1], w.e1[2], __int_as_float(in.tri_obj[i]));
-        out.tri[3ll * k + 2] = make_float4(w.e2[0], w.e2[1], w.e2[2], __int_as_float(in.tri_mtl[i]));
-        const float *nn = in.tri_n + 9ll * i;
-        for (int j = 0; j < 3; ++j) out.trin[3ll * k + j] = make_float4(nn[3 * j], nn[3 * j + 1], nn[3 * j + 2], 0.0f);
-        if (out.triuv) {
-            const float *uv = in.tri_uv ? in.tri_uv + 6ll * i : nullptr;
-            for (int j = 0; j < 3; ++j) out.triuv[3ll * k + j] = uv ? make_float2(uv[2 * j], uv[2 * j + 1]) : make_float2(0, 0);
+        TriWorld w = leaf_world(in, i);
+        if (i < in.n) {
+            out.tri[3ll * k] = make_float4(w.p0[0], w.p0[1], w.p0[2], __int_as_float(in.tri_id[i]));
+            out.tri[3ll * k + 1] = make_float4(w.e1[0], w.e1[1], w.e1[2], __int_as_float(in.tri_obj[i]));
+            out.tri[3ll * k + 2] = make_float4(w.e2[0], w.e2[1], w.e2[2], __int_as_float(in.tri_mtl[i]));
+            const float *nn = in.tri_n + 9ll * i;
+            for (int j = 0; j < 3; ++j) out.trin[3ll * k + j] = make_float4(nn[3 * j], nn[3 * j + 1], nn[3 * j + 2], 0.0f);
+            if (out.triuv) {
+                const float *uv = in.tri_uv ? in.tri_uv + 6ll * i : nullptr;
+                for (int j = 0; j < 3; ++j) out.triuv[3ll * k + j] = uv ? make_float2(uv[2 * j], uv[2 * j + 1]) : make_float2(0, 0);
+            }
+        } else {
+            const int sidx = i - in.n;
+            out.tri[3ll * k] = in.sph[sidx];
+            out.tri[3ll * k + 1] = make_float4(0.0f, 0.0f, 0.0f, __int_as_float(in.sph_obj[sidx]));
+            out.tri[3ll * k + 2] = make_float4(0.0f, 0.0f, 0.0f, __int_as_float(-1 - in.sph_prim[sidx]));
+            for (int j = 0; j < 3; ++j) out.trin[3ll * k + j] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            if (out.triuv)
+                for (int j = 0; j < 3; ++j) out.triuv[3ll * k + j] = make_float2(0, 0);
         }
         // padded leaf box: the exact triangle test may accept a hit a few ulps outside
         float mag = 0.0f, ext = 0.0f;
@@ -298,6 +321,20 @@ __global__ void k_refit(int n, float4 *nodes, const int *parent, int *flags)
     }
 }
 
+// both children of internal node i side by side: one 64-byte load per traversal step
+__global__ void k_pairs(int n, const float4 *nodes, float4 *pairs)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n - 1; i += gridDim.x * blockDim.x) {
+        const int c[2] = {__float_as_int(nodes[2ll * i].w), __float_as_int(nodes[2ll * i + 1].w)};
+        for (int j = 0; j < 2; ++j) {
+            const float4 lo = __ldcg(&nodes[2ll * c[j]]), hi = __ldcg(&nodes[2ll * c[j] + 1]);
+            const int ref = c[j] >= n - 1 ? ~(c[j] - (n - 1)) : c[j];
+            pairs[4ll * i + 2 * j] = make_float4(lo.x, lo.y, lo.z, __int_as_float(ref));
+            pairs[4ll * i + 2 * j + 1] = make_float4(hi.x, hi.y, hi.z, 0.0f);
+        }
+    }
+}
+
 struct Scratch {
     unsigned *box;        // 8
     float4 *centroid;     // n
@@ -342,7 +379,7 @@ int grid_of(long long n, int block)
 // sorted codes end in codes[0] / idx[0] after an even number of passes
 cudaError_t morton_and_sort(const LbvhInput &in, const Scratch &sc, cudaStream_t s)
 {
-    const int n = in.n;
+    const int n = in.n + in.n_sph;
     const int tiles = (n + kTileKeys - 1) / kTileKeys;
     cudaMemsetAsync(sc.box, 0xff, 12, s);
     cudaMemsetAsync(sc.box + 3, 0, 12, s);
@@ -389,18 +426,19 @@ size_t lbvh_scratch_bytes(int n)
 
 cudaError_t lbvh_morton_sort(const LbvhInput &in, uint32_t *codes_out, uint32_t *perm_out, void *scratch, cudaStream_t s)
 {
-    if (in.n <= 0) return cudaSuccess;
-    Scratch sc = carve(scratch, in.n);
+    const int n = in.n + in.n_sph;
+    if (n <= 0) return cudaSuccess;
+    Scratch sc = carve(scratch, n);
     cudaError_t e = morton_and_sort(in, sc, s);
     if (e != cudaSuccess) return e;
-    cudaMemcpyAsync(codes_out, sc.codes[0], 4 * (size_t)in.n, cudaMemcpyDeviceToDevice, s);
-    cudaMemcpyAsync(perm_out, sc.idx[0], 4 * (size_t)in.n, cudaMemcpyDeviceToDevice, s);
+    cudaMemcpyAsync(codes_out, sc.codes[0], 4 * (size_t)n, cudaMemcpyDeviceToDevice, s);
+    cudaMemcpyAsync(perm_out, sc.idx[0], 4 * (size_t)n, cudaMemcpyDeviceToDevice, s);
     return cudaGetLastError();
 }
 
 cudaError_t lbvh_build(const LbvhInput &in, const LbvhOutput &out, void *scratch, cudaStream_t s)
 {
-    const int n = in.n;
+    const int n = in.n + in.n_sph;
     if (n <= 0) return cudaSuccess;
     Scratch sc = carve(scratch, n);
     cudaError_t e = morton_and_sort(in, sc, s);
@@ -410,6 +448,7 @@ cudaError_t lbvh_build(const LbvhInput &in, const LbvhOutput &out, void *scratch
         k_karras<<<grid_of(n - 1, 256), 256, 0, s>>>(n, sc.codes[0], out.nodes, sc.parent);
         cudaMemsetAsync(sc.flags, 0, 4 * (size_t)(n - 1), s);
         k_refit<<<grid_of(n, 256), 256, 0, s>>>(n, out.nodes, sc.parent, sc.flags);
+        if (out.pairs) k_pairs<<<grid_of(n - 1, 256), 256, 0, s>>>(n, out.nodes, out.pairs);
     }
     return cudaGetLastError();
 }

@@ -12,17 +12,27 @@ struct LbvhInput {
     const float *tri_p, *tri_n, *tri_uv;
     const int *tri_mtl, *tri_id, *tri_obj;
     const float *obj_pos;
-    int n;
+    int n;                 // triangles
+    // spheres as further leaves after the triangles (NULL / 0 when none)
+    const float4 *sph;     // centre xyz, r*r (the exact test's data)
+    const float *sph_r;    // radius (leaf box half extent)
+    const int *sph_prim;   // analytic primitive index = the hit key
+    const int *sph_obj;    // object order
+    int n_sph;
 };
 
+// leaves = n + n_sph; leaf record k (Morton order), 3 float4:
+//   triangle: (p0 | reported id), (e1 | object), (e2 | material >= 0)
+//   sphere:   (centre | r*r),     (0 | object),  (0 | -1 - primitive index)
 struct LbvhOutput {
-    float4 *nodes;   // 2 * (2n-1)
-    float4 *tri;     // 3n
-    float4 *trin;    // 3n
-    float2 *triuv;   // 3n or NULL
+    float4 *nodes;   // 2 * (2L-1): own box per node, for refit and inspection
+    float4 *pairs;   // 4 * (L-1): per internal node both children (min|child, max|-), child < 0 = leaf ~k
+    float4 *tri;     // 3L leaf records
+    float4 *trin;    // 3L (vertex normals; zero for spheres)
+    float2 *triuv;   // 3L or NULL
 };
 
-// scratch bytes needed for n triangles
+// scratch bytes needed for n leaves (triangles + spheres)
 size_t lbvh_scratch_bytes(int n);
 // build into `out` using `scratch` (lbvh_scratch_bytes(n) bytes, 256-byte aligned)
 cudaError_t lbvh_build(const LbvhInput &in, const LbvhOutput &out, void *scratch, cudaStream_t s);

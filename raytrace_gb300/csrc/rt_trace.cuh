@@ -141,6 +141,21 @@ struct WorkCount {
 // corrupt tree into an error flag instead of a fault or an endless loop
 constexpr unsigned kMaxVisits = 1u << 22;
 
+// ---- LBVH leaf tests -------------------------------------------------------------------------
+// Leaf k holds a triangle (tag = material >= 0) or a sphere (tag = -1 - primitive index).
+struct Leaf {
+    float4 a, b, c;
+};
+// a child reference is an internal node 0..last or a leaf ~k with k < n_leaves
+__device__ __forceinline__ bool child_ok(int c, unsigned last, int n_leaves)
+{
+    return c >= 0 ? (unsigned)c <= last : (unsigned)~c < (unsigned)n_leaves;
+}
+__device__ __forceinline__ Leaf load_leaf(const float4 *__restrict__ tri, int k)
+{
+    return Leaf{__ldg(&tri[3 * k]), __ldg(&tri[3 * k + 1]), __ldg(&tri[3 * k + 2])};
+}
+
 // ---- closest hit ---------------------------------------------------------------------------
 // excl: the ray's exclude key (-1 = none). inside: Ray::isInside != 0. Writes the winner to
 // `best` and the exclude key for the children to `newobj`.
@@ -165,77 +180,77 @@ __device__ void closest_hit(const DevScene &S, V3 O, V3 D, int excl, bool inside
     before.t = kMiss;
     before.key = -1;
     before.ord = -1;
+    auto consider = [&](float t, int key, int ord, float u, float v) {
+        if (better(t, ord, best.t, best.ord)) best.t = t, best.key = key, best.ord = ord, best.u = u, best.v = v;
+        if (self_inside && ord < self_ord && key != excl && better(t, ord, before.t, before.ord))
+            before.t = t, before.key = key, before.ord = ord;
+    };
 
-    for (int p = 0; p < S.n_prims; ++p) {
+    // planes and boxes: unbounded or few, tested linearly
+    for (int p = 0; p < S.n_linear; ++p) {
+        if (p == excl) continue;
         const DevPrim &P = S.prims[p];
         float t;
-        bool ok;
-        if (P.type == kPrimSphere) {
-            if (COUNT) wc.spheres++;
-            if (p == excl) {
-                if (!inside) continue;
-                ok = sphere_inside(O, D, P.a, t);
-            } else
-                ok = sphere_outside(O, D, P.a, t);
-        } else if (p == excl)
-            continue;
-        else if (P.type == kPrimPlane)
-            ok = plane_hit(O, D, P, t);
-        else
-            ok = box_hit(O, D, P, t);
-        if (!ok) continue;
-        if (better(t, P.obj, best.t, best.ord)) best.t = t, best.key = p, best.ord = P.obj;
-        if (self_inside && P.obj < self_ord && p != excl && better(t, P.obj, before.t, before.ord))
-            before.t = t, before.key = p, before.ord = P.obj;
+        const bool ok = P.type == kPrimPlane ? plane_hit(O, D, P, t) : box_hit(O, D, P, t);
+        if (ok) consider(t, p, P.obj, 0.0f, 0.0f);
     }
 
-    if (S.n_tris > 0) {
-        const float4 *__restrict__ nodes = S.nodes;
+    if (S.n_leaves > 0) {
         const float4 *__restrict__ tri = S.tri;
-        const int leaf0 = S.n_tris - 1;
-        RayInv ri = make_inv(O, D);
         auto test_leaf = [&](int k) {
-            if (COUNT) wc.tris++;
-            if ((k | kTriFlag) == excl) return;
-            float4 a = __ldg(&tri[3 * k]), b = __ldg(&tri[3 * k + 1]), c = __ldg(&tri[3 * k + 2]);
-            float t, u, v;
-            if (!tri_test(O, D, mk(a), mk(b), mk(c), t, u, v)) return;
-            int ord = __float_as_int(b.w);
-            if (better(t, ord, best.t, best.ord)) best.t = t, best.key = k | kTriFlag, best.ord = ord, best.u = u, best.v = v;
-            if (self_inside && ord < self_ord && better(t, ord, before.t, before.ord))
-                before.t = t, before.key = k | kTriFlag, before.ord = ord;
+            const Leaf L = load_leaf(tri, k);
+            const int tag = __float_as_int(L.c.w);
+            const int ord = __float_as_int(L.b.w);
+            float t;
+            if (tag >= 0) {   // triangle
+                if (COUNT) wc.tris++;
+                if ((k | kTriFlag) == excl) return;
+                float u, v;
+                if (tri_test(O, D, mk(L.a), mk(L.b), mk(L.c), t, u, v)) consider(t, k | kTriFlag, ord, u, v);
+            } else {          // sphere
+                if (COUNT) wc.spheres++;
+                const int p = -1 - tag;
+                bool ok;
+                if (p == excl) {
+                    if (!inside) return;
+                    ok = sphere_inside(O, D, L.a, t);
+                } else
+                    ok = sphere_outside(O, D, L.a, t);
+                if (ok) consider(t, p, ord, 0.0f, 0.0f);
+            }
         };
-        if (S.n_tris == 1) {
+        if (S.n_leaves == 1) {
             test_leaf(0);
         } else {
+            const float4 *__restrict__ pairs = S.pairs;
+            const RayInv ri = make_inv(O, D);
+            const unsigned last = (unsigned)S.n_leaves - 2u;   // internal nodes 0..L-2
             int stack[STACK];
             int sp = 0;
             int node = 0;
-            const unsigned last = 2u * (unsigned)S.n_tris - 2u;
             for (unsigned visits = 0;; ++visits) {
                 if (COUNT) wc.nodes++;
-                float4 lo = __ldg(&nodes[2 * node]), hi = __ldg(&nodes[2 * node + 1]);
-                int c0 = __float_as_int(lo.w), c1 = __float_as_int(hi.w);
-                if ((unsigned)c0 > last || (unsigned)c1 > last || visits >= kMaxVisits) {
+                const float4 l0 = __ldg(&pairs[4 * node]), h0 = __ldg(&pairs[4 * node + 1]);
+                const float4 l1 = __ldg(&pairs[4 * node + 2]), h1 = __ldg(&pairs[4 * node + 3]);
+                const int c0 = __float_as_int(l0.w), c1 = __float_as_int(l1.w);
+                if (!child_ok(c0, last, S.n_leaves) || !child_ok(c1, last, S.n_leaves) || visits >= kMaxVisits) {
                     wc.err |= visits >= kMaxVisits ? 2 : 1;
                     break;
                 }
-                float4 l0 = __ldg(&nodes[2 * c0]), h0 = __ldg(&nodes[2 * c0 + 1]);
-                float4 l1 = __ldg(&nodes[2 * c1]), h1 = __ldg(&nodes[2 * c1 + 1]);
-                float cull = self_inside ? before.t : best.t;
+                const float cull = self_inside ? before.t : best.t;
                 bool hit0, hit1;
-                float tn0 = slab(ri, l0, h0, cull, hit0);
-                float tn1 = slab(ri, l1, h1, cull, hit1);
-                if (hit0 && c0 >= leaf0) {
-                    test_leaf(c0 - leaf0);
+                const float tn0 = slab(ri, l0, h0, cull, hit0);
+                const float tn1 = slab(ri, l1, h1, cull, hit1);
+                if (hit0 && c0 < 0) {
+                    test_leaf(~c0);
                     hit0 = false;
                 }
-                if (hit1 && c1 >= leaf0) {
-                    test_leaf(c1 - leaf0);
+                if (hit1 && c1 < 0) {
+                    test_leaf(~c1);
                     hit1 = false;
                 }
                 if (hit0 && hit1) {
-                    int nearc = tn0 <= tn1 ? c0 : c1, farc = tn0 <= tn1 ? c1 : c0;
+                    const int nearc = tn0 <= tn1 ? c0 : c1, farc = tn0 <= tn1 ? c1 : c0;
                     if (sp < STACK) stack[sp++] = farc;
                     else wc.err |= 4;
                     node = nearc;
@@ -263,60 +278,58 @@ __device__ void closest_hit(const DevScene &S, V3 O, V3 D, int excl, bool inside
 template <int STACK, bool COUNT>
 __device__ bool any_hit(const DevScene &S, V3 O, V3 D, float dis, int excl, WorkCount &wc)
 {
-    for (int p = 0; p < S.n_prims; ++p) {
+    for (int p = 0; p < S.n_linear; ++p) {
         if (p == excl) continue;   // shadow rays are never inside: the own primitive is skipped
         const DevPrim &P = S.prims[p];
         float t;
-        bool ok;
-        if (P.type == kPrimSphere) {
-            if (COUNT) wc.spheres++;
-            ok = sphere_outside(O, D, P.a, t);
-        } else if (P.type == kPrimPlane)
-            ok = plane_hit(O, D, P, t);
-        else
-            ok = box_hit(O, D, P, t);
+        const bool ok = P.type == kPrimPlane ? plane_hit(O, D, P, t) : box_hit(O, D, P, t);
         if (ok && t < dis) return true;
     }
-    if (S.n_tris == 0) return false;
-    const float4 *__restrict__ nodes = S.nodes;
+    if (S.n_leaves == 0) return false;
     const float4 *__restrict__ tri = S.tri;
-    const int leaf0 = S.n_tris - 1;
     auto test_leaf = [&](int k) -> bool {
-        if (COUNT) wc.tris++;
-        if ((k | kTriFlag) == excl) return false;
-        float4 a = __ldg(&tri[3 * k]), b = __ldg(&tri[3 * k + 1]), c = __ldg(&tri[3 * k + 2]);
-        float t, u, v;
-        return tri_test(O, D, mk(a), mk(b), mk(c), t, u, v) && t < dis;
+        const Leaf L = load_leaf(tri, k);
+        const int tag = __float_as_int(L.c.w);
+        float t;
+        if (tag >= 0) {
+            if (COUNT) wc.tris++;
+            if ((k | kTriFlag) == excl) return false;
+            float u, v;
+            return tri_test(O, D, mk(L.a), mk(L.b), mk(L.c), t, u, v) && t < dis;
+        }
+        if (COUNT) wc.spheres++;
+        if (-1 - tag == excl) return false;
+        return sphere_outside(O, D, L.a, t) && t < dis;
     };
-    if (S.n_tris == 1) return test_leaf(0);
-    RayInv ri = make_inv(O, D);
+    if (S.n_leaves == 1) return test_leaf(0);
+    const float4 *__restrict__ pairs = S.pairs;
+    const RayInv ri = make_inv(O, D);
+    const unsigned last = (unsigned)S.n_leaves - 2u;
     int stack[STACK];
     int sp = 0;
     int node = 0;
-    const unsigned last = 2u * (unsigned)S.n_tris - 2u;
     for (unsigned visits = 0;; ++visits) {
         if (COUNT) wc.nodes++;
-        float4 lo = __ldg(&nodes[2 * node]), hi = __ldg(&nodes[2 * node + 1]);
-        int c0 = __float_as_int(lo.w), c1 = __float_as_int(hi.w);
-        if ((unsigned)c0 > last || (unsigned)c1 > last || visits >= kMaxVisits) {
+        const float4 l0 = __ldg(&pairs[4 * node]), h0 = __ldg(&pairs[4 * node + 1]);
+        const float4 l1 = __ldg(&pairs[4 * node + 2]), h1 = __ldg(&pairs[4 * node + 3]);
+        const int c0 = __float_as_int(l0.w), c1 = __float_as_int(l1.w);
+        if (!child_ok(c0, last, S.n_leaves) || !child_ok(c1, last, S.n_leaves) || visits >= kMaxVisits) {
             wc.err |= visits >= kMaxVisits ? 2 : 1;
             return false;
         }
-        float4 l0 = __ldg(&nodes[2 * c0]), h0 = __ldg(&nodes[2 * c0 + 1]);
-        float4 l1 = __ldg(&nodes[2 * c1]), h1 = __ldg(&nodes[2 * c1 + 1]);
         bool hit0, hit1;
-        float tn0 = slab(ri, l0, h0, dis, hit0);
-        float tn1 = slab(ri, l1, h1, dis, hit1);
-        if (hit0 && c0 >= leaf0) {
-            if (test_leaf(c0 - leaf0)) return true;
+        const float tn0 = slab(ri, l0, h0, dis, hit0);
+        const float tn1 = slab(ri, l1, h1, dis, hit1);
+        if (hit0 && c0 < 0) {
+            if (test_leaf(~c0)) return true;
             hit0 = false;
         }
-        if (hit1 && c1 >= leaf0) {
-            if (test_leaf(c1 - leaf0)) return true;
+        if (hit1 && c1 < 0) {
+            if (test_leaf(~c1)) return true;
             hit1 = false;
         }
         if (hit0 && hit1) {
-            int nearc = tn0 <= tn1 ? c0 : c1, farc = tn0 <= tn1 ? c1 : c0;
+            const int nearc = tn0 <= tn1 ? c0 : c1, farc = tn0 <= tn1 ? c1 : c0;
             if (sp < STACK) stack[sp++] = farc;
             else wc.err |= 4;
             node = nearc;

@@ -173,31 +173,44 @@ def test_morton_sort_bit_exact(ctx):
 
 
 def test_lbvh_invariants(ctx):
+    """Leaves (triangles and spheres) all reachable exactly once, child boxes inside parent
+    boxes, depth <= 64, and every leaf box contains its primitive."""
     scene = rt.SceneHost.config(3, 5)
     sid = ctx.upload(scene)
     nodes, perm = ctx.bvh(sid)
     ctx.release_scene(sid)
-    n = scene.desc.n_tris
-    assert nodes.shape[0] == 2 * n - 1
-    assert sorted(perm.tolist()) == list(range(n))   # single model: ids are 0..n-1
+    d = scene.desc
+    n_tri = d.n_tris
+    spheres = [d.objects[k] for k in range(d.n_objects) if d.objects[k].type == rt.RT_OBJECT_SPHERE]
+    L = n_tri + len(spheres)
+    assert nodes.shape[0] == 2 * L - 1
+    is_sph = (perm & 0x80000000) != 0
+    assert sorted(perm[~is_sph].tolist()) == list(range(n_tri))   # single model: ids 0..n-1
+    assert sorted((perm[is_sph] & 0x7FFFFFFF).tolist()) == list(range(len(spheres)))
     lo, hi = nodes[:, :3], nodes[:, 4:7]
     left = nodes[:, 3].view(np.int32)
     right = nodes[:, 7].view(np.int32)
-    seen = np.zeros(2 * n - 1, np.int32)
+    seen = np.zeros(2 * L - 1, np.int32)
     stack = [0]
     depth = {0: 0}
     while stack:
         k = stack.pop()
         seen[k] += 1
-        if k >= n - 1:
+        if k >= L - 1:
             continue
         for c in (left[k], right[k]):
-            assert 0 <= c < 2 * n - 1
+            assert 0 <= c < 2 * L - 1
             assert np.all(lo[c] >= lo[k]) and np.all(hi[c] <= hi[k])
             depth[c] = depth[k] + 1
             stack.append(c)
     assert np.all(seen == 1), "every node reachable exactly once"
     assert max(depth.values()) <= 64
-    tri = scene.tri_points().reshape(-1, 3, 3)[perm]
-    leaf_lo, leaf_hi = lo[n - 1:], hi[n - 1:]
-    assert np.all(tri.min(axis=1) >= leaf_lo) and np.all(tri.max(axis=1) <= leaf_hi)
+    tri = scene.tri_points().reshape(-1, 3, 3)
+    leaf_lo, leaf_hi = lo[L - 1:], hi[L - 1:]
+    t_idx = np.nonzero(~is_sph)[0]
+    pts = tri[perm[t_idx]]
+    assert np.all(pts.min(axis=1) >= leaf_lo[t_idx]) and np.all(pts.max(axis=1) <= leaf_hi[t_idx])
+    for k in np.nonzero(is_sph)[0]:
+        sph = spheres[perm[k] & 0x7FFFFFFF]
+        c, r = np.array(list(sph.position), np.float32), np.float32(sph.radius)
+        assert np.all(c - r >= leaf_lo[k]) and np.all(c + r <= leaf_hi[k])
