@@ -11,6 +11,15 @@ Mrays/s = traced ray segments (primary + reflect + refract + shadow) per second.
           memory, device LBVH build, render and download of the uint8 image, wall clock
   roofline, cpu_baseline, clocks, per-kernel times: see the keys of the JSON line
 
+  batched config 3: 256 seeded scenes (displaced icosphere of 1k..500k triangles + 16 spheres,
+          resolution from {256^2, 512^2, 1024x768, 1920x1080}, 1 spp, depth 3) in shared waves
+          (rt_batch_render: persistent kernels, CUDA graph, autotuned tuning) against a loop of
+          plain per-scene renders (rt_batch_render_plain)
+  served  config 4: 64 resident scenes of the same law; Poisson request streams (lambda 50, 200,
+          800 /s) with orbit cameras through the continuous-batching server and through the
+          plain one-request-at-a-time server; p50/p99 latency and Mrays/s, plus a saturated
+          stream (all requests at once) for peak throughput
+
 `--impl reference` times the CPU oracle (a restatement of the reference's own algorithm,
 checked bit-for-bit against the reference compiled from its sources) on a seeded sample of
 the same frame's 64x64 tiles, with every host core.
@@ -161,6 +170,94 @@ def run_reference(args) -> None:
     }), flush=True)
 
 
+def gen_scenes(config: int, n: int):
+    """Seeded scenes of config 3 or 4, generated on all host cores (the generator is reentrant)."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    import raytrace_gb300 as rt
+
+    with ThreadPoolExecutor(max_workers=os.cpu_count() or 4) as ex:
+        return list(ex.map(lambda i: rt.SceneHost.config(config, i), range(n)))
+
+
+def run_batched(ctx, n_scenes: int, reps: int) -> dict:
+    """Config 3: n scenes in shared waves vs a loop of plain per-scene renders."""
+    import raytrace_gb300 as rt
+
+    t0 = time.perf_counter()
+    scenes = gen_scenes(3, n_scenes)
+    gen_s = time.perf_counter() - t0
+    sids, fids, rds, pixels = [], [], [], 0
+    for sc in scenes:
+        cam = sc.desc.camera
+        sids.append(ctx.upload(sc))
+        fids.append(ctx.frame(cam.width, cam.height))
+        rds.append(ctx.render_desc(cam.width, cam.height, 1, 3))
+        pixels += cam.width * cam.height
+    tris = sum(int(sc.desc.n_tris) for sc in scenes)
+
+    def timed(fn) -> tuple[float, int]:
+        fn()   # warm (graph capture, workspace growth)
+        best, rays = 1e30, 0
+        for _ in range(reps):
+            ctx.synchronize()
+            t = time.perf_counter()
+            fn()
+            ctx.synchronize()
+            best = min(best, time.perf_counter() - t)
+            rays = ctx.wait().total_rays()   # ray counters of the batch just run
+        return best, rays
+
+    plain_s, plain_rays = timed(lambda: ctx.batch(sids, fids, rds, plain=True))
+    tuned = ctx.autotune(sids, fids, rds)
+    batch_s, batch_rays = timed(lambda: ctx.batch(sids, fids, rds, tuning=tuned))
+    default_s, _ = timed(lambda: ctx.batch(sids, fids, rds))
+    for f in fids:
+        ctx.release_frame(f)
+    for s_ in sids:
+        ctx.release_scene(s_)
+    return {
+        "workload": f"config3: {n_scenes} seeded scenes (displaced icosphere 1k..500k tris + 16 spheres), "
+                    f"resolutions from 256^2..1080p, 1 spp, depth 3",
+        "scenes": n_scenes, "triangles": tris, "pixels": pixels, "rays": batch_rays,
+        "plain_ms": round(plain_s * 1e3, 3), "batched_ms": round(batch_s * 1e3, 3),
+        "batched_default_ms": round(default_s * 1e3, 3),
+        "plain_mrays_per_s": round(plain_rays / plain_s / 1e6, 2),
+        "batched_mrays_per_s": round(batch_rays / batch_s / 1e6, 2),
+        "speedup": round(plain_s / batch_s, 3), "tuning": tuned.as_dict(),
+        "timing": f"best of {reps} wall-clock passes after a warm pass (host->device scene data resident)",
+        "scene_gen_s": round(gen_s, 2),
+    }
+
+
+def run_served(ctx, seconds: float) -> dict:
+    """Config 4: Poisson request streams over 64 resident scenes, batched server vs plain server."""
+    import raytrace_gb300 as rt
+
+    scenes = gen_scenes(4, 64)
+    out = {"workload": "config4: 64 resident scenes (config-3 law, seed 4), Poisson arrivals, orbit cameras "
+                       "(azimuth U[0,360), elevation U[10,60]), resolution uniform over 256^2/512^2/1024x768/1080p, "
+                       "1 spp, depth 3, 120 GB budget with LRU eviction", "seconds_per_stream": seconds}
+    keys = ("requests", "completed", "rejected", "p50_ms", "p99_ms", "mean_ms", "max_ms", "mrays_per_s", "wall_s",
+            "rays", "waves", "mean_wave_requests", "admitted_busy", "evictions", "rebuilds", "peak_bytes")
+    for plain in (False, True):
+        arm = "plain" if plain else "batched"
+        with rt.Server(ctx, 120 << 30, max_inflight=64, plain=plain, keep_images=False) as srv:
+            for sc in scenes:
+                srv.add_scene(sc)
+            for lam in (50, 200, 800):
+                st = srv.run_poisson(float(lam), seconds, seed=4)
+                out.setdefault(f"lambda_{lam}", {})[arm] = {k: (round(st[k], 3) if isinstance(st[k], float) else st[k])
+                                                            for k in keys}
+            st = srv.run_poisson(20000.0, 0.05, seed=5)   # ~1000 requests at once: peak throughput
+            out.setdefault("saturated", {})[arm] = {k: (round(st[k], 3) if isinstance(st[k], float) else st[k])
+                                                    for k in keys}
+    for k in [k for k in out if k.startswith("lambda_") or k == "saturated"]:
+        b, p = out[k]["batched"], out[k]["plain"]
+        out[k]["speedup_mrays"] = round(b["mrays_per_s"] / max(p["mrays_per_s"], 1e-9), 3)
+    return out
+
+
 def run_gpu(args) -> None:
     import numpy as np
     import torch
@@ -293,6 +390,10 @@ def run_gpu(args) -> None:
         "wall_s_timed": round(wall, 4),
         "bvh_build_ms": round(ctx.build_ms(sid), 3),
     }
+    if world == 1 and not args.skip_batched:
+        out["batched"] = run_batched(ctx, args.batched_scenes, 2)
+    if world == 1 and not args.skip_served:
+        out["served"] = run_served(ctx, args.served_seconds)
     print(json.dumps(out), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
@@ -305,6 +406,10 @@ def main() -> None:
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--skip-cpu", action="store_true", help="omit the CPU-baseline sample")
+    ap.add_argument("--skip-batched", action="store_true", help="omit the config-3 batched comparison")
+    ap.add_argument("--skip-served", action="store_true", help="omit the config-4 serving comparison")
+    ap.add_argument("--batched-scenes", type=int, default=256)
+    ap.add_argument("--served-seconds", type=float, default=5.0, help="length of each Poisson stream")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

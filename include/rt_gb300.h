@@ -247,57 +247,88 @@ int rt_batch_render_plain(rt_ctx *ctx, int32_t n, const int32_t *scene_ids,
 int rt_batch_autotune(rt_ctx *ctx, int32_t n, const int32_t *scene_ids, const int32_t *frame_ids,
                       const rt_render_desc *rds, rt_batch_tuning *out);
 
-/* ---- serving: continuous batching over resident scenes ---------------------------------- */
+/* ---- serving: continuous batching over resident scenes ----------------------------------
+ * No counterpart in the reference (its RayTracer renders one scene per start() call).
+ * Requests (scene, camera, resolution) are queued as they arrive; each step admits queued
+ * requests while frame slots and the HBM budget allow (LRU-evicting idle scenes, rebuilding
+ * an evicted scene's LBVH on a miss), then traces one wave made of sample chunks of every
+ * admitted request, so frames admitted at different times share the same kernels. A finished
+ * frame is resolved and copied to pinned host memory on a copy stream. Each frame is the same
+ * alone or in any mix: colours accumulate as exact fixed-point sums. */
 typedef struct rt_server rt_server;
 
 typedef struct rt_server_config {
-    int64_t hbm_budget_bytes;    /* admission budget for scenes + frames + queues */
-    int32_t max_inflight;        /* frame slots admitted at once */
-    int32_t max_level;
-    int32_t spp;
-    int64_t queue_rays;          /* capacity of the shared wavefront queue (0 = default) */
+    int64_t hbm_budget_bytes;    /* device bytes for resident scenes + frame slots + wave queues */
+    int32_t max_inflight;        /* frame slots: requests admitted at once (0 = 64) */
+    int32_t max_level;           /* recursion depth of every request */
+    int32_t spp;                 /* samples per pixel of every request (>= 1) */
+    int32_t plain;               /* 1: one request at a time through rt_render (comparison path) */
+    int64_t queue_rays;          /* ray-queue entries of one wave (0 = 2^23) */
+    int64_t max_pixels;          /* largest width*height of a request (0 = 1920*1080) */
+    int32_t keep_images;         /* 1: keep finished images in host memory until rt_server_result */
+    int32_t stages;              /* waves the host may enqueue ahead of the device (0 = 2) */
 } rt_server_config;
 
 typedef struct rt_request {
     int32_t scene;               /* server scene id */
     int32_t width, height;
-    rt_camera camera;
-    double arrival_s;            /* arrival time on the server clock */
+    rt_camera camera;            /* the camera's own width/height are ignored */
+    uint64_t seed;               /* sub-pixel jitter seed (spp > 1) */
+    double arrival_s;            /* arrival on the server clock; < 0 = now */
 } rt_request;
 
 typedef struct rt_request_result {
     int64_t request;
     int32_t status;              /* RT_OK or RT_ERR_* */
     int32_t width, height;
-    double arrival_s, admit_s, done_s;
-    int64_t rays;                /* ray segments traced for this frame */
+    int32_t scene;
+    double arrival_s, admit_s, done_s;   /* server clock; done = image in host memory */
+    int64_t samples;             /* primary rays of the frame */
+    int32_t rebuilt;             /* 1 when the scene was rebuilt on a miss for this request */
+    int32_t pad;
 } rt_request_result;
 
 typedef struct rt_serve_stats {
     int64_t requests, completed, rejected, evictions, rebuilds;
-    double p50_ms, p99_ms, mean_ms, max_ms;
-    double mrays_per_s;          /* all ray segments / wall time */
+    double p50_ms, p99_ms, mean_ms, max_ms;   /* frame latency: arrival to image in host memory */
+    double mrays_per_s;          /* ray segments traced / wall time */
     double wall_s;
     int64_t rays;
-    int64_t peak_bytes;
+    int64_t peak_bytes;          /* most device bytes held against the budget */
+    int64_t waves;
+    double mean_wave_requests;   /* requests sharing a wave, averaged over waves */
+    int64_t admitted_busy;       /* requests admitted while other requests were in flight */
+    int64_t pixels;              /* pixels of the completed frames */
 } rt_serve_stats;
 
 int    rt_server_create(rt_ctx *ctx, const rt_server_config *cfg, rt_server **out);
 void   rt_server_destroy(rt_server *srv);
-/* register a scene; the host copy is kept so an evicted scene can be rebuilt on a miss */
+const char *rt_server_last_error(const rt_server *srv);
+/* register a scene (deep copy kept for rebuilds); it is uploaded now if the budget allows */
 int    rt_server_add_scene(rt_server *srv, const rt_scene_desc *desc, int32_t *scene);
 int    rt_server_submit(rt_server *srv, const rt_request *req, int64_t *request_id);
-/* one continuous-batching step: admit, trace one bounce of every in-flight frame, retire */
-int    rt_server_step(rt_server *srv, int32_t *n_inflight);
-/* drain: step until nothing is queued or in flight */
+/* one continuous-batching step: retire finished frames, admit, enqueue one wave.
+ * *n_pending = requests queued or in flight afterwards. */
+int    rt_server_step(rt_server *srv, int32_t *n_pending);
+/* step until nothing is queued or in flight */
 int    rt_server_drain(rt_server *srv);
-/* result + image of a finished request (rgb may be NULL); RT_ERR_NOT_FOUND if not done */
-int    rt_server_result(rt_server *srv, int64_t request_id, rt_request_result *res, float *rgb);
+/* result (and image, if kept) of a finished request; the request is forgotten afterwards.
+ * RT_ERR_BUSY while it is queued or in flight, RT_ERR_NOT_FOUND if unknown. */
+int    rt_server_result(rt_server *srv, int64_t request_id, rt_request_result *res, float *rgb, uint8_t *rgb8);
 int    rt_server_resident(rt_server *srv, int32_t scene, int32_t *resident);
 double rt_server_now(rt_server *srv);
-/* run a Poisson arrival stream of requests over the registered scenes in real time */
+/* counters since creation or the last rt_server_run_poisson; latency over finished requests */
+int    rt_server_stats(rt_server *srv, rt_serve_stats *stats);
+/* a Poisson stream of requests in real time over the registered scenes: scene uniform, camera
+ * orbiting the world origin at the distance of the scene's own camera (azimuth U[0,360),
+ * elevation U[10,60] degrees), resolution uniform over 256^2, 512^2, 1024x768, 1920x1080.
+ * Arrivals stop at duration_s; the server then drains. Stats cover this run only. */
 int    rt_server_run_poisson(rt_server *srv, double lambda_per_s, double duration_s, uint64_t seed,
                              rt_serve_stats *stats);
+/* the orbit camera of those requests: `base` moved to the given azimuth/elevation about the
+ * world origin at its own distance, looking at the origin with up = +y (host only) */
+int    rt_orbit_camera(const rt_camera *base, double azimuth_deg, double elevation_deg, int32_t width,
+                       int32_t height, rt_camera *out);
 
 /* ---- LBVH pieces exposed for tests ------------------------------------------------------ */
 /* 30-bit Morton codes of triangle centroids over the AABB of the centroids, radix-sorted

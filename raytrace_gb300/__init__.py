@@ -97,24 +97,30 @@ class BatchTuning(C.Structure):
 
 class ServerConfig(C.Structure):
     _fields_ = [("hbm_budget_bytes", C.c_int64), ("max_inflight", C.c_int32), ("max_level", C.c_int32),
-                ("spp", C.c_int32), ("queue_rays", C.c_int64)]
+                ("spp", C.c_int32), ("plain", C.c_int32), ("queue_rays", C.c_int64), ("max_pixels", C.c_int64),
+                ("keep_images", C.c_int32), ("stages", C.c_int32)]
 
 
 class Request(C.Structure):
     _fields_ = [("scene", C.c_int32), ("width", C.c_int32), ("height", C.c_int32), ("camera", Camera),
-                ("arrival_s", C.c_double)]
+                ("seed", C.c_uint64), ("arrival_s", C.c_double)]
 
 
 class RequestResult(C.Structure):
     _fields_ = [("request", C.c_int64), ("status", C.c_int32), ("width", C.c_int32), ("height", C.c_int32),
-                ("arrival_s", C.c_double), ("admit_s", C.c_double), ("done_s", C.c_double), ("rays", C.c_int64)]
+                ("scene", C.c_int32), ("arrival_s", C.c_double), ("admit_s", C.c_double), ("done_s", C.c_double),
+                ("samples", C.c_int64), ("rebuilt", C.c_int32), ("pad", C.c_int32)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_ if k != "pad"}
 
 
 class ServeStats(C.Structure):
     _fields_ = [("requests", C.c_int64), ("completed", C.c_int64), ("rejected", C.c_int64),
                 ("evictions", C.c_int64), ("rebuilds", C.c_int64), ("p50_ms", C.c_double), ("p99_ms", C.c_double),
                 ("mean_ms", C.c_double), ("max_ms", C.c_double), ("mrays_per_s", C.c_double),
-                ("wall_s", C.c_double), ("rays", C.c_int64), ("peak_bytes", C.c_int64)]
+                ("wall_s", C.c_double), ("rays", C.c_int64), ("peak_bytes", C.c_int64), ("waves", C.c_int64),
+                ("mean_wave_requests", C.c_double), ("admitted_busy", C.c_int64), ("pixels", C.c_int64)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -149,11 +155,15 @@ _SIGS = {
     "rt_batch_autotune": (C.c_int, [P, C.c_int32, P, P, P, C.POINTER(BatchTuning)]),
     "rt_server_create": (C.c_int, [P, C.POINTER(ServerConfig), C.POINTER(P)]),
     "rt_server_destroy": (None, [P]),
+    "rt_server_last_error": (C.c_char_p, [P]),
+    "rt_server_stats": (C.c_int, [P, C.POINTER(ServeStats)]),
+    "rt_orbit_camera": (C.c_int, [C.POINTER(Camera), C.c_double, C.c_double, C.c_int32, C.c_int32,
+                                  C.POINTER(Camera)]),
     "rt_server_add_scene": (C.c_int, [P, C.POINTER(SceneDesc), C.POINTER(C.c_int32)]),
     "rt_server_submit": (C.c_int, [P, C.POINTER(Request), C.POINTER(C.c_int64)]),
     "rt_server_step": (C.c_int, [P, C.POINTER(C.c_int32)]),
     "rt_server_drain": (C.c_int, [P]),
-    "rt_server_result": (C.c_int, [P, C.c_int64, C.POINTER(RequestResult), P]),
+    "rt_server_result": (C.c_int, [P, C.c_int64, C.POINTER(RequestResult), P, P]),
     "rt_server_resident": (C.c_int, [P, C.c_int32, C.POINTER(C.c_int32)]),
     "rt_server_now": (C.c_double, [P]),
     "rt_server_run_poisson": (C.c_int, [P, C.c_double, C.c_double, C.c_uint64, C.POINTER(ServeStats)]),
@@ -329,6 +339,11 @@ class Context:
         lib.rt_scene_build_ms(self._h, sid, C.byref(ms))
         return ms.value
 
+    def device_bytes(self, sid: int) -> int:
+        b = C.c_int64()
+        self._ck(lib.rt_scene_device_bytes(self._h, sid, C.byref(b)), "rt_scene_device_bytes")
+        return b.value
+
     def build_ms(self, sid: int) -> float:
         ms = C.c_float()
         self._ck(lib.rt_scene_build_ms(self._h, sid, C.byref(ms)), "rt_scene_build_ms")
@@ -426,9 +441,127 @@ class Context:
         return nodes, perm
 
     def close(self) -> None:
+        for ref in getattr(self, "_servers", []):   # servers live inside the context
+            srv = ref()
+            if srv is not None:
+                srv.close()
         h, self._h = getattr(self, "_h", None), None
         if h:
             lib.rt_ctx_destroy(h)
+
+    def __del__(self):
+        self.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+
+def orbit_camera(base: Camera, azimuth_deg: float, elevation_deg: float, width: int, height: int) -> Camera:
+    """`base` moved about the world origin at its own distance, looking at the origin (rt_orbit_camera)."""
+    out = Camera()
+    rc = lib.rt_orbit_camera(C.byref(base), azimuth_deg, elevation_deg, width, height, C.byref(out))
+    if rc:
+        raise RTError(rc, "rt_orbit_camera")
+    return out
+
+
+class Server:
+    """Continuous-batching render server over device-resident scenes (rt_server)."""
+
+    def __init__(self, ctx: Context, budget_bytes: int, max_inflight: int = 64, max_level: int = 3, spp: int = 1,
+                 plain: bool = False, queue_rays: int = 0, max_pixels: int = 0, keep_images: bool = True,
+                 stages: int = 0):
+        import weakref
+
+        cfg = ServerConfig(int(budget_bytes), max_inflight, max_level, spp, int(plain), queue_rays, max_pixels,
+                           int(keep_images), stages)
+        h = P()
+        rc = lib.rt_server_create(ctx.handle, C.byref(cfg), C.byref(h))
+        if rc:
+            raise RTError(rc, f"rt_server_create: {lib.rt_last_error(ctx.handle).decode(errors='replace')}")
+        self._h, self._ctx, self.config = h, ctx, cfg
+        self._cams: list[Camera] = []
+        if not hasattr(ctx, "_servers"):
+            ctx._servers = []
+        ctx._servers.append(weakref.ref(self))
+
+    def _ck(self, rc: int, what: str) -> None:
+        if rc:
+            raise RTError(rc, f"{what}: {lib.rt_server_last_error(self._h).decode(errors='replace')}")
+
+    def add_scene(self, scene: SceneHost) -> int:
+        sid = C.c_int32()
+        self._ck(lib.rt_server_add_scene(self._h, scene.desc_ptr(), C.byref(sid)), "rt_server_add_scene")
+        cam = Camera()
+        C.pointer(cam)[0] = scene.desc.camera
+        self._cams.append(cam)
+        return sid.value
+
+    def camera(self, sid: int) -> Camera:
+        return self._cams[sid]
+
+    def submit(self, scene: int, width: int, height: int, camera: Camera | None = None, seed: int = 0,
+               arrival_s: float = -1.0) -> int:
+        if camera is None:   # the scene's own camera; an unknown scene is reported by the library
+            camera = self._cams[scene] if 0 <= scene < len(self._cams) else Camera()
+        req = Request(scene, width, height, camera, seed, arrival_s)
+        rid = C.c_int64()
+        self._ck(lib.rt_server_submit(self._h, C.byref(req), C.byref(rid)), "rt_server_submit")
+        return rid.value
+
+    def step(self) -> int:
+        n = C.c_int32()
+        self._ck(lib.rt_server_step(self._h, C.byref(n)), "rt_server_step")
+        return n.value
+
+    def drain(self) -> None:
+        self._ck(lib.rt_server_drain(self._h), "rt_server_drain")
+
+    def result(self, rid: int, image: bool = True) -> dict | None:
+        """The finished request (with its image if kept), or None while it is queued or in flight."""
+        res = RequestResult()
+        rgb = rgb8 = None
+        if image and self.config.keep_images:
+            # the size is only known from the record: peek without images first is not possible
+            # (taking the result forgets it), so allocate for the largest frame and trim
+            n = int(self.config.max_pixels or 1920 * 1080)
+            rgb, rgb8 = np.empty(3 * n, np.float32), np.empty(3 * n, np.uint8)
+        rc = lib.rt_server_result(self._h, rid, C.byref(res), _ptr(rgb), _ptr(rgb8))
+        if rc == RT_ERR_BUSY:
+            return None
+        self._ck(rc, "rt_server_result")
+        out = res.as_dict()
+        if rgb is not None and res.status == 0:
+            npx = res.width * res.height
+            out["rgb"] = rgb[: 3 * npx].reshape(res.height, res.width, 3)
+            out["rgb8"] = rgb8[: 3 * npx].reshape(res.height, res.width, 3)
+        return out
+
+    def resident(self, sid: int) -> bool:
+        r = C.c_int32()
+        self._ck(lib.rt_server_resident(self._h, sid, C.byref(r)), "rt_server_resident")
+        return bool(r.value)
+
+    def now(self) -> float:
+        return lib.rt_server_now(self._h)
+
+    def stats(self) -> dict:
+        st = ServeStats()
+        self._ck(lib.rt_server_stats(self._h, C.byref(st)), "rt_server_stats")
+        return st.as_dict()
+
+    def run_poisson(self, lam: float, duration_s: float, seed: int = 4) -> dict:
+        st = ServeStats()
+        self._ck(lib.rt_server_run_poisson(self._h, lam, duration_s, seed, C.byref(st)), "rt_server_run_poisson")
+        return st.as_dict()
+
+    def close(self) -> None:
+        h, self._h = getattr(self, "_h", None), None
+        if h:
+            lib.rt_server_destroy(h)
 
     def __del__(self):
         self.close()

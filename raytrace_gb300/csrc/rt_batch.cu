@@ -1,7 +1,8 @@
-// rt_batch.cu — batched multi-scene rendering: many (scene, frame) jobs traced as one
-// wavefront by persistent kernels that pull ray tiles from global work counters, with the
-// per-bounce launch sequence captured once as a CUDA graph and replayed per wave; plus the
-// plain loop of per-scene renders it is compared against, and the autotuner.
+// rt_batch.cu — batched multi-scene rendering: many (scene, frame) jobs traced as shared
+// waves by persistent kernels that pull ray tiles from global work counters, with the
+// per-bounce launch sequence captured once as a CUDA graph and replayed per wave; the wave
+// runner (also used by the server), the plain loop of per-scene renders it is compared
+// against, and the autotuner.
 #include <algorithm>
 #include <chrono>
 #include <cstring>
@@ -12,21 +13,200 @@
 
 using namespace rtg;
 
+// ---- wave runner --------------------------------------------------------------------------------------------
+
+WaveRunner::~WaveRunner()
+{
+    for (WaveStage &st : stages) {
+        if (st.done) {
+            cudaEventSynchronize(st.done);
+            cudaEventDestroy(st.done);
+        }
+        if (st.jobs) cudaFreeHost(st.jobs);
+    }
+}
+
+// A sample's rays at bounce l number at most b^l (b = children per hit, one queue holds one
+// bounce), so a wave whose chunks satisfy sum(samples * b^max_level) <= capacity cannot overflow
+// its ray queue or its shadow queue (at most one shadow record per hit).
+long long wave_weight(int branching, int max_level)
+{
+    return branching >= 2 ? 1ll << max_level : 1ll;
+}
+
+size_t wave_runner_bytes(const WaveRunner &R) { return R.ws.mem.bytes; }
+
+static int stage_harvest(rt_ctx *ctx, WaveRunner &R, WaveStage &st, bool wait)
+{
+    if (!st.busy) return RT_OK;
+    cudaError_t e = wait ? cudaEventSynchronize(st.done) : cudaEventQuery(st.done);
+    if (e == cudaErrorNotReady) return RT_OK;
+    if (e != cudaSuccess) return ctx_fail(ctx, RT_ERR_CUDA, "wave: %s", cudaGetErrorString(e));
+    const Counters &C = *st.counters;
+    R.rays_primary += C.rays_primary;
+    R.rays_secondary += C.rays_secondary;
+    R.rays_shadow += C.rays_shadow;
+    R.overflow |= C.overflow;
+    R.error |= C.error;
+    st.busy = false;
+    return RT_OK;
+}
+
+int wave_harvest(rt_ctx *ctx, WaveRunner &R, bool wait)
+{
+    for (size_t k = 0; k < R.stages.size(); ++k) {   // oldest first
+        WaveStage &st = R.stages[(R.next + k) % R.stages.size()];
+        int rc = stage_harvest(ctx, R, st, wait);
+        if (rc) return rc;
+    }
+    return RT_OK;
+}
+
+int wave_runner_init(rt_ctx *ctx, WaveRunner &R, long long qcap, int jobcap, int n_stages)
+{
+    if (R.ws.mem.p && qcap <= R.ws.qcap && jobcap <= R.jobcap && (int)R.stages.size() >= n_stages) return RT_OK;
+    int rc = wave_harvest(ctx, R, true);
+    if (rc) return rc;
+    qcap = std::max(qcap, R.ws.qcap);
+    jobcap = std::max(jobcap, R.jobcap);
+    n_stages = std::max(n_stages, (int)R.stages.size());
+    rc = ws_ensure(ctx, R.ws, qcap, jobcap);
+    if (rc) return rc;
+    R.graphs.clear();   // captured graphs point into the old workspace
+    R.ws.wf.cancel = ctx->cancel_dev;
+    for (WaveStage &st : R.stages) {
+        if (st.jobs) cudaFreeHost(st.jobs);
+        if (st.done) cudaEventDestroy(st.done);
+    }
+    R.stages.assign((size_t)n_stages, WaveStage());
+    R.next = 0;
+    R.jobcap = jobcap;
+    const size_t o_end = sizeof(DevJob) * jobcap, o_scn = o_end + 8 * (size_t)jobcap,
+                 o_sc = o_scn + sizeof(DevScene) * jobcap, o_ctr = o_sc + 64, total = o_ctr + sizeof(Counters);
+    for (WaveStage &st : R.stages) {
+        void *p = nullptr;
+        CK(ctx, cudaHostAlloc(&p, total, cudaHostAllocDefault));
+        char *b = (char *)p;
+        st.jobs = (DevJob *)b;
+        st.end = (long long *)(b + o_end);
+        st.scenes = (DevScene *)(b + o_scn);
+        st.scalars = (long long *)(b + o_sc);
+        st.counters = (Counters *)(b + o_ctr);
+        CK(ctx, cudaEventCreate(&st.done));
+    }
+    return RT_OK;
+}
+
+static int wave_graph(rt_ctx *ctx, WaveRunner &R, int max_level, const Tuning &t, cudaGraphExec_t &exec)
+{
+    const long long key = ((long long)max_level << 40) ^ ((long long)t.block << 24) ^ ((long long)t.tile << 8) ^
+                          (long long)t.stack ^ ((long long)t.dynamic << 50) ^ ((long long)t.min_blocks << 52);
+    auto it = R.graphs.find(key);
+    if (it != R.graphs.end()) {
+        exec = it->second->exec;
+        return RT_OK;
+    }
+    cudaStream_t cap;
+    CK(ctx, cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+    cudaGraph_t g;
+    cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
+    cudaMemsetAsync(R.ws.wf.C, 0, sizeof(Counters), cap);
+    enqueue_levels(ctx, R.ws, max_level, t, cap, nullptr);
+    cudaError_t e = cudaStreamEndCapture(cap, &g);
+    cudaStreamDestroy(cap);
+    if (e != cudaSuccess) return ctx_fail(ctx, RT_ERR_CUDA, "graph capture: %s", cudaGetErrorString(e));
+    std::unique_ptr<GraphEntry> ge(new GraphEntry());
+    e = cudaGraphInstantiate(&ge->exec, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return ctx_fail(ctx, RT_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
+    exec = ge->exec;
+    R.graphs[key] = std::move(ge);
+    return RT_OK;
+}
+
+int wave_enqueue(rt_ctx *ctx, WaveRunner &R, const std::vector<WaveJob *> &jobs, const Tuning &t, bool use_graph,
+                 cudaStream_t s, long long *samples_out)
+{
+    *samples_out = 0;
+    WaveStage &st = R.stages[R.next];
+    int rc = stage_harvest(ctx, R, st, true);   // the ring is full: wait for its oldest wave
+    if (rc) return rc;
+    const long long Q = R.ws.qcap;
+    long long used = 0, samples = 0;
+    int n = 0, n_scenes = 0, max_level = 0, max_lights = 0;
+    std::vector<const SceneDev *> seen;
+    for (WaveJob *j : jobs) {
+        if (j->cursor >= j->total) continue;
+        if (n == R.jobcap) break;
+        const long long room = (Q - used) / j->weight;
+        if (room <= 0) break;   // jobs keep their order: the wave is full
+        const long long take = std::min(room, j->total - j->cursor);
+        int slot = -1;
+        for (int k = 0; k < n_scenes; ++k)
+            if (seen[k] == j->scene) slot = k;
+        if (slot < 0) {
+            slot = n_scenes++;
+            seen.push_back(j->scene);
+            st.scenes[slot] = j->scene->hdr;
+            max_lights = std::max(max_lights, j->scene->hdr.n_lights);
+        }
+        DevJob J = j->job;
+        J.scene = slot;
+        J.sample_base = samples - j->cursor;   // wave sample g maps to job sample g - sample_base
+        st.jobs[n] = J;
+        samples += take;
+        st.end[n] = samples;
+        used += take * j->weight;
+        j->cursor += take;
+        max_level = std::max(max_level, J.max_level);
+        ++n;
+    }
+    if (n == 0) return RT_OK;
+    st.scalars[0] = samples;
+    st.scalars[1] = 0;
+    st.scalars[2] = n;
+    st.scalars[3] = max_lights;
+    st.n_jobs = n;
+    st.samples = samples;
+    Workspace &ws = R.ws;
+    CK(ctx, cudaMemcpyAsync(ws.scenes, st.scenes, sizeof(DevScene) * n_scenes, cudaMemcpyHostToDevice, s));
+    CK(ctx, cudaMemcpyAsync(ws.jobs, st.jobs, sizeof(DevJob) * n, cudaMemcpyHostToDevice, s));
+    CK(ctx, cudaMemcpyAsync(ws.job_end, st.end, 8 * (size_t)n, cudaMemcpyHostToDevice, s));
+    CK(ctx, cudaMemcpyAsync(ws.scalars, st.scalars, 32, cudaMemcpyHostToDevice, s));
+    cudaGraphExec_t exec = nullptr;
+    if (use_graph) {
+        rc = wave_graph(ctx, R, max_level, t, exec);
+        if (rc) return rc;
+        CK(ctx, cudaGraphLaunch(exec, s));
+    } else {
+        CK(ctx, cudaMemsetAsync(ws.wf.C, 0, sizeof(Counters), s));
+        enqueue_levels(ctx, ws, max_level, t, s, nullptr);
+    }
+    CK(ctx, cudaMemcpyAsync(st.counters, ws.wf.C, sizeof(Counters), cudaMemcpyDeviceToHost, s));
+    CK(ctx, cudaEventRecord(st.done, s));
+    st.busy = true;
+    R.next = (R.next + 1) % R.stages.size();
+    R.waves++;
+    R.wave_jobs += n;
+    *samples_out = samples;
+    return RT_OK;
+}
+
+// ---- batch ---------------------------------------------------------------------------------------------------
+
 namespace {
+// ray-queue entries of one batch wave: 2^24 entries hold 228 B each (two ray queues, shadow
+// queue, hit record)
+constexpr long long kBatchQueue = 1ll << 24;
+} // namespace
 
-struct JobPlan {
-    std::vector<DevJob> jobs;
-    std::vector<long long> samples;
-    std::vector<FrameDev *> frames;
-    std::vector<int> spp;
-    int max_level = 0;
-};
-
-int plan_jobs(rt_ctx *ctx, int32_t n, const int32_t *scene_ids, const int32_t *frame_ids, const rt_render_desc *rds,
-              JobPlan &plan, std::vector<DevScene> &hdrs)
+static int batch_core(rt_ctx *ctx, int32_t n, const int32_t *scene_ids, const int32_t *frame_ids,
+                      const rt_render_desc *rds, const Tuning &t, bool use_graph)
 {
     if (n <= 0 || !scene_ids || !frame_ids || !rds) return ctx_fail(ctx, RT_ERR_INVALID, "empty batch");
-    std::map<int, int> slot_of;
+    std::vector<WaveJob> jobs((size_t)n);
+    std::vector<FrameDev *> frames((size_t)n);
+    long long weighted = 0, heaviest = 1;
     for (int i = 0; i < n; ++i) {
         auto si = ctx->scenes.find(scene_ids[i]);
         if (si == ctx->scenes.end()) return ctx_fail(ctx, RT_ERR_NOT_FOUND, "unknown scene %d", scene_ids[i]);
@@ -34,119 +214,49 @@ int plan_jobs(rt_ctx *ctx, int32_t n, const int32_t *scene_ids, const int32_t *f
         if (fi == ctx->frames.end()) return ctx_fail(ctx, RT_ERR_NOT_FOUND, "unknown frame %d", frame_ids[i]);
         for (int j = 0; j < i; ++j)
             if (frame_ids[j] == frame_ids[i]) return ctx_fail(ctx, RT_ERR_INVALID, "frame %d used twice", frame_ids[i]);
-        int slot;
-        auto it = slot_of.find(scene_ids[i]);
-        if (it == slot_of.end()) {
-            slot = (int)hdrs.size();
-            slot_of[scene_ids[i]] = slot;
-            hdrs.push_back(si->second->hdr);
-        } else
-            slot = it->second;
-        DevJob J;
-        long long s = 0;
-        int rc = make_job(ctx, *si->second, *fi->second, &rds[i], slot, J, s);
+        WaveJob &w = jobs[i];
+        int rc = make_job(ctx, *si->second, *fi->second, &rds[i], 0, w.job, w.total);
         if (rc) return rc;
-        plan.jobs.push_back(J);
-        plan.samples.push_back(s);
-        plan.frames.push_back(fi->second.get());
-        plan.spp.push_back(rds[i].spp);
-        plan.max_level = std::max(plan.max_level, rds[i].max_level);
+        w.scene = si->second.get();
+        w.weight = wave_weight(w.scene->branching, rds[i].max_level);
+        frames[i] = fi->second.get();
+        weighted += w.total * w.weight;
+        heaviest = std::max(heaviest, w.weight);
     }
-    return RT_OK;
-}
-
-// samples per wave: bounds the queue memory of a batch
-constexpr long long kWaveSamples = 1ll << 24;
-
-} // namespace
-
-static int batch_core(rt_ctx *ctx, int32_t n, const int32_t *scene_ids, const int32_t *frame_ids,
-                      const rt_render_desc *rds, const Tuning &t, bool use_graph)
-{
-    JobPlan plan;
-    std::vector<DevScene> hdrs;
-    int rc = plan_jobs(ctx, n, scene_ids, frame_ids, rds, plan, hdrs);
+    if (!ctx->batch) ctx->batch.reset(new WaveRunner());
+    WaveRunner &R = *ctx->batch;
+    const long long qcap = std::max(std::min(weighted, kBatchQueue), std::max<long long>(heaviest, 4096));
+    int rc = wave_runner_init(ctx, R, qcap, std::max(n, 64), 2);
     if (rc) return rc;
-    long long total = 0;
-    std::vector<long long> end(plan.jobs.size());
-    for (size_t i = 0; i < plan.jobs.size(); ++i) {
-        plan.jobs[i].sample_base = total;
-        total += plan.samples[i];
-        end[i] = total;
-    }
-    const long long wave = std::min(total, kWaveSamples);
-    rc = ws_ensure(ctx, ctx->ws, std::max<long long>(2 * wave, 4096), (int)std::max(plan.jobs.size(), hdrs.size()));
-    if (rc) return rc;
-    Workspace &ws = ctx->ws;
     cudaStream_t s = ctx->stream;
-    ws.wf.cancel = ctx->cancel_dev;
     *ctx->cancel_host = 0;
-    if (cudaEventRecord(ctx->ev_start, s) != cudaSuccess) return ctx_fail(ctx, RT_ERR_CUDA, "event record");
-    cudaMemcpyAsync(ws.scenes, hdrs.data(), sizeof(DevScene) * hdrs.size(), cudaMemcpyHostToDevice, s);
-    cudaMemcpyAsync(ws.jobs, plan.jobs.data(), sizeof(DevJob) * plan.jobs.size(), cudaMemcpyHostToDevice, s);
-    cudaMemcpyAsync(ws.job_end, end.data(), 8 * end.size(), cudaMemcpyHostToDevice, s);
-    for (FrameDev *f : plan.frames) {
-        cudaMemsetAsync(f->fb.acc, 0, 24 * (size_t)f->w * f->h, s);
+    R.rays_primary = R.rays_secondary = R.rays_shadow = 0;
+    R.overflow = R.error = 0;
+    CK(ctx, cudaEventRecord(ctx->ev_start, s));
+    for (int i = 0; i < n; ++i) {
+        CK(ctx, cudaMemsetAsync(frames[i]->fb.acc, 0, 24 * (size_t)frames[i]->w * frames[i]->h, s));
+        if (jobs[i].job.plane_obj) launch_plane_init(frames[i]->fb, (long long)frames[i]->w * frames[i]->h, s);
     }
-    for (size_t i = 0; i < plan.jobs.size(); ++i)
-        if (plan.jobs[i].plane_obj) launch_plane_init(plan.frames[i]->fb, (long long)plan.frames[i]->w * plan.frames[i]->h, s);
-    // per-wave sequence; captured once per (max_level, tuning) and replayed
-    const long long key = ((long long)plan.max_level << 40) ^ ((long long)t.block << 24) ^ ((long long)t.tile << 8) ^
-                          (long long)t.stack ^ ((long long)t.dynamic << 50) ^ ((long long)t.min_blocks << 52);
-    cudaGraphExec_t exec = nullptr;
-    if (use_graph) {
-        auto it = ctx->graphs.find(key);
-        if (it == ctx->graphs.end()) {
-            cudaStream_t cap;
-            cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking);
-            cudaGraph_t g;
-            cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
-            cudaMemsetAsync(ws.wf.C, 0, sizeof(Counters), cap);
-            enqueue_levels(ctx, ws, plan.max_level, t, cap, nullptr);
-            cudaError_t e = cudaStreamEndCapture(cap, &g);
-            cudaStreamDestroy(cap);
-            if (e != cudaSuccess) return ctx_fail(ctx, RT_ERR_CUDA, "graph capture: %s", cudaGetErrorString(e));
-            std::unique_ptr<GraphEntry> ge(new GraphEntry());
-            e = cudaGraphInstantiate(&ge->exec, g, 0);
-            cudaGraphDestroy(g);
-            if (e != cudaSuccess) return ctx_fail(ctx, RT_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
-            exec = ge->exec;
-            ctx->graphs[key] = std::move(ge);
-        } else
-            exec = it->second->exec;
+    std::vector<WaveJob *> order((size_t)n);
+    for (int i = 0; i < n; ++i) order[i] = &jobs[i];
+    for (;;) {
+        long long got = 0;
+        rc = wave_enqueue(ctx, R, order, t, use_graph, s, &got);
+        if (rc) return rc;
+        if (!got) break;
     }
-    unsigned long long prim = 0, sec = 0, shd = 0;
-    int overflow = 0;
-    for (long long first = 0; first < total; first += wave) {
-        ctx->h_scalars[0] = std::min(wave, total - first);
-        ctx->h_scalars[1] = first;
-        ctx->h_scalars[2] = (long long)plan.jobs.size();
-        long long ml = 0;
-        for (const DevScene &hd : hdrs) ml = std::max<long long>(ml, hd.n_lights);
-        ctx->h_scalars[3] = ml;
-        cudaMemcpyAsync(ws.scalars, ctx->h_scalars, 32, cudaMemcpyHostToDevice, s);
-        if (exec)
-            cudaGraphLaunch(exec, s);
-        else {
-            cudaMemsetAsync(ws.wf.C, 0, sizeof(Counters), s);
-            enqueue_levels(ctx, ws, plan.max_level, t, s, nullptr);
-        }
-        cudaMemcpyAsync(ctx->counters_host, ws.wf.C, sizeof(Counters), cudaMemcpyDeviceToHost, s);
-        if (cudaStreamSynchronize(s) != cudaSuccess) return ctx_fail(ctx, RT_ERR_CUDA, "batch wave failed");
-        prim += ctx->counters_host->rays_primary;
-        sec += ctx->counters_host->rays_secondary;
-        shd += ctx->counters_host->rays_shadow;
-        overflow |= ctx->counters_host->overflow;
-    }
-    for (size_t i = 0; i < plan.jobs.size(); ++i)
-        launch_resolve(plan.frames[i]->fb, plan.frames[i]->w, plan.frames[i]->h, plan.spp[i], s);
-    cudaEventRecord(ctx->ev_stop, s);
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return ctx_fail(ctx, RT_ERR_CUDA, "batch: %s", cudaGetErrorString(e));
+    for (int i = 0; i < n; ++i) launch_resolve(frames[i]->fb, frames[i]->w, frames[i]->h, rds[i].spp, s);
+    CK(ctx, cudaGetLastError());
+    CK(ctx, cudaEventRecord(ctx->ev_stop, s));
+    rc = wave_harvest(ctx, R, true);
+    if (rc) return rc;
+    CK(ctx, cudaStreamSynchronize(s));
     Counters &C = *ctx->counters_host;
-    C.rays_primary = prim, C.rays_secondary = sec, C.rays_shadow = shd, C.overflow = overflow;
+    C.rays_primary = R.rays_primary, C.rays_secondary = R.rays_secondary, C.rays_shadow = R.rays_shadow;
+    C.overflow = R.overflow, C.error = R.error;
     ctx->pending.active = false;
-    if (overflow) return ctx_fail(ctx, RT_ERR_OVERFLOW, "batch ray queue overflow");
+    if (R.overflow) return ctx_fail(ctx, RT_ERR_OVERFLOW, "batch ray queue overflow");
+    if (R.error) return ctx_fail(ctx, RT_ERR_CUDA, "traversal stopped on a corrupt LBVH (flags 0x%x)", R.error);
     return RT_OK;
 }
 

@@ -36,14 +36,6 @@ int ctx_fail(rt_ctx *ctx, int code, const char *fmt, ...)
     return code;
 }
 
-#define CK(ctx, call)                                                                                             \
-    do {                                                                                                          \
-        cudaError_t e_ = (call);                                                                                  \
-        if (e_ != cudaSuccess)                                                                                    \
-            return ctx_fail(ctx, e_ == cudaErrorMemoryAllocation ? RT_ERR_OOM : RT_ERR_CUDA, "%s: %s (%s:%d)",       \
-                            #call, cudaGetErrorString(e_), __FILE__, __LINE__);                                  \
-    } while (0)
-
 DevBuf::~DevBuf() { release(); }
 void DevBuf::release()
 {
@@ -102,7 +94,7 @@ extern "C" void rt_ctx_destroy(rt_ctx *ctx)
     cudaStreamSynchronize(ctx->stream);
     ctx->scenes.clear();
     ctx->frames.clear();
-    ctx->graphs.clear();
+    ctx->batch.reset();
     ctx->ws = Workspace();
     if (ctx->cancel_host) cudaFreeHost((void *)ctx->cancel_host);
     if (ctx->counters_host) cudaFreeHost(ctx->counters_host);
@@ -296,6 +288,8 @@ extern "C" int rt_scene_upload(rt_ctx *ctx, const rt_scene_desc *d, int32_t *sce
     build_tables(d, h);
     std::unique_ptr<SceneDev> sc(new SceneDev());
     sc->camera = d->camera;
+    for (const DevMaterial &m : h.mtl)   // the spawn tests of the shade kernel
+        sc->branching = std::max(sc->branching, (int)(m.reflect > 0.01f) + (int)(m.refract > 0.01f));
     const int64_t n = h.n_tris;
     sc->n_tris = (int)n;
     sc->n_leaves = (int)(n + (int64_t)h.prims.size() - h.n_linear);
@@ -653,7 +647,6 @@ int ws_ensure(rt_ctx *ctx, Workspace &ws, long long qcap, int njobs)
     ws.wf.scenes = ws.scenes;
     ws.qcap = qcap;
     ws.jobcap = njobs;
-    ctx->graphs.clear();   // captured graphs point into the old workspace
     return RT_OK;
 }
 

@@ -42,6 +42,7 @@ struct SceneDev {
     rt_camera camera{};
     int n_tris = 0;
     int n_leaves = 0;   // triangles + spheres in the LBVH
+    int branching = 0;  // most child rays one hit can spawn: (reflect > 0.01) + (refract > 0.01)
     int64_t bytes = 0;
     float build_ms = 0.0f;
 };
@@ -133,6 +134,58 @@ struct GraphEntry {
     }
 };
 
+// one job of a wave-run batch (a frame, or a served request): samples [cursor, total) remain
+struct WaveJob {
+    rtg::DevJob job{};            // job.scene is set per wave (index into that wave's scene table)
+    const SceneDev *scene = nullptr;
+    long long total = 0;
+    long long cursor = 0;
+    long long weight = 1;         // queue entries one sample can need at its busiest bounce
+};
+
+// pinned host staging of one wave in flight: its tables go up, its counters come back
+struct WaveStage {
+    rtg::DevJob *jobs = nullptr;
+    long long *end = nullptr;
+    rtg::DevScene *scenes = nullptr;
+    long long *scalars = nullptr;
+    rtg::Counters *counters = nullptr;
+    cudaEvent_t done = nullptr;
+    bool busy = false;
+    int n_jobs = 0;
+    long long samples = 0;
+};
+
+// waves of chunks traced through one workspace: the per-bounce sequence is a CUDA graph
+// replayed per wave, tables are staged through a ring of pinned buffers so the host can run
+// ahead of the device by `stages` waves, and the queue never overflows because each wave's
+// chunks are sized against the capacity with every sample's branching bound
+struct WaveRunner {
+    Workspace ws;
+    std::vector<WaveStage> stages;
+    size_t next = 0;
+    int jobcap = 0;
+    std::map<long long, std::unique_ptr<GraphEntry>> graphs;
+    // totals of harvested waves
+    unsigned long long rays_primary = 0, rays_secondary = 0, rays_shadow = 0;
+    int overflow = 0, error = 0;
+    long long waves = 0, wave_jobs = 0;
+    WaveRunner() = default;
+    WaveRunner(const WaveRunner &) = delete;
+    WaveRunner &operator=(const WaveRunner &) = delete;
+    ~WaveRunner();
+};
+
+long long wave_weight(int branching, int max_level);
+int wave_runner_init(rt_ctx *ctx, WaveRunner &R, long long qcap, int jobcap, int stages);
+// plan and enqueue the next wave from `jobs` (taken in order) on stream s; waits only when the
+// staging ring is full. Sets *samples to the samples enqueued (0 = nothing left to trace).
+int wave_enqueue(rt_ctx *ctx, WaveRunner &R, const std::vector<WaveJob *> &jobs, const rtg::Tuning &t, bool use_graph,
+                 cudaStream_t s, long long *samples);
+// harvest every finished wave (wait = block until all enqueued waves are done)
+int wave_harvest(rt_ctx *ctx, WaveRunner &R, bool wait);
+size_t wave_runner_bytes(const WaveRunner &R);
+
 struct rt_ctx {
     int device = 0;
     cudaStream_t own_stream = nullptr, stream = nullptr;
@@ -151,10 +204,18 @@ struct rt_ctx {
     Pending pending;
     rtg::Tuning plain_tuning;
     KernelProfiler prof;
-    std::map<long long, std::unique_ptr<GraphEntry>> graphs;
+    std::unique_ptr<WaveRunner> batch;   // workspace + graphs of rt_batch_render
 };
 
 int ctx_fail(rt_ctx *ctx, int code, const char *fmt, ...);
+#define CK(ctx, call)                                                                                             \
+    do {                                                                                                          \
+        cudaError_t e_ = (call);                                                                                  \
+        if (e_ != cudaSuccess)                                                                                    \
+            return ctx_fail(ctx, e_ == cudaErrorMemoryAllocation ? RT_ERR_OOM : RT_ERR_CUDA, "%s: %s (%s:%d)",       \
+                            #call, cudaGetErrorString(e_), __FILE__, __LINE__);                                  \
+    } while (0)
+
 int validate_desc(rt_ctx *ctx, const rt_scene_desc *d);
 int frame_alloc(rt_ctx *ctx, int32_t w, int32_t h, FrameDev &f);
 int ws_ensure(rt_ctx *ctx, Workspace &ws, long long qcap, int njobs);
