@@ -231,7 +231,8 @@ typedef struct rt_batch_tuning {
     int32_t use_graph;           /* capture the per-bounce launch sequence as a CUDA graph */
     int32_t min_blocks;          /* 0, 6, 8, 10 or 12: resident 128-thread blocks per SM the register
                                     budget of the traversal kernels must allow (0 = compiler's) */
-    int32_t dynamic;             /* plain path: pull ray tiles from a counter (1) or stride (0) */
+    int32_t dynamic;             /* 0 or 1: pull ray tiles from a counter; 2: static grid stride */
+    int64_t wave_rays;           /* batch: ray-queue entries of one wave (0 = 2^24) */
 } rt_batch_tuning;
 
 /* kernel tuning of the plain per-scene path (rt_render); NULL restores the defaults */
@@ -243,7 +244,8 @@ int rt_batch_render(rt_ctx *ctx, int32_t n, const int32_t *scene_ids, const int3
 /* the same jobs through a loop of plain per-scene renders (the comparison path) */
 int rt_batch_render_plain(rt_ctx *ctx, int32_t n, const int32_t *scene_ids,
                           const int32_t *frame_ids, const rt_render_desc *rds);
-/* pick block / tile / stack for these jobs by timing candidates; writes the choice */
+/* pick block size, register cap and ray tile (or the static stride) for these jobs by timing
+ * candidates; the stack stays at 64 entries (the depth bound of the LBVH). Writes the choice. */
 int rt_batch_autotune(rt_ctx *ctx, int32_t n, const int32_t *scene_ids, const int32_t *frame_ids,
                       const rt_render_desc *rds, rt_batch_tuning *out);
 
@@ -329,6 +331,13 @@ int    rt_server_run_poisson(rt_server *srv, double lambda_per_s, double duratio
  * world origin at its own distance, looking at the origin with up = +y (host only) */
 int    rt_orbit_camera(const rt_camera *base, double azimuth_deg, double elevation_deg, int32_t width,
                        int32_t height, rt_camera *out);
+
+/* ---- test hook: the kernels' integer-exact replacements of FP64 expressions --------------
+ * out_mul[i] = (float)((double)x[i] * d) and out_fix[i] = llrint(v[i] * 2^32) (finite v,
+ * |v| < 2^31), computed on the device the way ray generation, frame resolve and colour
+ * accumulation compute them. d must be a positive normal double. Synchronous. */
+int rt_selftest_conversions(rt_ctx *ctx, const int64_t *x, int32_t n, double d, const float *v,
+                            float *out_mul, int64_t *out_fix);
 
 /* ---- LBVH pieces exposed for tests ------------------------------------------------------ */
 /* 30-bit Morton codes of triangle centroids over the AABB of the centroids, radix-sorted

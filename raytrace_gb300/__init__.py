@@ -89,7 +89,7 @@ class RenderStats(C.Structure):
 
 class BatchTuning(C.Structure):
     _fields_ = [("block", C.c_int32), ("tile", C.c_int32), ("stack", C.c_int32), ("use_graph", C.c_int32),
-                ("min_blocks", C.c_int32), ("dynamic", C.c_int32)]
+                ("min_blocks", C.c_int32), ("dynamic", C.c_int32), ("wave_rays", C.c_int64)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -155,6 +155,7 @@ _SIGS = {
     "rt_batch_autotune": (C.c_int, [P, C.c_int32, P, P, P, C.POINTER(BatchTuning)]),
     "rt_server_create": (C.c_int, [P, C.POINTER(ServerConfig), C.POINTER(P)]),
     "rt_server_destroy": (None, [P]),
+    "rt_selftest_conversions": (C.c_int, [P, P, C.c_int32, C.c_double, P, P, P]),
     "rt_server_last_error": (C.c_char_p, [P]),
     "rt_server_stats": (C.c_int, [P, C.POINTER(ServeStats)]),
     "rt_orbit_camera": (C.c_int, [C.POINTER(Camera), C.c_double, C.c_double, C.c_int32, C.c_int32,
@@ -430,6 +431,17 @@ class Context:
         perm = np.empty(n, np.uint32)
         self._ck(lib.rt_morton_sort(self._h, _ptr(tri_p), n, _ptr(codes), _ptr(perm)), "rt_morton_sort")
         return codes, perm
+
+    def selftest_conversions(self, x: np.ndarray, d: float, v: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
+        """The kernels' (float)((double)x * d) and llrint(v * 2^32), computed on the device."""
+        x = np.ascontiguousarray(x, np.int64)
+        v = np.ascontiguousarray(v, np.float32)
+        assert x.shape == v.shape
+        mul = np.empty(x.shape, np.float32)
+        fix = np.empty(x.shape, np.int64)
+        self._ck(lib.rt_selftest_conversions(self._h, _ptr(x), x.size, d, _ptr(v), _ptr(mul), _ptr(fix)),
+                 "rt_selftest_conversions")
+        return mul, fix
 
     def bvh(self, sid: int) -> tuple[np.ndarray, np.ndarray]:
         nn = C.c_int64()

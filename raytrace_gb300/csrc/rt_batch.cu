@@ -73,7 +73,7 @@ int wave_runner_init(rt_ctx *ctx, WaveRunner &R, long long qcap, int jobcap, int
     rc = ws_ensure(ctx, R.ws, qcap, jobcap);
     if (rc) return rc;
     R.graphs.clear();   // captured graphs point into the old workspace
-    R.ws.wf.cancel = ctx->cancel_dev;
+    R.ws.wf.cancel = nullptr;   // rt_batch_render arms and sets the context's flag
     for (WaveStage &st : R.stages) {
         if (st.jobs) cudaFreeHost(st.jobs);
         if (st.done) cudaEventDestroy(st.done);
@@ -125,7 +125,7 @@ static int wave_graph(rt_ctx *ctx, WaveRunner &R, int max_level, const Tuning &t
 }
 
 int wave_enqueue(rt_ctx *ctx, WaveRunner &R, const std::vector<WaveJob *> &jobs, const Tuning &t, bool use_graph,
-                 cudaStream_t s, long long *samples_out)
+                 cudaStream_t s, long long *samples_out, KernelProfiler *prof)
 {
     *samples_out = 0;
     WaveStage &st = R.stages[R.next];
@@ -180,7 +180,7 @@ int wave_enqueue(rt_ctx *ctx, WaveRunner &R, const std::vector<WaveJob *> &jobs,
         CK(ctx, cudaGraphLaunch(exec, s));
     } else {
         CK(ctx, cudaMemsetAsync(ws.wf.C, 0, sizeof(Counters), s));
-        enqueue_levels(ctx, ws, max_level, t, s, nullptr);
+        enqueue_levels(ctx, ws, max_level, t, s, prof);
     }
     CK(ctx, cudaMemcpyAsync(st.counters, ws.wf.C, sizeof(Counters), cudaMemcpyDeviceToHost, s));
     CK(ctx, cudaEventRecord(st.done, s));
@@ -195,13 +195,14 @@ int wave_enqueue(rt_ctx *ctx, WaveRunner &R, const std::vector<WaveJob *> &jobs,
 // ---- batch ---------------------------------------------------------------------------------------------------
 
 namespace {
-// ray-queue entries of one batch wave: 2^24 entries hold 228 B each (two ray queues, shadow
-// queue, hit record)
+// ray-queue entries of one batch wave by default: 2^24 entries hold 228 B each (two ray
+// queues, shadow queue, hit record)
 constexpr long long kBatchQueue = 1ll << 24;
 } // namespace
 
+// RT_FLAG_PROFILE on any job: launches go without the graph, bracketed by events per kernel
 static int batch_core(rt_ctx *ctx, int32_t n, const int32_t *scene_ids, const int32_t *frame_ids,
-                      const rt_render_desc *rds, const Tuning &t, bool use_graph)
+                      const rt_render_desc *rds, const Tuning &t, bool use_graph, long long wave_rays)
 {
     if (n <= 0 || !scene_ids || !frame_ids || !rds) return ctx_fail(ctx, RT_ERR_INVALID, "empty batch");
     std::vector<WaveJob> jobs((size_t)n);
@@ -225,11 +226,19 @@ static int batch_core(rt_ctx *ctx, int32_t n, const int32_t *scene_ids, const in
     }
     if (!ctx->batch) ctx->batch.reset(new WaveRunner());
     WaveRunner &R = *ctx->batch;
-    const long long qcap = std::max(std::min(weighted, kBatchQueue), std::max<long long>(heaviest, 4096));
+    const long long cap = wave_rays > 0 ? wave_rays : kBatchQueue;
+    const long long qcap = std::max(std::min(weighted, cap), std::max<long long>(heaviest, 4096));
     int rc = wave_runner_init(ctx, R, qcap, std::max(n, 64), 2);
     if (rc) return rc;
+    bool profile = false;
+    for (int i = 0; i < n; ++i) profile |= (rds[i].flags & RT_FLAG_PROFILE) != 0;
+    ctx->prof.reset(profile);
+    if (profile) use_graph = false;
+    KernelProfiler *P = profile ? &ctx->prof : nullptr;
     cudaStream_t s = ctx->stream;
-    *ctx->cancel_host = 0;
+    R.ws.wf.cancel = ctx->cancel_dev;
+    rc = cancel_arm(ctx);
+    if (rc) return rc;
     R.rays_primary = R.rays_secondary = R.rays_shadow = 0;
     R.overflow = R.error = 0;
     CK(ctx, cudaEventRecord(ctx->ev_start, s));
@@ -241,11 +250,13 @@ static int batch_core(rt_ctx *ctx, int32_t n, const int32_t *scene_ids, const in
     for (int i = 0; i < n; ++i) order[i] = &jobs[i];
     for (;;) {
         long long got = 0;
-        rc = wave_enqueue(ctx, R, order, t, use_graph, s, &got);
+        rc = wave_enqueue(ctx, R, order, t, use_graph, s, &got, P);
         if (rc) return rc;
         if (!got) break;
     }
+    if (P) P->begin(RT_KERNEL_RESOLVE, s);
     for (int i = 0; i < n; ++i) launch_resolve(frames[i]->fb, frames[i]->w, frames[i]->h, rds[i].spp, s);
+    if (P) P->end(s);
     CK(ctx, cudaGetLastError());
     CK(ctx, cudaEventRecord(ctx->ev_stop, s));
     rc = wave_harvest(ctx, R, true);
@@ -266,12 +277,15 @@ extern "C" int rt_batch_render(rt_ctx *ctx, int32_t n, const int32_t *scene_ids,
     if (!ctx) return RT_ERR_INVALID;
     Tuning t;   // defaults: persistent grid, 32-ray tiles, 128-thread blocks capped at 64 registers
     bool graph = true;
+    long long wave = 0;
     if (tuning) {
         int rc = tuning_from(ctx, tuning, t);
         if (rc) return rc;
         graph = tuning->use_graph != 0;
+        wave = tuning->wave_rays;
+        if (wave < 0 || wave > (1ll << 27)) return ctx_fail(ctx, RT_ERR_INVALID, "wave_rays %lld outside [0, 2^27]", wave);
     }
-    return batch_core(ctx, n, scene_ids, frame_ids, rds, t, graph);
+    return batch_core(ctx, n, scene_ids, frame_ids, rds, t, graph, wave);
 }
 
 extern "C" int rt_batch_render_plain(rt_ctx *ctx, int32_t n, const int32_t *scene_ids, const int32_t *frame_ids,
@@ -300,13 +314,14 @@ extern "C" int rt_batch_autotune(rt_ctx *ctx, int32_t n, const int32_t *scene_id
     if (!ctx || !out) return RT_ERR_INVALID;
     // (threads per block, register cap as resident blocks per SM) x rays per tile fetch; the
     // stack stays at 64 entries, the depth bound of a 30-bit Morton LBVH with index tie-breaks
+    // tile 0 stands for the static grid stride
     const int shapes[][2] = {{128, 8}, {128, 6}, {64, 8}, {256, 0}};
-    const int tiles[] = {32, 64, 128, 256};
+    const int tiles[] = {0, 32, 64, 128, 256};
     double best = 1e30;
-    rt_batch_tuning best_t{128, 32, 64, 1, 8, 1};
+    rt_batch_tuning best_t{128, 32, 64, 1, 8, 1, 0};
     for (const auto &sh : shapes)
         for (int tl : tiles) {
-            rt_batch_tuning t{sh[0], tl, 64, 1, sh[1], 1};
+            rt_batch_tuning t{sh[0], tl ? tl : 32, 64, 1, sh[1], tl ? 1 : 2, 0};
             int rc = rt_batch_render(ctx, n, scene_ids, frame_ids, rds, &t);   // warm (captures the graph)
             if (rc) return rc;
             auto t0 = std::chrono::steady_clock::now();

@@ -61,6 +61,18 @@ cudaError_t DevBuf::ensure(size_t need)
 static size_t a256(size_t x) { return (x + 255) & ~(size_t)255; }
 
 // ---- version / context -------------------------------------------------------------------------------
+// Cancel: rt_cancel writes 1 into a device word from page-locked memory on a side stream, which
+// runs beside the render; each render clears it on the same stream first and its kernels wait
+// for the clear. Kernels then read device memory, not host memory over the bus.
+int cancel_arm(rt_ctx *ctx)
+{
+    ctx->cancel_host = 0;
+    CK(ctx, cudaMemcpyAsync(ctx->cancel_dev, ctx->cancel_vals, sizeof(int), cudaMemcpyHostToDevice, ctx->side));
+    CK(ctx, cudaEventRecord(ctx->ev_armed, ctx->side));
+    CK(ctx, cudaStreamWaitEvent(ctx->stream, ctx->ev_armed, 0));
+    return RT_OK;
+}
+
 extern "C" int rt_version(void) { return RT_ABI_VERSION; }
 
 extern "C" int rt_ctx_create(int device, rt_ctx **out)
@@ -79,10 +91,16 @@ extern "C" int rt_ctx_create(int device, rt_ctx **out)
     if (cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess) return RT_ERR_CUDA;
     c->stream = c->own_stream;
     if (cudaEventCreate(&c->ev_start) != cudaSuccess || cudaEventCreate(&c->ev_stop) != cudaSuccess) return RT_ERR_CUDA;
-    if (cudaHostAlloc((void **)&c->cancel_host, sizeof(int), cudaHostAllocMapped) != cudaSuccess) return RT_ERR_CUDA;
-    *c->cancel_host = 0;
-    if (cudaHostGetDevicePointer((void **)&c->cancel_dev, (void *)c->cancel_host, 0) != cudaSuccess) return RT_ERR_CUDA;
+    if (cudaMalloc((void **)&c->cancel_dev, sizeof(int)) != cudaSuccess) return RT_ERR_CUDA;
+    if (cudaMallocHost((void **)&c->cancel_vals, 2 * sizeof(int)) != cudaSuccess) return RT_ERR_CUDA;
+    c->cancel_vals[0] = 0, c->cancel_vals[1] = 1;
+    if (cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking) != cudaSuccess) return RT_ERR_CUDA;
+    if (cudaEventCreateWithFlags(&c->ev_armed, cudaEventDisableTiming) != cudaSuccess) return RT_ERR_CUDA;
+    if (cudaMemset(c->cancel_dev, 0, sizeof(int)) != cudaSuccess) return RT_ERR_CUDA;
     if (cudaMallocHost((void **)&c->counters_host, sizeof(Counters)) != cudaSuccess) return RT_ERR_CUDA;
+    if (cudaMallocHost(&c->plain_stage, kPlainStageBytes) != cudaSuccess) return RT_ERR_CUDA;
+    if (cudaEventCreateWithFlags(&c->ev_staged, cudaEventDisableTiming) != cudaSuccess) return RT_ERR_CUDA;
+    if (cudaEventRecord(c->ev_staged, c->stream) != cudaSuccess) return RT_ERR_CUDA;
     *out = c.release();
     return RT_OK;
 }
@@ -95,9 +113,16 @@ extern "C" void rt_ctx_destroy(rt_ctx *ctx)
     ctx->scenes.clear();
     ctx->frames.clear();
     ctx->batch.reset();
+    ctx->plain_graphs.clear();
     ctx->ws = Workspace();
-    if (ctx->cancel_host) cudaFreeHost((void *)ctx->cancel_host);
+    if (ctx->side) cudaStreamSynchronize(ctx->side);
+    if (ctx->cancel_dev) cudaFree(ctx->cancel_dev);
+    if (ctx->cancel_vals) cudaFreeHost(ctx->cancel_vals);
+    if (ctx->ev_armed) cudaEventDestroy(ctx->ev_armed);
+    if (ctx->side) cudaStreamDestroy(ctx->side);
     if (ctx->counters_host) cudaFreeHost(ctx->counters_host);
+    if (ctx->plain_stage) cudaFreeHost(ctx->plain_stage);
+    if (ctx->ev_staged) cudaEventDestroy(ctx->ev_staged);
     cudaEventDestroy(ctx->ev_start);
     cudaEventDestroy(ctx->ev_stop);
     cudaStreamDestroy(ctx->own_stream);
@@ -715,6 +740,41 @@ void enqueue_levels(rt_ctx *ctx, Workspace &ws, int max_level, const Tuning &t, 
     }
 }
 
+// the level loop of a plain render as a CUDA graph, captured once per (depth, tuning) and
+// recaptured when the workspace moves
+static int plain_graph(rt_ctx *ctx, int max_level, const Tuning &t, cudaGraphExec_t &exec)
+{
+    Workspace &ws = ctx->ws;
+    if (ctx->plain_graph_ws != ws.mem.p) {
+        ctx->plain_graphs.clear();
+        ctx->plain_graph_ws = ws.mem.p;
+    }
+    const long long key = ((long long)max_level << 40) ^ ((long long)t.block << 24) ^ ((long long)t.tile << 8) ^
+                          (long long)t.stack ^ ((long long)t.dynamic << 50) ^ ((long long)t.min_blocks << 52) ^
+                          ((long long)t.count << 58);
+    auto it = ctx->plain_graphs.find(key);
+    if (it != ctx->plain_graphs.end()) {
+        exec = it->second->exec;
+        return RT_OK;
+    }
+    cudaStream_t cap;
+    CK(ctx, cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+    cudaGraph_t g;
+    cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
+    cudaMemsetAsync(ws.wf.C, 0, sizeof(Counters), cap);
+    enqueue_levels(ctx, ws, max_level, t, cap, nullptr);
+    cudaError_t e = cudaStreamEndCapture(cap, &g);
+    cudaStreamDestroy(cap);
+    if (e != cudaSuccess) return ctx_fail(ctx, RT_ERR_CUDA, "graph capture: %s", cudaGetErrorString(e));
+    std::unique_ptr<GraphEntry> ge(new GraphEntry());
+    e = cudaGraphInstantiate(&ge->exec, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return ctx_fail(ctx, RT_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
+    exec = ge->exec;
+    ctx->plain_graphs[key] = std::move(ge);
+    return RT_OK;
+}
+
 static int render_once(rt_ctx *ctx, SceneDev &sc, FrameDev &f, const rt_render_desc *rd, long long qcap)
 {
     DevJob J;
@@ -727,21 +787,27 @@ static int render_once(rt_ctx *ctx, SceneDev &sc, FrameDev &f, const rt_render_d
     Workspace &ws = ctx->ws;
     cudaStream_t s = ctx->stream;
     ws.wf.cancel = ctx->cancel_dev;
-    *ctx->cancel_host = 0;
-    ctx->h_scalars[0] = samples;
-    ctx->h_scalars[1] = 0;
-    ctx->h_scalars[2] = 1;
-    ctx->h_scalars[3] = sc.hdr.n_lights;
-    ctx->h_job_end[0] = samples;
+    rc = cancel_arm(ctx);
+    if (rc) return rc;
+    // the job tables (job, its sample end, the wave scalars, the scene header) go up in one copy
+    // from page-locked memory laid out as in the workspace
+    char *dst = (char *)ws.jobs;
+    const size_t span = (size_t)((char *)ws.scenes + sizeof(DevScene) - dst);
+    if (span > kPlainStageBytes) return ctx_fail(ctx, RT_ERR_INVALID, "job tables of %zu bytes exceed the staging", span);
+    CK(ctx, cudaEventSynchronize(ctx->ev_staged));   // the previous render's copy has left the staging
+    char *st = (char *)ctx->plain_stage;
+    const long long end = samples, scal[4] = {samples, 0, 1, sc.hdr.n_lights};
+    std::memcpy(st + ((char *)ws.jobs - dst), &J, sizeof J);
+    std::memcpy(st + ((char *)ws.job_end - dst), &end, sizeof end);
+    std::memcpy(st + ((char *)ws.scalars - dst), scal, sizeof scal);
+    std::memcpy(st + ((char *)ws.scenes - dst), &sc.hdr, sizeof(DevScene));
     CK(ctx, cudaEventRecord(ctx->ev_start, s));
-    CK(ctx, cudaMemcpyAsync(ws.scenes, &sc.hdr, sizeof(DevScene), cudaMemcpyHostToDevice, s));
-    CK(ctx, cudaMemcpyAsync(ws.jobs, &J, sizeof(DevJob), cudaMemcpyHostToDevice, s));
-    CK(ctx, cudaMemcpyAsync(ws.job_end, ctx->h_job_end, 8, cudaMemcpyHostToDevice, s));
-    CK(ctx, cudaMemcpyAsync(ws.scalars, ctx->h_scalars, 32, cudaMemcpyHostToDevice, s));
-    CK(ctx, cudaMemsetAsync(ws.wf.C, 0, sizeof(Counters), s));
+    CK(ctx, cudaMemcpyAsync(dst, st, span, cudaMemcpyHostToDevice, s));
+    CK(ctx, cudaEventRecord(ctx->ev_staged, s));
     CK(ctx, cudaMemsetAsync(f.fb.acc, 0, 24 * (size_t)f.w * f.h, s));
     KernelProfiler &P = ctx->prof;
-    P.reset((rd->flags & RT_FLAG_PROFILE) != 0);
+    const bool profile = (rd->flags & RT_FLAG_PROFILE) != 0;
+    P.reset(profile);
     if (rd->flags & RT_FLAG_HIT_PLANES) {
         P.begin(RT_KERNEL_OTHER, s);
         launch_plane_init(f.fb, (long long)f.w * f.h, s);
@@ -749,7 +815,18 @@ static int render_once(rt_ctx *ctx, SceneDev &sc, FrameDev &f, const rt_render_d
     }
     Tuning t = ctx->plain_tuning;
     t.count = (rd->flags & RT_FLAG_COUNT_WORK) != 0;
-    enqueue_levels(ctx, ws, rd->max_level, t, s, &P);
+    if (profile) {   // kernels one by one between events
+        CK(ctx, cudaMemsetAsync(ws.wf.C, 0, sizeof(Counters), s));
+        enqueue_levels(ctx, ws, rd->max_level, t, s, &P);
+    } else {
+        cudaGraphExec_t exec = nullptr;
+        rc = plain_graph(ctx, rd->max_level, t, exec);
+        if (rc) return rc;
+        CK(ctx, cudaGraphLaunch(exec, s));
+        // launches of the captured sequence, as the profiler would count them
+        P.launches[RT_KERNEL_RAYGEN] = 1;
+        P.launches[RT_KERNEL_EXTEND] = P.launches[RT_KERNEL_SHADE] = P.launches[RT_KERNEL_SHADOW] = rd->max_level + 1;
+    }
     P.begin(RT_KERNEL_RESOLVE, s);
     launch_resolve(f.fb, f.w, f.h, rd->spp, s);
     P.end(s);
@@ -788,8 +865,8 @@ extern "C" int rt_render_wait(rt_ctx *ctx, rt_render_stats *stats)
         CK(ctx, cudaEventSynchronize(ctx->ev_stop));
     }
     ctx->pending.retries = retries;
-    const bool was_cancelled = *ctx->cancel_host != 0;
-    *ctx->cancel_host = 0;
+    const bool was_cancelled = ctx->cancel_host != 0;
+    ctx->cancel_host = 0;
     if (stats) {
         const Counters &C = *ctx->counters_host;
         stats->rays_primary = (int64_t)C.rays_primary;
@@ -823,6 +900,8 @@ int tuning_from(rt_ctx *ctx, const rt_batch_tuning *in, Tuning &t)
     if (in->tile) t.tile = in->tile;
     if (in->stack) t.stack = in->stack;
     t.min_blocks = in->min_blocks;
+    if (in->dynamic < 0 || in->dynamic > 2) return ctx_fail(ctx, RT_ERR_INVALID, "dynamic %d: use 0, 1 or 2", in->dynamic);
+    t.dynamic = in->dynamic != 2;
     if (t.block % 32 || t.block < 32 || t.block > 256 || t.tile % 32 || t.tile <= 0)
         return ctx_fail(ctx, RT_ERR_INVALID, "tuning block %d / tile %d not supported", t.block, t.tile);
     if (t.min_blocks != 0 && t.min_blocks != 6 && t.min_blocks != 8 && t.min_blocks != 10 && t.min_blocks != 12)
@@ -839,7 +918,6 @@ extern "C" int rt_ctx_set_tuning(rt_ctx *ctx, const rt_batch_tuning *tuning)
     if (tuning) {
         int rc = tuning_from(ctx, tuning, t);
         if (rc) return rc;
-        t.dynamic = tuning->dynamic != 0;
     }
     ctx->plain_tuning = t;
     return RT_OK;
@@ -848,7 +926,8 @@ extern "C" int rt_ctx_set_tuning(rt_ctx *ctx, const rt_batch_tuning *tuning)
 extern "C" int rt_cancel(rt_ctx *ctx)
 {
     if (!ctx) return RT_ERR_INVALID;
-    *ctx->cancel_host = 1;
+    ctx->cancel_host = 1;
+    CK(ctx, cudaMemcpyAsync(ctx->cancel_dev, ctx->cancel_vals + 1, sizeof(int), cudaMemcpyHostToDevice, ctx->side));
     return RT_OK;
 }
 
@@ -928,6 +1007,34 @@ extern "C" int rt_scene_bvh_download(rt_ctx *ctx, int32_t id, float *nodes, uint
             perm[k] = tag >= 0 ? (uint32_t)id32 : (0x80000000u | (uint32_t)(-1 - tag));
         }
     }
+    CK(ctx, cudaStreamSynchronize(s));
+    return RT_OK;
+}
+
+// ---- test hook: the kernels' integer-exact conversions ------------------------------------------------------
+extern "C" int rt_selftest_conversions(rt_ctx *ctx, const int64_t *x, int32_t n, double d, const float *v,
+                                       float *out_mul, int64_t *out_fix)
+{
+    if (!ctx || n < 0 || (n && (!x || !v || !out_mul || !out_fix)) || !(d > 0) || !std::isfinite(d))
+        return RT_ERR_INVALID;
+    if (n == 0) return RT_OK;
+    CK(ctx, cudaSetDevice(ctx->device));
+    DevBuf buf;
+    const size_t nn = (size_t)n;
+    CK(ctx, buf.ensure(nn * (8 + 4 + 4 + 8)));
+    char *b = (char *)buf.p;
+    long long *dx = (long long *)b;
+    long long *dfix = (long long *)(b + 8 * nn);
+    float *dv = (float *)(b + 16 * nn), *dmul = (float *)(b + 20 * nn);
+    unsigned long long bits;
+    std::memcpy(&bits, &d, sizeof bits);
+    cudaStream_t s = ctx->stream;
+    CK(ctx, cudaMemcpyAsync(dx, x, 8 * nn, cudaMemcpyHostToDevice, s));
+    CK(ctx, cudaMemcpyAsync(dv, v, 4 * nn, cudaMemcpyHostToDevice, s));
+    launch_selftest_conversions(dx, n, bits, dv, dmul, dfix, s);
+    CK(ctx, cudaGetLastError());
+    CK(ctx, cudaMemcpyAsync(out_mul, dmul, 4 * nn, cudaMemcpyDeviceToHost, s));
+    CK(ctx, cudaMemcpyAsync(out_fix, dfix, 8 * nn, cudaMemcpyDeviceToHost, s));
     CK(ctx, cudaStreamSynchronize(s));
     return RT_OK;
 }

@@ -181,10 +181,12 @@ int wave_runner_init(rt_ctx *ctx, WaveRunner &R, long long qcap, int jobcap, int
 // plan and enqueue the next wave from `jobs` (taken in order) on stream s; waits only when the
 // staging ring is full. Sets *samples to the samples enqueued (0 = nothing left to trace).
 int wave_enqueue(rt_ctx *ctx, WaveRunner &R, const std::vector<WaveJob *> &jobs, const rtg::Tuning &t, bool use_graph,
-                 cudaStream_t s, long long *samples);
+                 cudaStream_t s, long long *samples, KernelProfiler *prof = nullptr);
 // harvest every finished wave (wait = block until all enqueued waves are done)
 int wave_harvest(rt_ctx *ctx, WaveRunner &R, bool wait);
 size_t wave_runner_bytes(const WaveRunner &R);
+
+constexpr size_t kPlainStageBytes = 4096;
 
 struct rt_ctx {
     int device = 0;
@@ -196,8 +198,11 @@ struct rt_ctx {
     int next_scene = 0, next_frame = 0;
     Workspace ws;
     DevBuf lbvh_scratch;
-    volatile int *cancel_host = nullptr;
-    int *cancel_dev = nullptr;
+    volatile int cancel_host = 0;        // rt_cancel was called since the render started
+    int *cancel_dev = nullptr;           // device copy the kernels read (written on `side`)
+    int *cancel_vals = nullptr;          // page-locked {0, 1}: sources of those writes
+    cudaStream_t side = nullptr;         // cancel writes, ordered apart from the render stream
+    cudaEvent_t ev_armed = nullptr;      // the last clear of the device flag
     rtg::Counters *counters_host = nullptr;
     long long h_scalars[4] = {0, 0, 0, 0};
     long long h_job_end[1] = {0};
@@ -205,9 +210,15 @@ struct rt_ctx {
     rtg::Tuning plain_tuning;
     KernelProfiler prof;
     std::unique_ptr<WaveRunner> batch;   // workspace + graphs of rt_batch_render
+    std::map<long long, std::unique_ptr<GraphEntry>> plain_graphs;   // level loops of rt_render
+    void *plain_graph_ws = nullptr;      // workspace the plain graphs point into
+    void *plain_stage = nullptr;         // page-locked staging of the plain job tables
+    cudaEvent_t ev_staged = nullptr;     // the last staging copy
 };
 
 int ctx_fail(rt_ctx *ctx, int code, const char *fmt, ...);
+// clear the cancel flag for a render about to be enqueued on the context stream
+int cancel_arm(rt_ctx *ctx);
 #define CK(ctx, call)                                                                                             \
     do {                                                                                                          \
         cudaError_t e_ = (call);                                                                                  \

@@ -13,21 +13,25 @@
 // the sum independent of the order in which rays finish: the same frame gives the same bits
 // alone or batched with other frames.
 #include <cstdio>
+#include <cstring>
 
+#include <map>
+#include <mutex>
+
+#include "rt_fixed.cuh"
 #include "rt_kernels.cuh"
 #include "rt_trace.cuh"
 
 namespace rtg {
 
 constexpr unsigned kFull = 0xffffffffu;
-constexpr float kFix = 4294967296.0f;   // 2^32
 
 __device__ __forceinline__ void acc_add(long long *acc, int pix, V3 c)
 {
     unsigned long long *a = reinterpret_cast<unsigned long long *>(acc + 3ll * pix);
-    if (c.x != 0.0f && c.x == c.x) atomicAdd(a + 0, (unsigned long long)__float2ll_rn(c.x * kFix));
-    if (c.y != 0.0f && c.y == c.y) atomicAdd(a + 1, (unsigned long long)__float2ll_rn(c.y * kFix));
-    if (c.z != 0.0f && c.z == c.z) atomicAdd(a + 2, (unsigned long long)__float2ll_rn(c.z * kFix));
+    if (c.x != 0.0f && c.x == c.x) atomicAdd(a + 0, (unsigned long long)float_to_fix32(c.x));
+    if (c.y != 0.0f && c.y == c.y) atomicAdd(a + 1, (unsigned long long)float_to_fix32(c.y));
+    if (c.z != 0.0f && c.z == c.z) atomicAdd(a + 2, (unsigned long long)float_to_fix32(c.z));
 }
 
 // Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11)
@@ -45,26 +49,59 @@ __device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint2 k)
     return c;
 }
 
-// warp-uniform loop over the rays [0, n): static grid stride, or tiles pulled from a counter
+// Warp-uniform loops over the rays [0, n).
+//
+// for_each_ray: each warp first takes its own 32 rays (no atomics: a launch with at most
+// 32 x warps rays touches no counter), then the rest by grid stride (DYN false) or in `tile`-ray
+// tiles pulled from a counter (DYN true) — fine-grained, for traversal, whose cost per ray
+// varies by orders of magnitude.
 template <bool DYN, class F>
 __device__ __forceinline__ void for_each_ray(int n, int *work, int tile, F &&body)
 {
     const int lane = threadIdx.x & 31;
+    const int nw = gridDim.x * (blockDim.x >> 5);
+    const int w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const int first = min(n, nw * 32);   // the static prefix
+    if (w * 32 < first) body(w * 32 + lane, w * 32 + lane < first);
+    if (first >= n) return;
     if (!DYN) {
-        long long nw = (long long)gridDim.x * (blockDim.x >> 5);
-        long long w = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-        for (long long base = w * 32; base < n; base += nw * 32)
+        for (long long base = (long long)first + (long long)w * 32; base < n; base += (long long)nw * 32)
             body((int)(base + lane), base + lane < n);
     } else {
         while (true) {
             int start = 0;
             if (lane == 0) start = atomicAdd(work, tile);
-            start = __shfl_sync(kFull, start, 0);
+            start = first + __shfl_sync(kFull, start, 0);
             if (start >= n) break;
-            int end = min(start + tile, n);
+            const int end = min(start + tile, n);
             for (int base = start; base < end; base += 32)
                 body(base + lane, base + lane < end);
         }
+    }
+}
+
+// for_each_ray_guided: for cheap, even work (shading). Chunks take a share of what is left
+// (left / (2 x warps), at least `tile` rays): few atomics on the one counter address, where
+// they serialise. The counter ends below 1.5 n + 32 x warps.
+template <bool DYN, class F>
+__device__ __forceinline__ void for_each_ray_guided(int n, int *work, int tile, F &&body)
+{
+    if (!DYN) {
+        for_each_ray<false>(n, work, tile, body);
+        return;
+    }
+    const int lane = threadIdx.x & 31;
+    const int nw = gridDim.x * (blockDim.x >> 5);
+    int chunk = max(tile, ((n / (2 * nw)) + 31) & ~31);
+    while (true) {
+        int start = 0;
+        if (lane == 0) start = atomicAdd(work, chunk);
+        start = __shfl_sync(kFull, start, 0);
+        if (start >= n) break;
+        const int end = min(start + chunk, n);
+        for (int base = start; base < end; base += 32)
+            body(base + lane, base + lane < end);
+        chunk = max(tile, (((n - end) / (2 * nw)) + 31) & ~31);
     }
 }
 
@@ -101,12 +138,16 @@ __global__ void k_raygen(Wavefront wf)
             unsigned pix = (unsigned)(row * J.width + col);
             uint4 r = philox4x32_10(make_uint4(pix, 0u, (unsigned)s, 0u),
                                     make_uint2((unsigned)J.seed, (unsigned)(J.seed >> 32)));
-            double jx = (double)(r.x >> 8) * (1.0 / 16777216.0), jy = (double)(r.y >> 8) * (1.0 / 16777216.0);
-            a = __double2float_rn(((double)xcur + jx) * J.dp);
-            b = __double2float_rn(((double)ycur + jy) * J.dp);
-        } else {
-            a = __double2float_rn((double)xcur * J.dp);
-            b = __double2float_rn((double)ycur * J.dp);
+            // (float)(((double)xcur + (r >> 8) * 2^-24) * dp): the sum is exact in 38 bits, so it
+            // is the integer xcur * 2^24 + (r >> 8) times dp * 2^-24
+            DSplit d = split_double_bits((unsigned long long)__double_as_longlong(J.dp));
+            d.e -= 24;
+            a = dmul_to_float((long long)xcur * 16777216ll + (long long)(r.x >> 8), d);
+            b = dmul_to_float((long long)ycur * 16777216ll + (long long)(r.y >> 8), d);
+        } else {   // (float)((double)xcur * dp)
+            const DSplit d = split_double_bits((unsigned long long)__double_as_longlong(J.dp));
+            a = dmul_to_float(xcur, d);
+            b = dmul_to_float(ycur, d);
         }
         V3 n = mk(J.cam_n[0], J.cam_n[1], J.cam_n[2]);
         V3 u = mk(J.cam_u[0], J.cam_u[1], J.cam_u[2]);
@@ -214,16 +255,17 @@ __global__ void __launch_bounds__(256) k_shade(Wavefront wf, int sel, int wslot,
     const int n = min(C->q_count[sel], q.capacity);
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
-    for_each_ray<DYN>(n, &C->work[wslot], tile, [&](int i, bool active) {
+    for_each_ray_guided<DYN>(n, &C->work[wslot], tile, [&](int i, bool active) {
         bool emit = false;
         int nchild = 0;
         float4 c_o[2], c_d[2], c_w[2];
         int4 c_m[2];
         float4 s_p, s_n, s_v, s_wc, s_ws;
-        if (active) {
+        const float4 h4 = active ? wf.hit[i] : make_float4(0.0f, 0.0f, 0.0f, __int_as_float(-1));
+        const int4 m4 = active ? q.m[i] : make_int4(0, 0, 0, 0);
+        // a miss of a ray that writes no hit plane has nothing to shade: skip its other loads
+        if (active && (__float_as_int(h4.w) >= 0 || ray_plane(m4.y))) {
             const float4 o4 = q.o[i], d4 = q.d[i], w4 = q.w[i];
-            const int4 m4 = q.m[i];
-            const float4 h4 = wf.hit[i];
             const int nob = wf.newobj[i];
             const DevJob &J = wf.jobs[m4.w];
             const DevScene &S = wf.scenes[J.scene];
@@ -477,12 +519,12 @@ __device__ __forceinline__ uint8_t put_channel(float c)
     if (c < 0.0f || c != c) return 0;
     return (uint8_t)(int)(c * 255);
 }
-__global__ void k_resolve(FrameBufs fb, long long npix, int spp)
+// colour = (float)((double)acc * scale), scale = 2^-32 / spp in double (split on the host)
+__global__ void k_resolve(FrameBufs fb, long long npix, DSplit scale)
 {
-    const double scale = 1.0 / 4294967296.0 / (double)spp;
     for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < npix; p += (long long)gridDim.x * blockDim.x) {
         float c[3];
-        for (int k = 0; k < 3; ++k) c[k] = (float)((double)fb.acc[3 * p + k] * scale);
+        for (int k = 0; k < 3; ++k) c[k] = dmul_to_float(fb.acc[3 * p + k], scale);
         if (fb.rgb) {
             fb.rgb[3 * p] = c[0];
             fb.rgb[3 * p + 1] = c[1];
@@ -494,6 +536,22 @@ __global__ void k_resolve(FrameBufs fb, long long npix, int spp)
             fb.rgb8[3 * p + 2] = put_channel(c[2]);
         }
     }
+}
+
+__global__ void k_selftest_conversions(const long long *x, int n, DSplit d, const float *v, float *out_mul,
+                                       long long *out_fix)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        out_mul[i] = dmul_to_float(x[i], d);
+        out_fix[i] = float_to_fix32(v[i]);
+    }
+}
+
+void launch_selftest_conversions(const long long *x, int n, unsigned long long d_bits, const float *v, float *out_mul,
+                                 long long *out_fix, cudaStream_t s)
+{
+    k_selftest_conversions<<<std::max(1, std::min((n + 255) / 256, sm_count() * 4)), 256, 0, s>>>(
+        x, n, split_double_bits(d_bits), v, out_mul, out_fix);
 }
 
 __global__ void k_plane_init(FrameBufs fb, long long npix)
@@ -518,13 +576,22 @@ int sm_count()
     return n;
 }
 
+// resident blocks per SM of a kernel at a block size, queried once (the query costs host time
+// on every launch otherwise, which small renders feel as idle gaps between kernels)
 static int grid_for(const Tuning &t, const void *kernel)
 {
     if (t.grid > 0) return t.grid;
-    int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, t.block, 0);
-    if (per_sm <= 0) per_sm = 1;
-    return sm_count() * per_sm;
+    static std::mutex mu;
+    static std::map<std::pair<const void *, int>, int> cache;
+    std::lock_guard<std::mutex> lock(mu);
+    auto key = std::make_pair(kernel, t.block);
+    auto it = cache.find(key);
+    if (it == cache.end()) {
+        int per_sm = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, t.block, 0);
+        it = cache.emplace(key, per_sm > 0 ? per_sm : 1).first;
+    }
+    return sm_count() * it->second;
 }
 
 void launch_raygen(const Wavefront &wf, int grid, int block, cudaStream_t s)
@@ -599,7 +666,10 @@ void launch_resolve(const FrameBufs &fb, int width, int height, int spp, cudaStr
     long long npix = (long long)width * height;
     int grid = (int)std::min<long long>((npix + 255) / 256, (long long)sm_count() * 8);
     if (grid < 1) grid = 1;
-    k_resolve<<<grid, 256, 0, s>>>(fb, npix, spp);
+    const double scale = 1.0 / 4294967296.0 / (double)spp;
+    unsigned long long bits;
+    std::memcpy(&bits, &scale, sizeof bits);
+    k_resolve<<<grid, 256, 0, s>>>(fb, npix, split_double_bits(bits));
 }
 
 void launch_plane_init(const FrameBufs &fb, long long npix, cudaStream_t s)

@@ -30,7 +30,7 @@ struct Wavefront {
     float4 *hit;
     int *newobj;
     Counters *C;
-    const volatile int *cancel;       // host-mapped cancel flag (may be NULL)
+    const volatile int *cancel;       // device cancel flag (NULL = not cancellable)
 };
 
 struct Tuning {
@@ -51,5 +51,8 @@ void launch_shade(const Wavefront &wf, int sel, int level, const Tuning &t, cuda
 void launch_shadow(const Wavefront &wf, int level, const Tuning &t, cudaStream_t s);
 void launch_resolve(const FrameBufs &fb, int width, int height, int spp, cudaStream_t s);
 void launch_plane_init(const FrameBufs &fb, long long npix, cudaStream_t s);
+// the integer-exact conversions of the kernels, on n inputs (a test hook)
+void launch_selftest_conversions(const long long *x, int n, unsigned long long d_bits, const float *v, float *out_mul,
+                                 long long *out_fix, cudaStream_t s);
 
 } // namespace rtg

@@ -113,9 +113,9 @@ __device__ __forceinline__ RayInv make_inv(V3 O, V3 D)
 {
     auto safe = [](float d) { return fabsf(d) < 1e-30f ? copysignf(1e-30f, d) : d; };
     RayInv r;
-    r.ix = 1.0f / safe(D.x);
-    r.iy = 1.0f / safe(D.y);
-    r.iz = 1.0f / safe(D.z);
+    r.ix = __frcp_rn(safe(D.x));   // the correctly rounded 1/d, as 1.0f / d
+    r.iy = __frcp_rn(safe(D.y));
+    r.iz = __frcp_rn(safe(D.z));
     r.ox = O.x * r.ix;
     r.oy = O.y * r.iy;
     r.oz = O.z * r.iz;
