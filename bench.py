@@ -258,6 +258,41 @@ def run_served(ctx, seconds: float) -> dict:
     return out
 
 
+def run_served_replicas(ctx, seconds: float, rank: int, world: int) -> dict | None:
+    """Config 4 on N GPUs: each rank keeps the scenes the owner map gives it and serves their
+    share of the stream (a Poisson stream split by an independent uniform scene choice is a
+    Poisson stream per rank, of rate lambda x owned / 64); latencies merge exactly on rank 0."""
+    import time as _t
+
+    import numpy as np
+    import torch.distributed as dist
+
+    import raytrace_gb300 as rt
+    from raytrace_gb300 import replicas
+
+    scenes = gen_scenes(4, 64)
+    owner = replicas.owner_map([int(s.nbytes) for s in scenes], world)
+    mine = [s for s, o in zip(scenes, owner) if o == rank]
+    out = {"workload": "config4 replicas: scenes split by the owner map, one continuous-batching server per GPU",
+           "scenes_per_rank": [owner.count(r) for r in range(world)]}
+    with rt.Server(ctx, 120 << 30, max_inflight=64, keep_images=False) as srv:
+        for sc in mine:
+            srv.add_scene(sc)
+        for lam in (50, 200, 800, 20000):
+            dur = seconds if lam < 20000 else 0.05
+            dist.barrier()
+            t0 = _t.time()
+            st = srv.run_poisson(lam * len(mine) / 64.0, dur, seed=4 + 1000 * rank) if mine else None
+            res = replicas.RankResult(rank, srv.latencies() if mine else np.zeros(0), int(st["rays"]) if st else 0,
+                                      int(st["pixels"]) if st else 0, int(st["completed"]) if st else 0,
+                                      int(st["requests"]) if st else 0, int(st["rejected"]) if st else 0,
+                                      t0, t0 + (st["wall_s"] if st else 0.0))
+            merged = replicas.gather(res)
+            if rank == 0:
+                out[f"lambda_{lam}" if lam < 20000 else "saturated"] = merged
+    return out if rank == 0 else None
+
+
 def run_gpu(args) -> None:
     import numpy as np
     import torch
@@ -327,6 +362,9 @@ def run_gpu(args) -> None:
         torch.distributed.all_reduce(r, op=torch.distributed.ReduceOp.SUM)
         dev_s, e2e_s, wall = t.tolist()
         rays, e2e_rays = r.tolist()
+    served_replicas = None
+    if world > 1 and not args.skip_served:   # every rank serves its scenes; rank 0 merges
+        served_replicas = run_served_replicas(ctx, args.served_seconds, rank, world)
     if rank != 0:
         torch.distributed.destroy_process_group()
         return
@@ -390,6 +428,8 @@ def run_gpu(args) -> None:
         "wall_s_timed": round(wall, 4),
         "bvh_build_ms": round(ctx.build_ms(sid), 3),
     }
+    if served_replicas is not None:
+        out["served"] = served_replicas
     if world == 1 and not args.skip_batched:
         out["batched"] = run_batched(ctx, args.batched_scenes, 2)
     if world == 1 and not args.skip_served:

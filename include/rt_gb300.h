@@ -321,6 +321,9 @@ int    rt_server_resident(rt_server *srv, int32_t scene, int32_t *resident);
 double rt_server_now(rt_server *srv);
 /* counters since creation or the last rt_server_run_poisson; latency over finished requests */
 int    rt_server_stats(rt_server *srv, rt_serve_stats *stats);
+/* frame latencies (ms, completion order) behind the current stats; *n = their count, at most
+ * `cap` are copied (replicas merge these to exact percentiles across GPUs) */
+int    rt_server_latencies(rt_server *srv, double *ms, int64_t cap, int64_t *n);
 /* a Poisson stream of requests in real time over the registered scenes: scene uniform, camera
  * orbiting the world origin at the distance of the scene's own camera (azimuth U[0,360),
  * elevation U[10,60] degrees), resolution uniform over 256^2, 512^2, 1024x768, 1920x1080.

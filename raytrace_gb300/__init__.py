@@ -158,6 +158,7 @@ _SIGS = {
     "rt_selftest_conversions": (C.c_int, [P, P, C.c_int32, C.c_double, P, P, P]),
     "rt_server_last_error": (C.c_char_p, [P]),
     "rt_server_stats": (C.c_int, [P, C.POINTER(ServeStats)]),
+    "rt_server_latencies": (C.c_int, [P, P, C.c_int64, C.POINTER(C.c_int64)]),
     "rt_orbit_camera": (C.c_int, [C.POINTER(Camera), C.c_double, C.c_double, C.c_int32, C.c_int32,
                                   C.POINTER(Camera)]),
     "rt_server_add_scene": (C.c_int, [P, C.POINTER(SceneDesc), C.POINTER(C.c_int32)]),
@@ -564,6 +565,14 @@ class Server:
         st = ServeStats()
         self._ck(lib.rt_server_stats(self._h, C.byref(st)), "rt_server_stats")
         return st.as_dict()
+
+    def latencies(self) -> np.ndarray:
+        """Frame latencies (ms) behind the current stats."""
+        n = C.c_int64()
+        self._ck(lib.rt_server_latencies(self._h, None, 0, C.byref(n)), "rt_server_latencies")
+        out = np.empty(n.value, np.float64)
+        self._ck(lib.rt_server_latencies(self._h, _ptr(out), out.size, C.byref(n)), "rt_server_latencies")
+        return out
 
     def run_poisson(self, lam: float, duration_s: float, seed: int = 4) -> dict:
         st = ServeStats()

@@ -742,6 +742,15 @@ int rt_server_stats(rt_server *srv, rt_serve_stats *stats)
     return RT_OK;
 }
 
+int rt_server_latencies(rt_server *srv, double *ms, int64_t cap, int64_t *n)
+{
+    if (!srv || !n || cap < 0 || (cap && !ms)) return RT_ERR_INVALID;
+    *n = (int64_t)srv->latencies_ms.size();
+    const size_t k = std::min(srv->latencies_ms.size(), (size_t)cap);
+    if (k) std::memcpy(ms, srv->latencies_ms.data(), k * sizeof(double));
+    return RT_OK;
+}
+
 int rt_server_run_poisson(rt_server *srv, double lambda, double duration, uint64_t seed, rt_serve_stats *stats)
 {
     if (!srv || !stats || !(lambda > 0) || !(duration > 0) || srv->scenes.empty()) return RT_ERR_INVALID;
