@@ -376,12 +376,12 @@ def run_gpu(args) -> None:
     shadow_items = cnt.rays_shadow / 4           # one work item per hit, 4 lights
     alg = {
         # per shadow ray (one thread per hit and light): the 80-B hit record and a 24-B
-        # fixed-point accumulate, then 64 B per internal node visited (the two 32-B child
-        # records of the pair), 36 B per triangle tested, 16 B per sphere tested
-        "shadow": cnt.rays_shadow * (80 + 24) + 64 * cnt.shadow_nodes_visited + 36 * cnt.shadow_tris_tested
+        # fixed-point accumulate, then 112 B per 4-wide node visited (six float4 of slot
+        # bounds and one of child references), 36 B per triangle tested, 16 B per sphere tested
+        "shadow": cnt.rays_shadow * (80 + 24) + 112 * cnt.shadow_nodes_visited + 36 * cnt.shadow_tris_tested
         + 16 * cnt.shadow_spheres_tested,
         # ray 48 B read, hit 20 B written, then the traversal as above
-        "extend": (cnt.rays_primary + cnt.rays_secondary) * (48 + 20) + 64 * cnt.nodes_visited
+        "extend": (cnt.rays_primary + cnt.rays_secondary) * (48 + 20) + 112 * cnt.nodes_visited
         + 36 * cnt.tris_tested + 16 * cnt.spheres_tested,
         # ray 64 B + hit 20 B read, children 64 B and shadow record 80 B written, accumulate 24 B
         "shade": (cnt.rays_primary + cnt.rays_secondary) * (64 + 20 + 24) + cnt.rays_secondary * 64

@@ -227,7 +227,7 @@ int rt_render_host(rt_ctx *ctx, const rt_scene_desc *desc, const rt_render_desc 
 typedef struct rt_batch_tuning {
     int32_t block;               /* threads per block of the traversal kernels (0 = default) */
     int32_t tile;                /* rays taken per work-counter fetch (0 = default) */
-    int32_t stack;               /* traversal stack entries; 64 holds any LBVH (0 = default) */
+    int32_t stack;               /* traversal stack entries: 0 or 96 (fixed; 96 holds any path) */
     int32_t use_graph;           /* capture the per-bounce launch sequence as a CUDA graph */
     int32_t min_blocks;          /* 0, 6, 8, 10 or 12: resident 128-thread blocks per SM the register
                                     budget of the traversal kernels must allow (0 = compiler's) */
@@ -245,7 +245,7 @@ int rt_batch_render(rt_ctx *ctx, int32_t n, const int32_t *scene_ids, const int3
 int rt_batch_render_plain(rt_ctx *ctx, int32_t n, const int32_t *scene_ids,
                           const int32_t *frame_ids, const rt_render_desc *rds);
 /* pick block size, register cap and ray tile (or the static stride) for these jobs by timing
- * candidates; the stack stays at 64 entries (the depth bound of the LBVH). Writes the choice. */
+ * candidates; the stack depth is fixed at the bound of the tree. Writes the choice. */
 int rt_batch_autotune(rt_ctx *ctx, int32_t n, const int32_t *scene_ids, const int32_t *frame_ids,
                       const rt_render_desc *rds, rt_batch_tuning *out);
 

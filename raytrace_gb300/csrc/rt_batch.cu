@@ -312,16 +312,15 @@ extern "C" int rt_batch_autotune(rt_ctx *ctx, int32_t n, const int32_t *scene_id
                                  const rt_render_desc *rds, rt_batch_tuning *out)
 {
     if (!ctx || !out) return RT_ERR_INVALID;
-    // (threads per block, register cap as resident blocks per SM) x rays per tile fetch; the
-    // stack stays at 64 entries, the depth bound of a 30-bit Morton LBVH with index tie-breaks
-    // tile 0 stands for the static grid stride
+    // (threads per block, register cap as resident blocks per SM) x rays per tile fetch
+    // tile 0 stands for the static grid stride; the stack depth is fixed (kStack)
     const int shapes[][2] = {{128, 8}, {128, 6}, {64, 8}, {256, 0}};
     const int tiles[] = {0, 32, 64, 128, 256};
     double best = 1e30;
-    rt_batch_tuning best_t{128, 32, 64, 1, 8, 1, 0};
+    rt_batch_tuning best_t{128, 32, 0, 1, 8, 1, 0};
     for (const auto &sh : shapes)
         for (int tl : tiles) {
-            rt_batch_tuning t{sh[0], tl ? tl : 32, 64, 1, sh[1], tl ? 1 : 2, 0};
+            rt_batch_tuning t{sh[0], tl ? tl : 32, 0, 1, sh[1], tl ? 1 : 2, 0};
             int rc = rt_batch_render(ctx, n, scene_ids, frame_ids, rds, &t);   // warm (captures the graph)
             if (rc) return rc;
             auto t0 = std::chrono::steady_clock::now();

@@ -341,7 +341,7 @@ extern "C" int rt_scene_upload(rt_ctx *ctx, const rt_scene_desc *d, int32_t *sce
     const size_t o_sph = take(sizeof(float4) * (size_t)std::max(1, n_sph)), o_sphr = take(sizeof(float) * (size_t)std::max(1, n_sph));
     const size_t o_sphp = take(sizeof(int) * (size_t)std::max(1, n_sph)), o_spho = take(sizeof(int) * (size_t)std::max(1, n_sph));
     const size_t o_nodes = take(sizeof(float4) * 2 * (size_t)std::max<int64_t>(1, 2 * L - 1));
-    const size_t o_pairs = take(sizeof(float4) * 4 * (size_t)std::max<int64_t>(1, L - 1));
+    const size_t o_quads = take(sizeof(float4) * 8 * (size_t)std::max<int64_t>(1, L - 1));
     const size_t o_tri = take(sizeof(float4) * 3 * (size_t)L), o_trin = take(sizeof(float4) * 3 * (size_t)L);
     const size_t o_triuv = has_uv ? take(sizeof(float2) * 3 * (size_t)L) : 0;
     const size_t o_hdr = take(sizeof(DevScene));
@@ -431,7 +431,7 @@ extern "C" int rt_scene_upload(rt_ctx *ctx, const rt_scene_desc *d, int32_t *sce
     H.n_tris = (int)n;
     H.n_leaves = (int)L;
     H.nodes = (const float4 *)(base + o_nodes);
-    H.pairs = (const float4 *)(base + o_pairs);
+    H.quads = (const float4 *)(base + o_quads);
     H.tri = (const float4 *)(base + o_tri);
     H.trin = (const float4 *)(base + o_trin);
     H.triuv = has_uv ? (const float2 *)(base + o_triuv) : nullptr;
@@ -458,7 +458,7 @@ extern "C" int rt_scene_upload(rt_ctx *ctx, const rt_scene_desc *d, int32_t *sce
     sc->in.sph_obj = (const int *)(base + o_spho);
     sc->in.n_sph = n_sph;
     sc->out.nodes = (float4 *)(base + o_nodes);
-    sc->out.pairs = (float4 *)(base + o_pairs);
+    sc->out.quads = (float4 *)(base + o_quads);
     sc->out.tri = (float4 *)(base + o_tri);
     sc->out.trin = (float4 *)(base + o_trin);
     sc->out.triuv = has_uv ? (float2 *)(base + o_triuv) : nullptr;
@@ -907,7 +907,7 @@ int tuning_from(rt_ctx *ctx, const rt_batch_tuning *in, Tuning &t)
     if (t.min_blocks != 0 && t.min_blocks != 6 && t.min_blocks != 8 && t.min_blocks != 10 && t.min_blocks != 12)
         return ctx_fail(ctx, RT_ERR_INVALID, "min_blocks %d: use 0, 6, 8, 10 or 12", t.min_blocks);
     if (t.min_blocks && t.block > 128) return ctx_fail(ctx, RT_ERR_INVALID, "min_blocks needs blocks of at most 128 threads");
-    if (t.stack != 64) return ctx_fail(ctx, RT_ERR_INVALID, "stack %d: the traversal needs 64 entries", t.stack);
+    if (t.stack != kStack) return ctx_fail(ctx, RT_ERR_INVALID, "stack %d: the traversal uses %d entries", t.stack, kStack);
     return RT_OK;
 }
 

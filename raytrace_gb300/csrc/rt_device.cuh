@@ -96,7 +96,7 @@ struct DevScene {
     int n_tris;                   // triangles
     int n_leaves;                 // LBVH leaves: triangles + spheres
     const float4 *nodes;          // LBVH: (2L-1) nodes x 2 float4 (min|left, max|right)
-    const float4 *pairs;          // per internal node both children: 4 float4 (min|child, max|-), child<0: leaf ~k
+    const float4 *quads;          // per internal node a 4-wide node of its grandchildren: 8 float4 (see k_quads)
     const float4 *tri;            // per leaf (Morton order): triangle p0|id, e1|obj, e2|mtl; sphere c|r2, 0|obj, 0|-1-prim
     const float4 *trin;           // per leaf: n0, n1, n2
     const float2 *triuv;          // per leaf: uv0, uv1, uv2 (NULL = zero)

@@ -604,7 +604,7 @@ static void extend_launch(const Wavefront &wf, int sel, int wslot, const Tuning 
 {
 #define RT_EXT(MB)                                                                                                \
     {                                                                                                             \
-        auto k = k_extend<64, DYN, CNT, MB>;                                                                      \
+        auto k = k_extend<kStack, DYN, CNT, MB>;                                                                      \
         k<<<grid_for(t, (const void *)k), t.block, 0, s>>>(wf, sel, wslot, t.tile);                              \
     }
     if (t.min_blocks == 8) RT_EXT(8) else if (t.min_blocks == 6) RT_EXT(6) else if (t.min_blocks == 10) RT_EXT(10)
@@ -641,7 +641,7 @@ static void shadow_launch(const Wavefront &wf, int wslot, const Tuning &t, cudaS
 {
 #define RT_SHD(MB)                                                                                                \
     {                                                                                                             \
-        auto k = k_shadow<64, DYN, CNT, MB>;                                                                      \
+        auto k = k_shadow<kStack, DYN, CNT, MB>;                                                                      \
         k<<<grid_for(t, (const void *)k), t.block, 0, s>>>(wf, wslot, t.tile);                                   \
     }
     if (t.min_blocks == 8) RT_SHD(8) else if (t.min_blocks == 6) RT_SHD(6) else if (t.min_blocks == 10) RT_SHD(10)

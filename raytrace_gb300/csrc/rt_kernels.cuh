@@ -33,10 +33,15 @@ struct Wavefront {
     const volatile int *cancel;       // device cancel flag (NULL = not cancellable)
 };
 
+// Traversal stack entries. A Karras node's common prefix grows by at least one bit per level
+// over 30 Morton bits plus the index bits that break ties, so a path has at most 63 binary
+// levels, i.e. 32 four-wide nodes, each pushing at most 3 entries.
+constexpr int kStack = 96;
+
 struct Tuning {
     int block = 128;     // threads per block of the traversal kernels
     int tile = 32;       // rays per dynamic work fetch (multiple of 32)
-    int stack = 64;      // traversal stack entries
+    int stack = kStack;  // traversal stack entries (fixed: see kStack)
     bool dynamic = true; // persistent grid pulling tiles from a global counter
     bool count = false;  // count BVH nodes / triangles / spheres
     int grid = 0;        // blocks (0 = derived from the SM count)

@@ -321,17 +321,46 @@ __global__ void k_refit(int n, float4 *nodes, const int *parent, int *flags)
     }
 }
 
-// both children of internal node i side by side: one 64-byte load per traversal step
-__global__ void k_pairs(int n, const float4 *nodes, float4 *pairs)
+// A 4-wide node for every internal node i: the slots are i's grandchildren — each child's two
+// children when the child is internal, the child itself when it is a leaf — so 2 to 4 slots.
+// Traversal starts at the root and steps from a node to its grandchildren, so it only ever
+// visits even depths: the binary tree collapsed two levels at a time, with no depth pass.
+// Record (128 B, one line): float4 lo.x[4], hi.x[4], lo.y[4], hi.y[4], lo.z[4], hi.z[4], then
+// int4 refs (>= 0 internal node, < 0 leaf ~k, kEmptySlot unused), then padding. An unused
+// slot's box is the point (1e38, 1e38, 1e38), which no ray reaches within a cull distance.
+__global__ void k_quads(int n, const float4 *nodes, float4 *quads)
 {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n - 1; i += gridDim.x * blockDim.x) {
+        float lo[3][4], hi[3][4];
+        int ref[4];
+        int k = 0;
         const int c[2] = {__float_as_int(nodes[2ll * i].w), __float_as_int(nodes[2ll * i + 1].w)};
+        auto put = [&](int x) {
+            const float4 l = __ldcg(&nodes[2ll * x]), h = __ldcg(&nodes[2ll * x + 1]);
+            lo[0][k] = l.x, lo[1][k] = l.y, lo[2][k] = l.z;
+            hi[0][k] = h.x, hi[1][k] = h.y, hi[2][k] = h.z;
+            ref[k] = x >= n - 1 ? ~(x - (n - 1)) : x;
+            ++k;
+        };
         for (int j = 0; j < 2; ++j) {
-            const float4 lo = __ldcg(&nodes[2ll * c[j]]), hi = __ldcg(&nodes[2ll * c[j] + 1]);
-            const int ref = c[j] >= n - 1 ? ~(c[j] - (n - 1)) : c[j];
-            pairs[4ll * i + 2 * j] = make_float4(lo.x, lo.y, lo.z, __int_as_float(ref));
-            pairs[4ll * i + 2 * j + 1] = make_float4(hi.x, hi.y, hi.z, 0.0f);
+            if (c[j] >= n - 1) {
+                put(c[j]);
+            } else {
+                put(__float_as_int(__ldcg(&nodes[2ll * c[j]]).w));
+                put(__float_as_int(__ldcg(&nodes[2ll * c[j] + 1]).w));
+            }
         }
+        for (; k < 4; ++k) {   // a point at 1e38: its entry distance exceeds every cull (<= 1e20)
+            for (int a = 0; a < 3; ++a) lo[a][k] = hi[a][k] = 1e38f;
+            ref[k] = kEmptySlot;
+        }
+        float4 *q = quads + 8ll * i;
+        for (int a = 0; a < 3; ++a) {
+            q[2 * a] = make_float4(lo[a][0], lo[a][1], lo[a][2], lo[a][3]);
+            q[2 * a + 1] = make_float4(hi[a][0], hi[a][1], hi[a][2], hi[a][3]);
+        }
+        q[6] = make_float4(__int_as_float(ref[0]), __int_as_float(ref[1]), __int_as_float(ref[2]), __int_as_float(ref[3]));
+        q[7] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     }
 }
 
@@ -448,7 +477,7 @@ cudaError_t lbvh_build(const LbvhInput &in, const LbvhOutput &out, void *scratch
         k_karras<<<grid_of(n - 1, 256), 256, 0, s>>>(n, sc.codes[0], out.nodes, sc.parent);
         cudaMemsetAsync(sc.flags, 0, 4 * (size_t)(n - 1), s);
         k_refit<<<grid_of(n, 256), 256, 0, s>>>(n, out.nodes, sc.parent, sc.flags);
-        if (out.pairs) k_pairs<<<grid_of(n - 1, 256), 256, 0, s>>>(n, out.nodes, out.pairs);
+        if (out.quads) k_quads<<<grid_of(n - 1, 256), 256, 0, s>>>(n, out.nodes, out.quads);
     }
     return cudaGetLastError();
 }

@@ -5,6 +5,9 @@
 
 namespace rtg {
 
+// an unused slot of a 4-wide node (no leaf index reaches ~0x80000000)
+constexpr int kEmptySlot = (int)0x80000000;
+
 // inputs of one build, all device pointers; triangle i of the scene has points tri_p[9i..],
 // normals tri_n[9i..], optional uvs tri_uv[6i..], material tri_mtl[i], reported id tri_id[i]
 // and object index tri_obj[i] (whose position obj_pos[3*obj..] is added to the points)
@@ -26,7 +29,7 @@ struct LbvhInput {
 //   sphere:   (centre | r*r),     (0 | object),  (0 | -1 - primitive index)
 struct LbvhOutput {
     float4 *nodes;   // 2 * (2L-1): own box per node, for refit and inspection
-    float4 *pairs;   // 4 * (L-1): per internal node both children (min|child, max|-), child < 0 = leaf ~k
+    float4 *quads;   // 8 * (L-1): per internal node its grandchildren (4-wide node), see k_quads
     float4 *tri;     // 3L leaf records
     float4 *trin;    // 3L (vertex normals; zero for spheres)
     float2 *triuv;   // 3L or NULL

@@ -399,6 +399,16 @@ static int pending(const rt_server *srv)
     return (int)(srv->queue.size() + srv->inflight.size() + srv->resolving.size());
 }
 
+static void wave_order(const rt_server *srv, std::vector<WaveJob *> &order)
+{
+    order.clear();
+    for (Request *r : srv->inflight)
+        if (r->wj.cursor < r->wj.total) order.push_back(&r->wj);
+}
+
+// retire, admit, enqueue one wave. With nothing left to enqueue, wait for the oldest frame in
+// flight and admit again, so a step that returns with nothing in flight and a non-empty queue
+// means the queue head cannot be admitted at all.
 static int step_batched(rt_server *srv)
 {
     rt_ctx *ctx = srv->ctx;
@@ -407,8 +417,14 @@ static int step_batched(rt_server *srv)
     rc = admit(srv);
     if (rc) return rc;
     std::vector<WaveJob *> order;
-    for (Request *r : srv->inflight)
-        if (r->wj.cursor < r->wj.total) order.push_back(&r->wj);
+    wave_order(srv, order);
+    if (order.empty() && !srv->resolving.empty()) {
+        rc = retire(srv, true);
+        if (rc) return rc;
+        rc = admit(srv);
+        if (rc) return rc;
+        wave_order(srv, order);
+    }
     if (!order.empty()) {
         long long got = 0;
         rc = wave_enqueue(ctx, srv->runner, order, srv->tuning, true, ctx->stream, &got);
@@ -423,9 +439,7 @@ static int step_batched(rt_server *srv)
         }
         srv->inflight.swap(still);
         note_peak(srv);
-        return RT_OK;
     }
-    if (!srv->resolving.empty()) return retire(srv, true);   // nothing to enqueue: wait for a frame
     return RT_OK;
 }
 

@@ -13,6 +13,7 @@
 // lists; its boxes are padded so that traversal never rejects a triangle the exact test hits.
 #pragma once
 #include "rt_device.cuh"
+#include "rt_lbvh.cuh"
 
 namespace rtg {
 
@@ -132,6 +133,47 @@ __device__ __forceinline__ float slab(const RayInv &r, float4 lo, float4 hi, flo
     return tn;
 }
 
+// ---- 4-wide nodes ----------------------------------------------------------------------------
+struct Quad {
+    float4 lx, hx, ly, hy, lz, hz;
+    int4 ref;
+};
+__device__ __forceinline__ Quad load_quad(const float4 *__restrict__ quads, int node)
+{
+    const float4 *q = quads + 8ll * node;
+    Quad Q;
+    Q.lx = __ldg(q), Q.hx = __ldg(q + 1), Q.ly = __ldg(q + 2), Q.hy = __ldg(q + 3);
+    Q.lz = __ldg(q + 4), Q.hz = __ldg(q + 5);
+    Q.ref = __ldg(reinterpret_cast<const int4 *>(q + 6));
+    return Q;
+}
+__device__ __forceinline__ float slab1(const RayInv &r, float lx, float hx, float ly, float hy, float lz, float hz,
+                                       float tmax, bool &hit)
+{
+    return slab(r, make_float4(lx, ly, lz, 0.0f), make_float4(hx, hy, hz, 0.0f), tmax, hit);
+}
+// the four slots against one ray: entry distance and hit flag per slot
+__device__ __forceinline__ void slab4(const RayInv &r, const Quad &Q, float tmax, float t[4], bool h[4])
+{
+    t[0] = slab1(r, Q.lx.x, Q.hx.x, Q.ly.x, Q.hy.x, Q.lz.x, Q.hz.x, tmax, h[0]);
+    t[1] = slab1(r, Q.lx.y, Q.hx.y, Q.ly.y, Q.hy.y, Q.lz.y, Q.hz.y, tmax, h[1]);
+    t[2] = slab1(r, Q.lx.z, Q.hx.z, Q.ly.z, Q.hy.z, Q.lz.z, Q.hz.z, tmax, h[2]);
+    t[3] = slab1(r, Q.lx.w, Q.hx.w, Q.ly.w, Q.hy.w, Q.lz.w, Q.hz.w, tmax, h[3]);
+}
+// order four (distance, ref) pairs by distance (entries not taken carry +inf): 5 exchanges
+__device__ __forceinline__ void sort4(float t[4], int c[4])
+{
+    auto cx = [&](int a, int b) {
+        const bool sw = t[b] < t[a];
+        const float ta = t[a], tb = t[b];
+        const int ca = c[a], cb = c[b];
+        t[a] = sw ? tb : ta, t[b] = sw ? ta : tb;
+        c[a] = sw ? cb : ca, c[b] = sw ? ca : cb;
+    };
+    cx(0, 1), cx(2, 3), cx(0, 2), cx(1, 3), cx(1, 2);
+}
+constexpr float kInf = __builtin_huge_valf();
+
 struct WorkCount {
     unsigned nodes, tris, spheres;
     int err;   // 1: a child index outside the node array, 2: visit limit reached
@@ -222,7 +264,7 @@ __device__ void closest_hit(const DevScene &S, V3 O, V3 D, int excl, bool inside
         if (S.n_leaves == 1) {
             test_leaf(0);
         } else {
-            const float4 *__restrict__ pairs = S.pairs;
+            const float4 *__restrict__ quads = S.quads;
             const RayInv ri = make_inv(O, D);
             const unsigned last = (unsigned)S.n_leaves - 2u;   // internal nodes 0..L-2
             int stack[STACK];
@@ -230,37 +272,44 @@ __device__ void closest_hit(const DevScene &S, V3 O, V3 D, int excl, bool inside
             int node = 0;
             for (unsigned visits = 0;; ++visits) {
                 if (COUNT) wc.nodes++;
-                const float4 l0 = __ldg(&pairs[4 * node]), h0 = __ldg(&pairs[4 * node + 1]);
-                const float4 l1 = __ldg(&pairs[4 * node + 2]), h1 = __ldg(&pairs[4 * node + 3]);
-                const int c0 = __float_as_int(l0.w), c1 = __float_as_int(l1.w);
-                if (!child_ok(c0, last, S.n_leaves) || !child_ok(c1, last, S.n_leaves) || visits >= kMaxVisits) {
+                if ((unsigned)node > last || visits >= kMaxVisits) {
                     wc.err |= visits >= kMaxVisits ? 2 : 1;
                     break;
                 }
-                const float cull = self_inside ? before.t : best.t;
-                bool hit0, hit1;
-                const float tn0 = slab(ri, l0, h0, cull, hit0);
-                const float tn1 = slab(ri, l1, h1, cull, hit1);
-                if (hit0 && c0 < 0) {
-                    test_leaf(~c0);
-                    hit0 = false;
+                const Quad Q = load_quad(quads, node);
+                float t[4];
+                bool h[4];
+                int c[4] = {Q.ref.x, Q.ref.y, Q.ref.z, Q.ref.w};
+                slab4(ri, Q, self_inside ? before.t : best.t, t, h);
+#pragma unroll
+                for (int k = 0; k < 4; ++k)   // leaves at once (ties resolve by object order, not by visit order)
+                    if (h[k] && c[k] < 0) {
+                        h[k] = false;
+                        if ((unsigned)~c[k] < (unsigned)S.n_leaves) test_leaf(~c[k]);
+                        else wc.err |= 1;
+                    }
+                const float cull = self_inside ? before.t : best.t;   // the leaves may have lowered it
+                int n_in = 0;
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    const bool in = h[k] && t[k] <= cull;
+                    t[k] = in ? t[k] : kInf;
+                    n_in += in;
                 }
-                if (hit1 && c1 < 0) {
-                    test_leaf(~c1);
-                    hit1 = false;
-                }
-                if (hit0 && hit1) {
-                    const int nearc = tn0 <= tn1 ? c0 : c1, farc = tn0 <= tn1 ? c1 : c0;
-                    if (sp < STACK) stack[sp++] = farc;
-                    else wc.err |= 4;
-                    node = nearc;
-                } else if (hit0)
-                    node = c0;
-                else if (hit1)
-                    node = c1;
-                else {
+                if (n_in == 0) {
                     if (sp == 0) break;
                     node = stack[--sp];
+                    continue;
+                }
+                if (n_in == 1) {
+                    node = t[0] < kInf ? c[0] : t[1] < kInf ? c[1] : t[2] < kInf ? c[2] : c[3];
+                    continue;
+                }
+                sort4(t, c);   // nearest next, the others pushed farthest first
+                node = c[0];
+                for (int k = n_in - 1; k >= 1; --k) {
+                    if (sp < STACK) stack[sp++] = c[k];
+                    else wc.err |= 4;
                 }
             }
         }
@@ -302,7 +351,7 @@ __device__ bool any_hit(const DevScene &S, V3 O, V3 D, float dis, int excl, Work
         return sphere_outside(O, D, L.a, t) && t < dis;
     };
     if (S.n_leaves == 1) return test_leaf(0);
-    const float4 *__restrict__ pairs = S.pairs;
+    const float4 *__restrict__ quads = S.quads;
     const RayInv ri = make_inv(O, D);
     const unsigned last = (unsigned)S.n_leaves - 2u;
     int stack[STACK];
@@ -310,37 +359,38 @@ __device__ bool any_hit(const DevScene &S, V3 O, V3 D, float dis, int excl, Work
     int node = 0;
     for (unsigned visits = 0;; ++visits) {
         if (COUNT) wc.nodes++;
-        const float4 l0 = __ldg(&pairs[4 * node]), h0 = __ldg(&pairs[4 * node + 1]);
-        const float4 l1 = __ldg(&pairs[4 * node + 2]), h1 = __ldg(&pairs[4 * node + 3]);
-        const int c0 = __float_as_int(l0.w), c1 = __float_as_int(l1.w);
-        if (!child_ok(c0, last, S.n_leaves) || !child_ok(c1, last, S.n_leaves) || visits >= kMaxVisits) {
+        if ((unsigned)node > last || visits >= kMaxVisits) {
             wc.err |= visits >= kMaxVisits ? 2 : 1;
             return false;
         }
-        bool hit0, hit1;
-        const float tn0 = slab(ri, l0, h0, dis, hit0);
-        const float tn1 = slab(ri, l1, h1, dis, hit1);
-        if (hit0 && c0 < 0) {
-            if (test_leaf(~c0)) return true;
-            hit0 = false;
+        const Quad Q = load_quad(quads, node);
+        float t[4];
+        bool h[4];
+        const int c[4] = {Q.ref.x, Q.ref.y, Q.ref.z, Q.ref.w};
+        slab4(ri, Q, dis, t, h);
+        int next = -1;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {   // any blocker ends the ray, so no ordering is needed
+            if (!h[k]) continue;
+            if (c[k] < 0) {
+                if ((unsigned)~c[k] >= (unsigned)S.n_leaves) {
+                    wc.err |= 1;
+                    return false;
+                }
+                if (test_leaf(~c[k])) return true;
+            } else if (next < 0)
+                next = c[k];
+            else if (sp < STACK)
+                stack[sp++] = c[k];
+            else
+                wc.err |= 4;
         }
-        if (hit1 && c1 < 0) {
-            if (test_leaf(~c1)) return true;
-            hit1 = false;
+        if (next >= 0) {
+            node = next;
+            continue;
         }
-        if (hit0 && hit1) {
-            const int nearc = tn0 <= tn1 ? c0 : c1, farc = tn0 <= tn1 ? c1 : c0;
-            if (sp < STACK) stack[sp++] = farc;
-            else wc.err |= 4;
-            node = nearc;
-        } else if (hit0)
-            node = c0;
-        else if (hit1)
-            node = c1;
-        else {
-            if (sp == 0) return false;
-            node = stack[--sp];
-        }
+        if (sp == 0) return false;
+        node = stack[--sp];
     }
 }
 

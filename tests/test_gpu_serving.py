@@ -63,7 +63,7 @@ def test_batch_jittered_depth4_equals_plain(ctx):
     fids = [ctx.frame(64, 48) for _ in scenes]
     rds = [ctx.render_desc(64, 48, 4, 4, seed=7) for _ in scenes]
     try:
-        ctx.batch(sids, fids, rds, tuning=rt.BatchTuning(64, 64, 64, 0, 8, 1))   # no graph, other tiles
+        ctx.batch(sids, fids, rds, tuning=rt.BatchTuning(64, 64, 0, 0, 8, 1))   # no graph, other tiles
         for sc, fid in zip(scenes, fids):
             got = ctx.download(fid, 64, 48, planes=False)
             ref = plain_render(ctx, sc, 64, 48, spp=4, level=4, seed=7)
