@@ -471,18 +471,20 @@ __global__ void __launch_bounds__(MINB ? 128 : 256, MINB ? MINB : 1) k_shadow(Wa
     for_each_ray<DYN>(n * nl, &C->work[wslot], tile, [&](int w, bool active) {
         if (!active) return;
         const int l = w / n, i = w - l * n;
-        const float4 wc4 = sq.wc[i];
-        const DevJob &J = wf.jobs[__float_as_int(wc4.w)];
-        const DevScene &S = wf.scenes[J.scene];
+        const int job = __float_as_int(sq.wc[i].w);
+        const DevScene &S = wf.scenes[wf.jobs[job].scene];
         if (l >= S.n_lights) return;
         const DevLight &L = S.lights[l];
         if (!L.on) return;
         ++rays;
-        const float4 p4 = sq.p[i], v4 = sq.v[i];
-        const V3 P = mk(p4), D = mk(v4);
+        const V3 P = mk(sq.p[i]);
         const LightTerm lt = light_term(L, P);
-        if (any_hit<STACK, COUNT>(S, P, lt.p2l, lt.dis, __float_as_int(v4.w), wc)) return;
-        const float4 n4 = sq.n[i], ws4 = sq.ws[i];
+        if (any_hit<STACK, COUNT>(S, P, lt.p2l, lt.dis, __float_as_int(sq.v[i].w), wc)) return;
+        // the light is visible: the rest of the hit record comes back from L1/L2 here rather
+        // than sitting in registers across the traversal
+        const DevJob &J = wf.jobs[job];
+        const float4 p4 = sq.p[i], v4 = sq.v[i], n4 = sq.n[i], wc4 = sq.wc[i], ws4 = sq.ws[i];
+        const V3 D = mk(v4);
         const DevMaterial &M = S.mtl[__float_as_int(n4.w)];
         const V3 N = mk(n4), Wc = mk(wc4), Ws = mk(ws4);
         V3 ld = mk(L.dif[0], L.dif[1], L.dif[2]), ls = mk(L.spec[0], L.spec[1], L.spec[2]);

@@ -323,75 +323,101 @@ __device__ void closest_hit(const DevScene &S, V3 O, V3 D, int excl, bool inside
 }
 
 // ---- any hit (shadow rays) ----------------------------------------------------------------
-// true when some primitive other than `excl` is hit at a distance below `dis`
-template <int STACK, bool COUNT>
-__device__ bool any_hit(const DevScene &S, V3 O, V3 D, float dis, int excl, WorkCount &wc)
+// Written as a start and single node visits so a kernel can advance each lane's ray one node at
+// a time and give a finished lane a new ray while the others continue.
+
+// leaf k blocks the segment [0, dis) of the ray (its own primitive `excl` never does)
+template <bool COUNT>
+__device__ __forceinline__ bool leaf_blocks(const float4 *__restrict__ tri, int k, V3 O, V3 D, float dis, int excl,
+                                            WorkCount &wc)
+{
+    const Leaf L = load_leaf(tri, k);
+    const int tag = __float_as_int(L.c.w);
+    float t;
+    if (tag >= 0) {
+        if (COUNT) wc.tris++;
+        if ((k | kTriFlag) == excl) return false;
+        float u, v;
+        return tri_test(O, D, mk(L.a), mk(L.b), mk(L.c), t, u, v) && t < dis;
+    }
+    if (COUNT) wc.spheres++;
+    if (-1 - tag == excl) return false;
+    return sphere_outside(O, D, L.a, t) && t < dis;
+}
+
+// the linear primitives and the trivial trees: 1 blocked, 0 not blocked, -1 traverse from node 0
+template <bool COUNT>
+__device__ __forceinline__ int any_hit_begin(const DevScene &S, V3 O, V3 D, float dis, int excl, WorkCount &wc)
 {
     for (int p = 0; p < S.n_linear; ++p) {
         if (p == excl) continue;   // shadow rays are never inside: the own primitive is skipped
         const DevPrim &P = S.prims[p];
         float t;
         const bool ok = P.type == kPrimPlane ? plane_hit(O, D, P, t) : box_hit(O, D, P, t);
-        if (ok && t < dis) return true;
+        if (ok && t < dis) return 1;
     }
-    if (S.n_leaves == 0) return false;
-    const float4 *__restrict__ tri = S.tri;
-    auto test_leaf = [&](int k) -> bool {
-        const Leaf L = load_leaf(tri, k);
-        const int tag = __float_as_int(L.c.w);
-        float t;
-        if (tag >= 0) {
-            if (COUNT) wc.tris++;
-            if ((k | kTriFlag) == excl) return false;
-            float u, v;
-            return tri_test(O, D, mk(L.a), mk(L.b), mk(L.c), t, u, v) && t < dis;
-        }
-        if (COUNT) wc.spheres++;
-        if (-1 - tag == excl) return false;
-        return sphere_outside(O, D, L.a, t) && t < dis;
-    };
-    if (S.n_leaves == 1) return test_leaf(0);
-    const float4 *__restrict__ quads = S.quads;
-    const RayInv ri = make_inv(O, D);
-    const unsigned last = (unsigned)S.n_leaves - 2u;
-    int stack[STACK];
-    int sp = 0;
-    int node = 0;
-    for (unsigned visits = 0;; ++visits) {
-        if (COUNT) wc.nodes++;
-        if ((unsigned)node > last || visits >= kMaxVisits) {
-            wc.err |= visits >= kMaxVisits ? 2 : 1;
-            return false;
-        }
-        const Quad Q = load_quad(quads, node);
-        float t[4];
-        bool h[4];
-        const int c[4] = {Q.ref.x, Q.ref.y, Q.ref.z, Q.ref.w};
-        slab4(ri, Q, dis, t, h);
-        int next = -1;
+    if (S.n_leaves == 0) return 0;
+    if (S.n_leaves == 1) return leaf_blocks<COUNT>(S.tri, 0, O, D, dis, excl, wc) ? 1 : 0;
+    return -1;
+}
+
+// one 4-wide node visit: 1 blocked, 0 not blocked (the stack ran empty), -1 continue at `node`
+// (the tree is given by its node and leaf arrays and leaf count, held in registers by the caller)
+template <int STACK, bool COUNT>
+__device__ __forceinline__ int any_hit_step(const float4 *__restrict__ quads, const float4 *__restrict__ tri, int n_leaves,
+                                            V3 O, V3 D, const RayInv &ri, float dis, int excl, int &node, int &sp,
+                                            int *stack, unsigned &visits, WorkCount &wc)
+{
+    if (COUNT) wc.nodes++;
+    if ((unsigned)node > (unsigned)n_leaves - 2u || visits++ >= kMaxVisits) {
+        wc.err |= visits > kMaxVisits ? 2 : 1;
+        return 0;
+    }
+    const Quad Q = load_quad(quads, node);
+    float t[4];
+    bool h[4];
+    const int c[4] = {Q.ref.x, Q.ref.y, Q.ref.z, Q.ref.w};
+    slab4(ri, Q, dis, t, h);
+    int next = -1;
 #pragma unroll
-        for (int k = 0; k < 4; ++k) {   // any blocker ends the ray, so no ordering is needed
-            if (!h[k]) continue;
-            if (c[k] < 0) {
-                if ((unsigned)~c[k] >= (unsigned)S.n_leaves) {
-                    wc.err |= 1;
-                    return false;
-                }
-                if (test_leaf(~c[k])) return true;
-            } else if (next < 0)
-                next = c[k];
-            else if (sp < STACK)
-                stack[sp++] = c[k];
-            else
-                wc.err |= 4;
-        }
-        if (next >= 0) {
-            node = next;
-            continue;
-        }
-        if (sp == 0) return false;
-        node = stack[--sp];
+    for (int k = 0; k < 4; ++k) {   // any blocker ends the ray, so no ordering is needed
+        if (!h[k]) continue;
+        if (c[k] < 0) {
+            if ((unsigned)~c[k] >= (unsigned)n_leaves) {
+                wc.err |= 1;
+                return 0;
+            }
+            if (leaf_blocks<COUNT>(tri, ~c[k], O, D, dis, excl, wc)) return 1;
+        } else if (next < 0)
+            next = c[k];
+        else if (sp < STACK)
+            stack[sp++] = c[k];
+        else
+            wc.err |= 4;
     }
+    if (next >= 0) {
+        node = next;
+        return -1;
+    }
+    if (sp == 0) return 0;
+    node = stack[--sp];
+    return -1;
+}
+
+// true when some primitive other than `excl` is hit at a distance below `dis`
+template <int STACK, bool COUNT>
+__device__ bool any_hit(const DevScene &S, V3 O, V3 D, float dis, int excl, WorkCount &wc)
+{
+    int r = any_hit_begin<COUNT>(S, O, D, dis, excl, wc);
+    if (r >= 0) return r == 1;
+    const RayInv ri = make_inv(O, D);
+    int stack[STACK];
+    int node = 0, sp = 0;
+    unsigned visits = 0;
+    while ((r = any_hit_step<STACK, COUNT>(S.quads, S.tri, S.n_leaves, O, D, ri, dis, excl, node, sp, stack, visits,
+                                           wc)) < 0) {
+    }
+    return r == 1;
 }
 
 } // namespace rtg
