@@ -18,7 +18,7 @@ LIB = os.path.join(HERE, "_build", "liboracle.so")
 class Params(C.Structure):
     _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("spp", C.c_int32), ("max_level", C.c_int32),
                 ("ref_tiles", C.c_int32), ("threads", C.c_int32), ("check", C.c_int32), ("seed", C.c_uint64),
-                ("tiles", C.POINTER(C.c_int32)), ("n_tiles", C.c_int32), ("block", C.c_int32)]
+                ("tiles", C.POINTER(C.c_int32)), ("n_tiles", C.c_int32), ("block", C.c_int32), ("mode", C.c_int32)]
 
 
 def _lib() -> C.CDLL:
@@ -55,20 +55,22 @@ def _desc_ptr(scene):
 
 
 def render(scene, width: int, height: int, spp: int = 1, max_level: int = 3, seed: int = 0, ref_tiles: bool = False,
-           threads: int | None = None, check: bool = True, tiles=None, fp64: bool = False, block: int = 8) -> dict:
+           threads: int | None = None, check: bool = True, tiles=None, fp64: bool = False, block: int = 8,
+           mode: int = 0x80) -> dict:
     """Render with the oracle. Returns rgb (float32 or float64), rgb8, obj, prim, t, ambiguous
     (with `reasons` bits: 1 near-tie, 2 winner differs from the exact per-primitive search,
     4 shadow blocker at the light distance, 8 shadow result differs, 16 texel read past the
     texel array, undefined in the reference; bit 16 is set with or without `check`),
     counts (primary, secondary, shadow) and seconds. `tiles` limits the render to those 64x64
     tile indices (row-major over the rendered region). `block` splits tiles into smaller work units
-    for the thread pool (64 keeps the reference's whole-tile units)."""
+    for the thread pool (64 keeps the reference's whole-tile units). `mode` is a RT_MODE_* value
+    (the reference's MY_MODEL_* test modes; ray tracing by default)."""
     L = lib()
     threads = threads or os.cpu_count() or 1
     tl = None if tiles is None else np.ascontiguousarray(tiles, np.int32)
     p = Params(width, height, spp, max_level, int(ref_tiles), threads, int(check and not fp64), seed,
                tl.ctypes.data_as(C.POINTER(C.c_int32)) if tl is not None else None, 0 if tl is None else len(tl),
-               block)
+               block, mode)
     obj = np.full((height, width), -1, np.int32)
     prim = np.zeros((height, width), np.int32)
     t = np.full((height, width), 1e20, np.float32)

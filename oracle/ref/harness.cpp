@@ -211,7 +211,7 @@ template <class T> void dump(const std::string &path, const std::vector<T> &v)
 int main(int argc, char **argv)
 {
     if (argc < 3) {
-        std::fprintf(stderr, "usage: %s scene.rtsc out_prefix [threads] [tiles_file]\n", argv[0]);
+        std::fprintf(stderr, "usage: %s scene.rtsc out_prefix [threads] [tiles_file|-] [mode]\n", argv[0]);
         return 2;
     }
     FileScene fs;
@@ -222,7 +222,9 @@ int main(int argc, char **argv)
     const std::string out = argv[2];
     const int threads = argc > 3 ? std::max(1, std::atoi(argv[3])) : 1;
     std::vector<int> tiles;
-    if (argc > 4) {
+    // render mode: MY_MODEL_* (RayTracer.cpp:629-662), MY_MODEL_RAYTRACE by default
+    const int mode = argc > 5 ? std::atoi(argv[5]) : MY_MODEL_RAYTRACE;
+    if (argc > 4 && std::strcmp(argv[4], "-") != 0) {
         FILE *f = std::fopen(argv[4], "r");
         int t;
         while (f && std::fscanf(f, "%d", &t) == 1) tiles.push_back(t);
@@ -271,7 +273,17 @@ int main(int argc, char **argv)
                         } else
                             dir = cam.n + cam.u * (xcur * dp) + cam.v * (ycur * dp);
                         Ray ray(cam.position, dir, MY_RAY_BASERAY);
-                        Color c = rt.proxyRTfrac(zNear, zFar, ray);
+                        Color c(false);
+                        switch (mode) {   // the worker start() would use for this mode
+                        case MY_MODEL_CHECK: c = Color(((row / 64) & 1) == ((col / 64) & 1)); break;   // RTcheck
+                        case MY_MODEL_DEPTHTEST: c = rt.RTdepth(zNear, zFar, ray); break;
+                        case MY_MODEL_NORMALTEST: c = rt.RTnorm(zNear, zFar, ray); break;
+                        case MY_MODEL_TEXTURETEST: c = rt.RTtex(zNear, zFar, ray); break;
+                        case MY_MODEL_MATERIALTEST: c = rt.RTmtl(zNear, zFar, ray); break;
+                        case MY_MODEL_SHADOWTEST: c = rt.RTshd(zNear, zFar, ray); break;
+                        case MY_MODEL_REFLECTTEST: c = rt.proxyRTflec(zNear, zFar, ray); break;
+                        default: c = rt.proxyRTfrac(zNear, zFar, ray); break;
+                        }
                         acc[0] += c.r, acc[1] += c.g, acc[2] += c.b;
                         if (s == 0) {   // primary closest hit, RTfrac's object loop
                             HitRes hr = rt.tmphr;
@@ -322,9 +334,9 @@ int main(int argc, char **argv)
 
     // the reference's own start(): its uint8 output over the full tile region (1 spp only)
     double start_wall = 0.0, use_time = 0.0;
-    if (fs.spp == 1 && argc <= 4) {
+    if (fs.spp == 1 && (argc <= 4 || std::strcmp(argv[4], "-") == 0)) {
         const auto s0 = std::chrono::steady_clock::now();
-        rt.start(MY_MODEL_RAYTRACE, (int8_t)std::min(threads, 32));
+        rt.start((uint8_t)mode, (int8_t)std::min(threads, 32));
         while (!rt.isFinish) std::this_thread::sleep_for(std::chrono::milliseconds(1));
         start_wall = std::chrono::duration<double>(std::chrono::steady_clock::now() - s0).count();
         use_time = rt.useTime;

@@ -642,6 +642,7 @@ template <class T> struct Tracer {
     const Scene<T> &S;
     int max_level;
     Tls &tls;
+    bool reflect_only = false;   // RTflec (RayTracer.cpp:332-448): RTfrac without the refraction branch
 
     Color<T> rtfrac(T zNear, T zFar, const Ray<T> &ray, int level, T bwc, int64_t base_obj, Hit<T> *primary)
     {
@@ -716,7 +717,7 @@ template <class T> struct Tracer {
             Color<T> cf = rtfrac(T(0), zFar, fr, level + 1, bwc * r, newobj, nullptr);
             c.r += cf.r * r, c.g += cf.g * r, c.b += cf.b * r;
         }
-        if (M.refract > T(0.01f)) {
+        if (!reflect_only && M.refract > T(0.01f)) {
             const T f = M.refract;
             c.r *= (1 - f), c.g *= (1 - f), c.b *= (1 - f);
             T n = ray.mtlrfr / hr.rfr;
@@ -736,6 +737,146 @@ template <class T> struct Tracer {
         }
         c.alpha = hr.dist;
         return c;
+    }
+
+    // ---- the test modes (RayTracer.cpp:81-444) ----------------------------------------------
+    // the first hit over Scene::Objects with a fresh HitRes (its key carried object to object,
+    // as those loops do)
+    Hit<T> first_hit(const Ray<T> &ray, Hit<T> *primary)
+    {
+        ++tls.counts.primary;
+        Hit<T> hr(T(1e20f));
+        for (const Obj<T> &o : S.objs)
+            if (o.show) hr = intersect(S, o, ray, hr, T(0));
+        if (tls.check) check_closest(S, ray, uid_of(S, NO_KEY), hr, tls);
+        if (primary) *primary = hr;
+        return hr;
+    }
+
+    // RTdepth + Color::set (3DElement.cpp:451-462); log of a float is the float overload
+    Color<T> rtdepth(T zNear, T zFar, const Ray<T> &ray, Hit<T> *primary)
+    {
+        const Hit<T> hr = first_hit(ray, primary);
+        const T d = hr.dist;
+        if (d <= zNear) return Color<T>{1, 0, 0, 0};
+        if (d >= zFar) return Color<T>{0, 0, 0, 0};
+        const T after = std::log(d), mx = std::log(zFar);
+        const T g = (mx - after) / mx;
+        return Color<T>{g, g, g, 0};
+    }
+
+    // RTnorm + Color(const Normal&): 0.5 * (n + 1) in double, stored as float
+    Color<T> rtnorm(T zNear, T zFar, const Ray<T> &ray, Hit<T> *primary)
+    {
+        const Hit<T> hr = first_hit(ray, primary);
+        if (hr.dist > zFar) return Color<T>{0, 0, 0, 0};
+        if (hr.dist < zNear) return Color<T>{1, 1, 1, 0};
+        return Color<T>{(T)(0.5 * ((double)hr.n.x + 1)), (T)(0.5 * ((double)hr.n.y + 1)), (T)(0.5 * ((double)hr.n.z + 1)), 0};
+    }
+
+    // RTtex
+    Color<T> rttex(T zNear, T zFar, const Ray<T> &ray, Hit<T> *primary)
+    {
+        const Hit<T> hr = first_hit(ray, primary);
+        if (hr.dist > zFar) return Color<T>{0, 0, 0, 0};
+        if (hr.dist < zNear) return Color<T>{1, 1, 1, 0};
+        if (hr.tex >= 0) return tex_color(S, hr.tex, hr.tu, hr.tv, tls.ambiguous);
+        return Color<T>{T(0.588f), T(0.588f), T(0.588f), 0};
+    }
+
+    // RTmtl: local terms of every light, no shadow test; point light when position.w != 0
+    Color<T> rtmtl(T zNear, T zFar, const Ray<T> &ray, Hit<T> *primary)
+    {
+        const Hit<T> hr = first_hit(ray, primary);
+        if (hr.dist > zFar) return Color<T>{0, 0, 0, 0};
+        if (hr.dist < zNear) return Color<T>{1, 1, 1, 0};
+        const Mtl<T> &M = S.mtls[hr.mtl];
+        const Color<T> vc = tex_color(S, hr.tex, hr.tu, hr.tv, tls.ambiguous);
+        V3<T> mix_vd = mk(T(0), T(0), T(0)), mix_va = mix_vd, mix_vsc = mix_vd;
+        for (const Lit<T> &L : S.lights) {
+            if (!L.on) continue;
+            T lum;
+            V3<T> p2l;
+            if (L.type != RT_LIGHT_PARALLEL) {   // position.alpha 1 for point and spot lights
+                V3<T> p2l_v = sub(L.pos, hr.pos);
+                T dis = dot(p2l_v, p2l_v);
+                T step = L.att.x + L.att.y * std::sqrt(dis) + L.att.z * dis;
+                lum = T(1) / step;
+                p2l = nrm(p2l_v);
+            } else {
+                lum = T(1);
+                p2l = nrm(L.pos);
+            }
+            const V3<T> la = scl(L.amb, lum), ld = scl(L.dif, lum), ls = scl(L.spec, lum);
+            mix_va = add(mix_va, mul(M.ka, la));
+            T nn = dot(hr.n, p2l);
+            if (nn > 0) mix_vd = add(mix_vd, scl(mul(M.kd, ld), nn));
+            V3<T> h = nrm(sub(p2l, ray.d));
+            nn = dot(hr.n, h);
+            if (nn > 0) {
+                V3<T> vs = scl(mul(M.ks, ls), (T)std::pow(nn, M.shininess));
+                mix_vsc = add(mix_vsc, mk(T(1) * vs.x, T(1) * vs.y, T(1) * vs.z));
+            }
+        }
+        mix_va = add(mix_va, mul(M.ka, S.env));
+        const V3<T> sm = add(mix_vd, mix_va);
+        return Color<T>{vc.r * sm.x + mix_vsc.x, vc.g * sm.y + mix_vsc.y, vc.b * sm.z + mix_vsc.z, 0};
+    }
+
+    // RTshd: one bounce with shadow rays (the hit excludes itself), environment ambient last
+    Color<T> rtshd(T zNear, T zFar, const Ray<T> &ray, Hit<T> *primary)
+    {
+        const Hit<T> hr = first_hit(ray, primary);
+        if (hr.dist > zFar) return Color<T>{0, 0, 0, 0};
+        if (hr.dist < zNear) return Color<T>{1, 1, 1, 0};
+        const Mtl<T> &M = S.mtls[hr.mtl];
+        const Color<T> vc = tex_color(S, hr.tex, hr.tu, hr.tv, tls.ambiguous);
+        V3<T> mix_vd = mk(T(0), T(0), T(0)), mix_va = mix_vd, mix_vsc = mix_vd;
+        for (const Lit<T> &L : S.lights) {
+            if (!L.on) continue;
+            T lum, dis;
+            V3<T> p2l;
+            if (L.type == RT_LIGHT_POINT) {
+                V3<T> p2l_v = sub(L.pos, hr.pos);
+                dis = dot(p2l_v, p2l_v);
+                T step = L.att.x + L.att.z * dis;
+                dis = std::sqrt(dis);
+                step += L.att.y * dis;
+                lum = T(1) / step;
+                p2l = nrm(p2l_v);
+            } else {
+                dis = T(1e10f);
+                lum = T(1);
+                p2l = nrm(L.pos);
+            }
+            const V3<T> la = scl(L.amb, lum), ld = scl(L.dif, lum), ls = scl(L.spec, lum);
+            mix_va = add(mix_va, mul(M.ka, la));
+            Ray<T> sr{hr.pos, p2l, T(1), RAY_SHADOW, 0};
+            Hit<T> shr(dis);
+            shr.obj = hr.obj;
+            ++tls.counts.shadow;
+            bool blocked = false;
+            for (const Obj<T> &o : S.objs) {
+                if (o.show) shr = intersect(S, o, sr, shr, dis);
+                if (shr.dist < dis) {
+                    blocked = true;
+                    break;
+                }
+            }
+            if (tls.check) check_shadow(S, sr, uid_of(S, hr.obj), dis, blocked, tls);
+            if (blocked) continue;
+            T nn = dot(hr.n, p2l);
+            if (nn > 0) mix_vd = add(mix_vd, scl(mul(M.kd, ld), nn));
+            V3<T> h = nrm(sub(p2l, ray.d));
+            nn = dot(hr.n, h);
+            if (nn > 0) {
+                V3<T> vs = scl(mul(M.ks, ls), (T)std::pow(nn, M.shininess));
+                mix_vsc = add(mix_vsc, mk(T(1) * vs.x, T(1) * vs.y, T(1) * vs.z));
+            }
+        }
+        mix_va = add(mix_va, mul(M.ka, S.env));
+        const V3<T> sm = add(mix_vd, mix_va);
+        return Color<T>{vc.r * sm.x + mix_vsc.x, vc.g * sm.y + mix_vsc.y, vc.b * sm.z + mix_vsc.z, 0};
     }
 };
 
@@ -766,6 +907,7 @@ struct Params {
     const int32_t *tiles;   // 64x64 tile indices to render (NULL = all)
     int32_t n_tiles;
     int32_t block;          // work-unit edge inside a tile for the thread pool (64 = whole tile)
+    int32_t mode;           // RT_MODE_* (0 = RT_MODE_RAYTRACE)
 };
 
 template <class T>
@@ -798,7 +940,9 @@ int render(const rt_scene_desc *d, const Params &p, T *rgb, uint8_t *rgb8, int32
     auto worker = [&](int tid) {
         Tls tls;
         tls.check = p.check;
+        const int mode = p.mode ? p.mode : RT_MODE_RAYTRACE;
         Tracer<T> tr{S, p.max_level, tls};
+        tr.reflect_only = mode == RT_MODE_REFLECT;
         while (true) {
             const int64_t k = next.fetch_add(1);
             if (k >= (int64_t)tiles.size() * per_tile) break;
@@ -826,7 +970,23 @@ int render(const rt_scene_desc *d, const Params &p, T *rgb, uint8_t *rgb8, int32
                         V3<T> dir = nrm(add(add(cn, scl(cu, a)), scl(cv, b)));
                         Ray<T> ray{cp, dir, T(1), RAY_BASE, 0};
                         Hit<T> prim;
-                        Color<T> c = tr.rtfrac(zNear, sizeof(T) == 4 ? (T)zFar32 : zFar, ray, 0, T(1), NO_KEY, s == 0 ? &prim : nullptr);
+                        const T zf = sizeof(T) == 4 ? (T)zFar32 : zFar;
+                        Hit<T> *pp = s == 0 ? &prim : nullptr;
+                        Color<T> c;
+                        switch (mode) {
+                        case RT_MODE_CHECK: {   // RTcheck: white where the tile row and column parities agree
+                            const T wv = ((row >> 6) & 1) == ((col >> 6) & 1) ? T(1) : T(0);
+                            c = Color<T>{wv, wv, wv, 0};
+                            prim = tr.first_hit(ray, nullptr);
+                            break;
+                        }
+                        case RT_MODE_DEPTH: c = tr.rtdepth(zNear, zf, ray, pp); break;
+                        case RT_MODE_NORMAL: c = tr.rtnorm(zNear, zf, ray, pp); break;
+                        case RT_MODE_TEXTURE: c = tr.rttex(zNear, zf, ray, pp); break;
+                        case RT_MODE_MATERIAL: c = tr.rtmtl(zNear, zf, ray, pp); break;
+                        case RT_MODE_SHADOW: c = tr.rtshd(zNear, zf, ray, pp); break;
+                        default: c = tr.rtfrac(zNear, zf, ray, 0, T(1), NO_KEY, pp); break;
+                        }
                         acc[0] += c.r, acc[1] += c.g, acc[2] += c.b;
                         if (s == 0) {
                             const bool hit = prim.dist < T(1e20f) && prim.obj_index >= 0;
@@ -880,6 +1040,7 @@ typedef struct orc_params {
     const int32_t *tiles;
     int32_t n_tiles;
     int32_t block;
+    int32_t mode;
 } orc_params;
 
 int orc_render_f32(const rt_scene_desc *d, const orc_params *p, float *rgb, uint8_t *rgb8, int32_t *obj, int32_t *prim,
@@ -887,7 +1048,7 @@ int orc_render_f32(const rt_scene_desc *d, const orc_params *p, float *rgb, uint
 {
     if (!d || !p) return -1;
     Params q{p->width, p->height, p->spp, p->max_level, p->ref_tiles, p->threads, p->check, p->seed, p->tiles, p->n_tiles,
-             p->block};
+             p->block, p->mode};
     return render<float>(d, q, rgb, rgb8, obj, prim, t, amb, counts, seconds);
 }
 
@@ -896,7 +1057,7 @@ int orc_render_f64(const rt_scene_desc *d, const orc_params *p, double *rgb, int
 {
     if (!d || !p) return -1;
     Params q{p->width, p->height, p->spp, p->max_level, p->ref_tiles, p->threads, 0, p->seed, p->tiles, p->n_tiles,
-             p->block};
+             p->block, p->mode};
     return render<double>(d, q, rgb, nullptr, obj, prim, t, nullptr, counts, seconds);
 }
 

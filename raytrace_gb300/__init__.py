@@ -175,6 +175,7 @@ _SIGS = {
     "rt_scenegen": (C.c_int, [C.c_int32, C.c_int32, C.POINTER(P)]),
     "rt_scenegen_small": (C.c_int, [C.c_uint64, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.POINTER(P)]),
     "rt_scenegen_extras": (C.c_int, [C.c_uint64, C.c_int32, C.c_int32, C.POINTER(P)]),
+    "rt_scenegen_textured": (C.c_int, [C.c_uint64, C.c_int32, C.c_int32, C.POINTER(P)]),
     "rt_scene_host_from_desc": (C.c_int, [C.POINTER(SceneDesc), C.c_int32, C.c_int32, C.c_uint64, C.POINTER(P)]),
     "rt_scene_host_desc": (C.POINTER(SceneDesc), [P]),
     "rt_scene_host_render_params": (C.c_int, [P, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_uint64)]),
@@ -239,6 +240,15 @@ class SceneHost:
         rc = lib.rt_scenegen_extras(seed, width, height, C.byref(h))
         if rc:
             raise RTError(rc, "rt_scenegen_extras")
+        return cls(h)
+
+    @classmethod
+    def textured(cls, seed: int, width: int = 128, height: int = 64) -> "SceneHost":
+        """Checker-textured plane, a textured icosphere (spherical uvs, procedural map), spheres, a cube."""
+        h = P()
+        rc = lib.rt_scenegen_textured(seed, width, height, C.byref(h))
+        if rc:
+            raise RTError(rc, "rt_scenegen_textured")
         return cls(h)
 
     @classmethod

@@ -38,7 +38,9 @@ void RayTracer::start(const uint8_t type, const int8_t)
     width = scene->cam.width;
     height = scene->cam.height;
     std::memset(output, 127, kOutputBytes);
-    const int mode = (type == MY_MODEL_RAYTRACE || type == MY_MODEL_REFRACTTEST) ? RT_MODE_RAYTRACE : -1;
+    // every mode of the reference's start() (RayTracer.cpp:629-662): the MY_MODEL_* values are
+    // the RT_MODE_* values of the C ABI
+    const int mode = ((type >= MY_MODEL_CHECK && type <= MY_MODEL_REFRACTTEST) || type == MY_MODEL_RAYTRACE) ? type : -1;
     if (!ctx || mode < 0 || width <= 0 || height <= 0 || width > 2048 || height > 2048) {
         status_ = !ctx ? RT_ERR_CUDA : RT_ERR_INVALID;
         error_ = !ctx ? "no usable CUDA device for the renderer"

@@ -396,6 +396,49 @@ extern "C" int rt_scenegen_extras(uint64_t seed, int32_t width, int32_t height, 
     return RT_OK;
 }
 
+// textured meshes: the plane with its default checker texture, a displaced icosphere with
+// spherical texture coordinates and a 64x32 procedural texture (map_Kd of its material), 6
+// spheres (some refractive), a cube, two point lights
+extern "C" int rt_scenegen_textured(uint64_t seed, int32_t width, int32_t height, rt_scene_host **out)
+{
+    if (!out || width <= 0 || height <= 0) return RT_ERR_INVALID;
+    Scene sc;
+    Rng r(seed);
+    sc.AddPlane();
+    const Vertex centre(0.0f, 1.4f, 0.5f);
+    std::vector<Triangle> tris = make_icosphere(12, centre, 1.3f, 0.15f, (uint32_t)seed);
+    const double pi = 3.14159265358979323846;
+    for (Triangle &t : tris)
+        for (int k = 0; k < 3; ++k) {
+            const Vertex d = t.points[k] - centre;
+            const double len = std::sqrt((double)d.x * d.x + (double)d.y * d.y + (double)d.z * d.z);
+            t.tcoords[k] = Coord2D((float)(0.5 + std::atan2((double)d.z, (double)d.x) / (2 * pi)),
+                                   (float)(0.5 + std::asin(std::max(-1.0, std::min(1.0, d.y / len))) / pi));
+        }
+    Material m = law_material(r);
+    Model *model = new Model();
+    model->setMesh(tris, m);
+    std::vector<uint8_t> img(64 * 32 * 3);
+    for (int y = 0; y < 32; ++y)
+        for (int x = 0; x < 64; ++x) {
+            uint8_t *px = &img[(size_t)(y * 64 + x) * 3];   // B, G, R
+            px[0] = (uint8_t)(x * 4);
+            px[1] = (uint8_t)(y * 8);
+            px[2] = ((x / 8 + y / 8) & 1) ? 230 : 40;
+        }
+    model->texs.push_back(Texture("procedural", 64, 32, img.data()));
+    model->mtl_tex[0] = 0;
+    sc.AddObject(model);
+    add_spheres(sc, r, 6, kSphereBox0, 3, nullptr);
+    uint8_t c = sc.AddCube(0.8f);
+    sc.MovePos(MY_MODEL_OBJECT, c, Vertex(-2.5f, 0.4f, 1.5f));
+    add_point_lights(sc, r, 2, kLightBox0);
+    sc.EnvLight = Vertex(0.1f, 0.1f, 0.1f, 1.0f);
+    set_camera(sc, Vertex(0, 2.5f, -8), Vertex(0, 1.0f, 0), width, height, 60.0f);
+    *out = finish(sc, 1, 3, seed);
+    return RT_OK;
+}
+
 // deep copy of a caller's scene description
 extern "C" int rt_scene_host_from_desc(const rt_scene_desc *d, int32_t spp, int32_t max_level, uint64_t seed,
                                        rt_scene_host **out)

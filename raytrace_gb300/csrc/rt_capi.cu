@@ -685,14 +685,17 @@ int make_job(rt_ctx *ctx, const SceneDev &sc, FrameDev &f, const rt_render_desc 
     if (W != f.w || H != f.h) return ctx_fail(ctx, RT_ERR_INVALID, "frame is %dx%d but the render is %dx%d", f.w, f.h, W, H);
     if (rd->spp < 1 || rd->spp > 1024) return ctx_fail(ctx, RT_ERR_INVALID, "spp %d outside [1,1024]", rd->spp);
     if (rd->max_level < 0 || rd->max_level > 4) return ctx_fail(ctx, RT_ERR_INVALID, "max_level %d outside [0,4]", rd->max_level);
-    if (rd->mode != RT_MODE_RAYTRACE && rd->mode != RT_MODE_REFRACT)
+    const int mode = rd->mode;
+    if (!(mode >= RT_MODE_CHECK && mode <= RT_MODE_REFRACT) && mode != RT_MODE_RAYTRACE)
         return ctx_fail(ctx, RT_ERR_INVALID, "render mode 0x%x is not supported", rd->mode);
     if (!(cam.fovy > 0 && cam.fovy < 180) || !finite3(cam.position) || !finite3(cam.n))
         return ctx_fail(ctx, RT_ERR_INVALID, "camera is not valid");
     J = DevJob{};
     J.scene = scene_slot;
     J.width = W, J.height = H, J.spp = rd->spp;
-    J.max_level = rd->max_level, J.flags = rd->flags, J.mode = rd->mode;
+    // the test modes but reflect and refract look at the first hit only (RayTracer.cpp:81-320)
+    const bool recursive = mode == RT_MODE_RAYTRACE || mode == RT_MODE_REFRACT || mode == RT_MODE_REFLECT;
+    J.max_level = recursive ? rd->max_level : 0, J.flags = rd->flags, J.mode = mode;
     J.xlim = (rd->flags & RT_FLAG_REF_TILES) ? (W / 64) * 64 : W;
     J.ylim = (rd->flags & RT_FLAG_REF_TILES) ? (H / 64) * 64 : H;
     J.acc = f.fb.acc;

@@ -22,6 +22,9 @@ constexpr int kMaxLights = 8;                // Scene::AddLight limit
 
 // ray type codes (MY_RAY_*)
 constexpr int kRayBase = 1, kRayShadow = 2, kRayReflect = 3, kRayRefract = 4;
+// render modes (RT_MODE_*, the reference's MY_MODEL_* test modes, RayTracer.cpp:631-662)
+constexpr int kModeCheck = 0x1, kModeDepth = 0x2, kModeNormal = 0x3, kModeTexture = 0x4, kModeMaterial = 0x5,
+              kModeShadow = 0x6, kModeReflect = 0x7, kModeRefract = 0x8, kModeRaytrace = 0x80;
 // analytic primitive types (MY_OBJECT_* for the shapes that are intersected analytically)
 constexpr int kPrimSphere = 1, kPrimBox = 2, kPrimPlane = 4;
 

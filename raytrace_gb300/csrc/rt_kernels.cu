@@ -154,6 +154,8 @@ __global__ void k_raygen(Wavefront wf)
         V3 v = mk(J.cam_v[0], J.cam_v[1], J.cam_v[2]);
         V3 dir = normalise(vadd(vadd(n, vscale(u, a)), vscale(v, b)));
         int pixel = row * J.width + col;
+        if (J.mode == kModeCheck && ((row >> 6) & 1) == ((col >> 6) & 1))   // RTcheck: white 64x64 tiles
+            acc_add(J.acc, pixel, mk(1.0f, 1.0f, 1.0f));
         q.o[g] = make_float4(J.cam_pos[0], J.cam_pos[1], J.cam_pos[2], 1.0f);
         q.d[g] = make_float4(dir.x, dir.y, dir.z, 1.0f);
         q.w[g] = make_float4(1.0f, 1.0f, 1.0f, __int_as_float(pixel));
@@ -244,6 +246,52 @@ __device__ __forceinline__ LightTerm light_term(const DevLight &L, V3 P)
     return r;
 }
 
+// ---- first-hit test modes (RayTracer.cpp:81-220) -----------------------------------------
+// RTdepth: Color::set(distance, zNear, zFar) (3DElement.cpp:451-462): red up to zNear, black
+// from zFar, else (log zFar - log t) / log zFar
+__device__ __forceinline__ V3 mode_depth(float t, float znear, float zfar)
+{
+    if (t <= znear) return mk(1.0f, 0.0f, 0.0f);
+    if (t >= zfar) return mk(0.0f, 0.0f, 0.0f);
+    const float after = logf(t), mx = logf(zfar);
+    const float g = __fdiv_rn(__fsub_rn(mx, after), mx);
+    return mk(g, g, g);
+}
+
+// RTmtl: the local Blinn-Phong terms of every switched-on light with no shadow test. A light
+// counts as a point light when its position's w is non-zero (point and spot lights,
+// 3DElement.cpp:513-525); attenuation x + y*sqrt(d2) + z*d2 in that order; the environment
+// ambient comes last.
+__device__ V3 mode_material(const DevScene &S, const DevMaterial &M, V3 P, V3 N, V3 D, V3 vc)
+{
+    const V3 ka = mk(M.ka[0], M.ka[1], M.ka[2]), kd = mk(M.kd[0], M.kd[1], M.kd[2]), ks = mk(M.ks[0], M.ks[1], M.ks[2]);
+    V3 mix_vd = mk(0.0f, 0.0f, 0.0f), mix_va = mix_vd, mix_vsc = mix_vd;
+    for (int l = 0; l < S.n_lights; ++l) {
+        const DevLight &L = S.lights[l];
+        if (!L.on) continue;
+        float lum = 1.0f;
+        V3 p2l;
+        if (L.type != 1) {
+            const V3 p2l_v = vsub(mk(L.pos[0], L.pos[1], L.pos[2]), P);
+            const float d2 = dot3(p2l_v, p2l_v);
+            const float step = __fadd_rn(__fadd_rn(L.att[0], __fmul_rn(L.att[1], __fsqrt_rn(d2))), __fmul_rn(L.att[2], d2));
+            lum = __fdiv_rn(1.0f, step);
+            p2l = normalise(p2l_v);
+        } else
+            p2l = normalise(mk(L.pos[0], L.pos[1], L.pos[2]));
+        const V3 la = vscale(mk(L.amb[0], L.amb[1], L.amb[2]), lum), ld = vscale(mk(L.dif[0], L.dif[1], L.dif[2]), lum),
+                 ls = vscale(mk(L.spec[0], L.spec[1], L.spec[2]), lum);
+        mix_va = vadd(mix_va, vmul(ka, la));
+        float nn = dot3(N, p2l);
+        if (nn > 0) mix_vd = vadd(mix_vd, vscale(vmul(kd, ld), nn));
+        const V3 h = normalise(vsub(p2l, D));
+        nn = dot3(N, h);
+        if (nn > 0) mix_vsc = vadd(mix_vsc, vscale(vmul(ks, ls), powf(nn, M.shininess)));
+    }
+    mix_va = vadd(mix_va, vmul(ka, mk(S.env[0], S.env[1], S.env[2])));
+    return vadd(vmul(vc, vadd(mix_vd, mix_va)), mix_vsc);
+}
+
 // ---- shade ------------------------------------------------------------------------------------
 template <bool DYN>
 __global__ void __launch_bounds__(256) k_shade(Wavefront wf, int sel, int wslot, int tile)
@@ -288,7 +336,16 @@ __global__ void __launch_bounds__(256) k_shade(Wavefront wf, int sel, int wslot,
                 J.plane_t[pix] = key >= 0 ? t : kMiss;
             }
             const float znear = level == 0 ? J.znear : 0.0f;
-            if (key >= 0 && !(t > J.zfar || t < znear)) {
+            const int mode = J.mode;
+            const bool far = t > J.zfar, near = t < znear;
+            // the trace modes cut both ends to black; the first-hit test modes (normal, texture,
+            // material, shadow) give white before zNear; depth maps the distance itself
+            const bool traced = mode == kModeRaytrace || mode == kModeRefract || mode == kModeReflect;
+            if (key >= 0 && mode == kModeDepth) {
+                acc_add(J.acc, pix, vmul(mk(w4), mode_depth(t, J.znear, J.zfar)));
+            } else if (key >= 0 && mode != kModeCheck && !far && near && !traced) {
+                acc_add(J.acc, pix, mk(w4));   // Color(true)
+            } else if (key >= 0 && mode != kModeCheck && !far && !near) {
                 const V3 O = mk(o4), D = mk(d4);
                 const V3 P = vadd(O, vscale(D, t));
                 int mtl_id, tex = -1, hit_inside = 0;
@@ -344,19 +401,35 @@ __global__ void __launch_bounds__(256) k_shade(Wavefront wf, int sel, int wslot,
                 const DevMaterial &M = S.mtl[mtl_id];
                 const V3 vc = tex >= 0 ? tex_color(S, tex, tu, tv) : mk(1.0f, 1.0f, 1.0f);
                 V3 W = mk(w4);
+                if (mode == kModeNormal || mode == kModeTexture || mode == kModeMaterial) {
+                    V3 c;
+                    if (mode == kModeNormal)   // Color(Normal): 0.5 * (n + 1), exact in one rounding
+                        c = mk(__fadd_rn(__fmul_rn(0.5f, N.x), 0.5f), __fadd_rn(__fmul_rn(0.5f, N.y), 0.5f),
+                               __fadd_rn(__fmul_rn(0.5f, N.z), 0.5f));
+                    else if (mode == kModeTexture)
+                        c = tex >= 0 ? vc : mk(0.588f, 0.588f, 0.588f);
+                    else
+                        c = mode_material(S, M, P, N, D, vc);
+                    acc_add(J.acc, pix, vmul(W, c));
+                } else {
                 if (m4.z >= 0) {   // Beer factor of a refracted parent that entered a sphere
                     const DevMaterial &B = S.mtl[m4.z];
                     W.x = __fmul_rn(W.x, expf(__fmul_rn(__fmul_rn(B.kd[0], 0.15f), -t)));
                     W.y = __fmul_rn(W.y, expf(__fmul_rn(__fmul_rn(B.kd[1], 0.15f), -t)));
                     W.z = __fmul_rn(W.z, expf(__fmul_rn(__fmul_rn(B.kd[2], 0.15f), -t)));
                 }
-                const bool refl = M.reflect > 0.01f, refr = M.refract > 0.01f;
+                // shadow mode (RTshd) is one bounce with unit weights; reflect mode (RTflec) has no
+                // refraction
+                const bool refl = M.reflect > 0.01f && mode != kModeShadow;
+                const bool refr = M.refract > 0.01f && (mode == kModeRaytrace || mode == kModeRefract);
                 const float a1 = refl ? __fsub_rn(1.0f, M.reflect) : 1.0f;
                 const float a2 = refr ? __fsub_rn(1.0f, M.refract) : 1.0f;
                 const V3 Wl = vscale(W, __fmul_rn(a1, a2));
-                // ambient: environment plus every switched-on light, shadowed or not
+                // ambient: environment plus every switched-on light, shadowed or not (RTshd adds
+                // the environment last, RTfrac and RTflec first)
                 const V3 ka = mk(M.ka[0], M.ka[1], M.ka[2]);
-                V3 mix_va = vmul(ka, mk(S.env[0], S.env[1], S.env[2]));
+                const V3 env = vmul(ka, mk(S.env[0], S.env[1], S.env[2]));
+                V3 mix_va = mode == kModeShadow ? mk(0.0f, 0.0f, 0.0f) : env;
                 int lights_on = 0;
                 for (int l = 0; l < S.n_lights; ++l) {
                     const DevLight &L = S.lights[l];
@@ -367,6 +440,7 @@ __global__ void __launch_bounds__(256) k_shade(Wavefront wf, int sel, int wslot,
                     const V3 la = L.type == 2 ? vscale(mk(L.amb[0], L.amb[1], L.amb[2]), lum) : mk(L.amb[0], L.amb[1], L.amb[2]);
                     mix_va = vadd(mix_va, vmul(ka, la));
                 }
+                if (mode == kModeShadow) mix_va = vadd(mix_va, env);
                 const V3 Wc = vmul(Wl, vc);
                 acc_add(J.acc, pix, vmul(Wc, mix_va));
                 if (lights_on > 0) {
@@ -410,6 +484,7 @@ __global__ void __launch_bounds__(256) k_shade(Wavefront wf, int sel, int wslot,
                                                 m4.w);
                         ++nchild;
                     }
+                }
                 }
             }
         }

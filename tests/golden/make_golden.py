@@ -32,7 +32,8 @@ from oracle import port  # noqa: E402
 HERE = os.path.dirname(os.path.abspath(__file__))
 HARNESS = os.path.join(ROOT, "oracle", "_ref", "rt_ref_harness")
 
-# name: (generator, args, width, height, spp, max_level, seed)
+# name: (generator, args, width, height, spp, max_level, seed[, mode]); mode is RT_MODE_* /
+# MY_MODEL_* (ray tracing when absent)
 CASES = {
     "cfg0_128x64": ("config", (0,), 128, 64, 1, 3, 0),
     "ico8_refr_128x64": ("small", (5, 8, 8, 128, 64, 3), 128, 64, 1, 3, 5),
@@ -41,12 +42,23 @@ CASES = {
     "jitter4_64x64": ("small", (9, 10, 4, 64, 64, 2), 64, 64, 4, 4, 2),
     "cfg1_128x64": ("config", (1,), 128, 64, 1, 3, 1),
     "cfg2_64x64": ("config", (2,), 64, 64, 4, 4, 2),
+    "extras_check_128x64": ("extras", (3, 128, 64), 128, 64, 1, 3, 3, 0x1),
+    "extras_depth_128x64": ("extras", (3, 128, 64), 128, 64, 1, 3, 3, 0x2),
+    "extras_normal_128x64": ("extras", (3, 128, 64), 128, 64, 1, 3, 3, 0x3),
+    "extras_texture_128x64": ("extras", (3, 128, 64), 128, 64, 1, 3, 3, 0x4),
+    "extras_material_128x64": ("extras", (3, 128, 64), 128, 64, 1, 3, 3, 0x5),
+    "extras_shadow_128x64": ("extras", (3, 128, 64), 128, 64, 1, 3, 3, 0x6),
+    "extras_reflect_128x64": ("extras", (3, 128, 64), 128, 64, 1, 3, 3, 0x7),
+    "textured_128x64": ("textured", (6, 128, 64), 128, 64, 1, 3, 6),
+    "textured_texture_128x64": ("textured", (6, 128, 64), 128, 64, 1, 3, 6, 0x4),
+    "textured_material_128x64": ("textured", (6, 128, 64), 128, 64, 1, 3, 6, 0x5),
 }
 EMBED_LIMIT = 256 * 1024
 
 
 def make_scene(gen: str, args: tuple, w: int, h: int, spp: int, lvl: int, seed: int) -> rt.SceneHost:
-    base = {"config": rt.SceneHost.config, "small": rt.SceneHost.small, "extras": rt.SceneHost.extras}[gen](*args)
+    base = {"config": rt.SceneHost.config, "small": rt.SceneHost.small, "extras": rt.SceneHost.extras,
+            "textured": rt.SceneHost.textured}[gen](*args)
     return base.with_camera(w, h, spp, lvl, seed)
 
 
@@ -58,14 +70,15 @@ def scene_bytes(s: rt.SceneHost) -> bytes:
 
 
 def run_case(name: str, spec) -> None:
-    gen, args, w, h, spp, lvl, seed = spec
+    gen, args, w, h, spp, lvl, seed = spec[:7]
+    mode = spec[7] if len(spec) > 7 else 0x80
     scene = make_scene(gen, args, w, h, spp, lvl, seed)
     data = scene_bytes(scene)
     with tempfile.TemporaryDirectory() as d:
         sp = os.path.join(d, "scene.rtsc")
         open(sp, "wb").write(data)
-        r = subprocess.run([HARNESS, sp, os.path.join(d, "out"), str(os.cpu_count() or 1)], capture_output=True,
-                           text=True, check=True)
+        r = subprocess.run([HARNESS, sp, os.path.join(d, "out"), str(os.cpu_count() or 1), "-", str(mode)],
+                           capture_output=True, text=True, check=True)
         info = json.loads(r.stdout)
 
         def ld(ext, dt, shp):
@@ -76,9 +89,9 @@ def run_case(name: str, spec) -> None:
                "t": ld("t.f32", np.float32, (h, w))}
         if os.path.exists(os.path.join(d, "out.start.rgb8")):
             out["start_rgb8"] = ld("start.rgb8", np.uint8, (h, w, 3))
-    chk = port.render(scene, w, h, spp, lvl, seed, ref_tiles=True, check=True)
+    chk = port.render(scene, w, h, spp, lvl, seed, ref_tiles=True, check=True, mode=mode)
     meta = {"generator": gen, "args": list(args), "width": w, "height": h, "spp": spp, "max_level": lvl,
-            "seed": seed, "scene_sha256": hashlib.sha256(data).hexdigest(), "harness": info}
+            "seed": seed, "mode": mode, "scene_sha256": hashlib.sha256(data).hexdigest(), "harness": info}
     extra = {"scene": np.frombuffer(data, np.uint8)} if len(data) <= EMBED_LIMIT else {}
     np.savez_compressed(os.path.join(HERE, name + ".npz"), meta=np.array(json.dumps(meta)),
                         ambiguous=chk["ambiguous"], reasons=chk["reasons"], **out, **extra)

@@ -16,11 +16,11 @@ pytestmark = pytest.mark.gpu
 TOL = 1e-4
 
 
-def gpu_render(ctx, scene, w, h, spp, lvl, seed, ref_tiles=True):
+def gpu_render(ctx, scene, w, h, spp, lvl, seed, ref_tiles=True, mode=rt.RT_MODE_RAYTRACE):
     sid = ctx.upload(scene)
     fid = ctx.frame(w, h)
     flags = rt.RT_FLAG_HIT_PLANES | (rt.RT_FLAG_REF_TILES if ref_tiles else 0)
-    st = ctx.render(sid, fid, ctx.render_desc(w, h, spp, lvl, flags=flags, seed=seed))
+    st = ctx.render(sid, fid, ctx.render_desc(w, h, spp, lvl, mode=mode, flags=flags, seed=seed))
     out = ctx.download(fid, w, h)
     ctx.release_frame(fid)
     ctx.release_scene(sid)
@@ -54,7 +54,8 @@ def check_parity(out, ref, amb, h, w, max_rgb8_lsb=1):
 def test_gpu_matches_reference_fixture(ctx, name):
     g, meta, scene = load_golden(name)
     w, h = meta["width"], meta["height"]
-    out, st = gpu_render(ctx, scene, w, h, meta["spp"], meta["max_level"], meta["seed"])
+    out, st = gpu_render(ctx, scene, w, h, meta["spp"], meta["max_level"], meta["seed"],
+                         mode=meta.get("mode", rt.RT_MODE_RAYTRACE))
     check_parity(out, g, g["ambiguous"], h, w)
 
 

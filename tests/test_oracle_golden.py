@@ -15,7 +15,8 @@ def test_oracle_matches_reference(name):
     g, meta, scene = load_golden(name)
     assert scene_sha(scene) == meta["scene_sha256"], "scene generator output changed"
     w, h = meta["width"], meta["height"]
-    r = port.render(scene, w, h, meta["spp"], meta["max_level"], meta["seed"], ref_tiles=True, check=False)
+    r = port.render(scene, w, h, meta["spp"], meta["max_level"], meta["seed"], ref_tiles=True, check=False,
+                    mode=meta.get("mode", 0x80))
     rh, rw = (h // 64) * 64, (w // 64) * 64
     sl = (slice(0, rh), slice(0, rw))
     np.testing.assert_array_equal(r["obj"][sl], g["obj"][sl])
