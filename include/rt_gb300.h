@@ -374,9 +374,14 @@ int  rt_scenegen_small(uint64_t seed, int32_t n_spheres, int32_t ico_freq, int32
                        int32_t height, int32_t refractive_every, rt_scene_host **out);
 /* every object kind in one scene: plane, ballplane, cubes, spheres, a mesh, parallel + point light */
 int  rt_scenegen_extras(uint64_t seed, int32_t width, int32_t height, rt_scene_host **out);
-/* textured meshes: checker-textured plane, an icosphere with spherical texture coordinates and a
+/* textured meshes: checker-textured plane, an icosphere with planar texture coordinates and a
  * procedural texture, spheres, a cube, two point lights */
 int  rt_scenegen_textured(uint64_t seed, int32_t width, int32_t height, rt_scene_host **out);
+/* a model read from OBJ/MTL files through the drop-in Scene::AddModel (Model::loadOBJ,
+ * Model.cpp:341 of the reference: texture files are read as <name>.bmp relative to the working
+ * directory), two point lights, a camera facing it. RT_ERR_NOT_FOUND when nothing was read. */
+int  rt_scenegen_obj(const char *obj_path, const char *mtl_path, int32_t width, int32_t height,
+                     rt_scene_host **out);
 /* deep copy of a caller-built description (render parameters attached) */
 int  rt_scene_host_from_desc(const rt_scene_desc *desc, int32_t spp, int32_t max_level, uint64_t seed,
                              rt_scene_host **out);

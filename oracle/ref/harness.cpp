@@ -208,8 +208,54 @@ template <class T> void dump(const std::string &path, const std::vector<T> &v)
 
 } // namespace
 
+// --obj model.obj model.mtl out_prefix: load a model through the reference's own
+// Model::loadOBJ (Model.cpp:14-349, textures relative to the working directory as there) and
+// write what it built: per triangle its part, points, normals and texture coordinates; per part
+// its material; per material Ka, Kd, Ks (xyzw), Ns, reflect, refract, rfr and texture; the
+// textures' texels; VerMin / VerMax.
+int dump_obj(const char *obj, const char *mtl, const std::string &out)
+{
+    std::string so(obj), sm(mtl);
+    Model m(0);
+    m.loadOBJ(std::wstring(so.begin(), so.end()), std::wstring(sm.begin(), sm.end()));
+    std::vector<float> tris, mtls, bounds;
+    std::vector<int32_t> tri_part, part_mtl, mtl_tex, tex_dims;
+    std::vector<uint8_t> texels;
+    for (size_t pa = 0; pa < m.parts.size(); ++pa)
+        for (const Triangle &t : m.parts[pa]) {
+            tri_part.push_back((int32_t)pa);
+            for (int k = 0; k < 3; ++k) tris.insert(tris.end(), {t.points[k].x, t.points[k].y, t.points[k].z});
+            for (int k = 0; k < 3; ++k) tris.insert(tris.end(), {t.norms[k].x, t.norms[k].y, t.norms[k].z});
+            for (int k = 0; k < 3; ++k) tris.insert(tris.end(), {t.tcoords[k].u, t.tcoords[k].v});
+        }
+    for (int8_t pm : m.part_mtl) part_mtl.push_back(pm);
+    for (size_t i = 0; i < m.mtls.size(); ++i) {
+        const Material &M = m.mtls[i];
+        for (const Vertex *v : {&M.ambient, &M.diffuse, &M.specular}) mtls.insert(mtls.end(), {v->x, v->y, v->z, v->alpha});
+        mtls.insert(mtls.end(), {M.shiness, M.reflect, M.refract, M.rfr});
+        mtl_tex.push_back(i < m.mtl_tex.size() ? m.mtl_tex[i] : -1);
+    }
+    for (const Texture &t : m.texs) {
+        tex_dims.push_back(t.w), tex_dims.push_back(t.h);
+        texels.insert(texels.end(), t.data, t.data + (size_t)t.w * t.h * 3);
+    }
+    bounds = {m.VerMin.x, m.VerMin.y, m.VerMin.z, m.VerMax.x, m.VerMax.y, m.VerMax.z};
+    dump(out + ".tris.f32", tris);
+    dump(out + ".tripart.i32", tri_part);
+    dump(out + ".partmtl.i32", part_mtl);
+    dump(out + ".mtls.f32", mtls);
+    dump(out + ".mtltex.i32", mtl_tex);
+    dump(out + ".texdims.i32", tex_dims);
+    dump(out + ".texels.u8", texels);
+    dump(out + ".bounds.f32", bounds);
+    std::printf("{\"parts\": %zu, \"triangles\": %zu, \"materials\": %zu, \"textures\": %zu}\n", m.parts.size(),
+                tri_part.size(), m.mtls.size(), m.texs.size());
+    return 0;
+}
+
 int main(int argc, char **argv)
 {
+    if (argc == 5 && std::strcmp(argv[1], "--obj") == 0) return dump_obj(argv[2], argv[3], argv[4]);
     if (argc < 3) {
         std::fprintf(stderr, "usage: %s scene.rtsc out_prefix [threads] [tiles_file|-] [mode]\n", argv[0]);
         return 2;

@@ -176,6 +176,7 @@ _SIGS = {
     "rt_scenegen_small": (C.c_int, [C.c_uint64, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.POINTER(P)]),
     "rt_scenegen_extras": (C.c_int, [C.c_uint64, C.c_int32, C.c_int32, C.POINTER(P)]),
     "rt_scenegen_textured": (C.c_int, [C.c_uint64, C.c_int32, C.c_int32, C.POINTER(P)]),
+    "rt_scenegen_obj": (C.c_int, [C.c_char_p, C.c_char_p, C.c_int32, C.c_int32, C.POINTER(P)]),
     "rt_scene_host_from_desc": (C.c_int, [C.POINTER(SceneDesc), C.c_int32, C.c_int32, C.c_uint64, C.POINTER(P)]),
     "rt_scene_host_desc": (C.POINTER(SceneDesc), [P]),
     "rt_scene_host_render_params": (C.c_int, [P, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_uint64)]),
@@ -244,11 +245,20 @@ class SceneHost:
 
     @classmethod
     def textured(cls, seed: int, width: int = 128, height: int = 64) -> "SceneHost":
-        """Checker-textured plane, a textured icosphere (spherical uvs, procedural map), spheres, a cube."""
+        """Checker-textured plane, a textured icosphere (planar uvs, procedural map), spheres, a cube."""
         h = P()
         rc = lib.rt_scenegen_textured(seed, width, height, C.byref(h))
         if rc:
             raise RTError(rc, "rt_scenegen_textured")
+        return cls(h)
+
+    @classmethod
+    def from_obj(cls, obj_path: str, mtl_path: str, width: int = 128, height: int = 64) -> "SceneHost":
+        """A model read by the drop-in OBJ/MTL loader (textures relative to the working directory)."""
+        h = P()
+        rc = lib.rt_scenegen_obj(obj_path.encode(), mtl_path.encode(), width, height, C.byref(h))
+        if rc:
+            raise RTError(rc, f"rt_scenegen_obj: cannot load {obj_path}")
         return cls(h)
 
     @classmethod

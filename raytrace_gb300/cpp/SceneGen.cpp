@@ -397,7 +397,7 @@ extern "C" int rt_scenegen_extras(uint64_t seed, int32_t width, int32_t height, 
 }
 
 // textured meshes: the plane with its default checker texture, a displaced icosphere with
-// spherical texture coordinates and a 64x32 procedural texture (map_Kd of its material), 6
+// planar texture coordinates and a 64x32 procedural texture (map_Kd of its material), 6
 // spheres (some refractive), a cube, two point lights
 extern "C" int rt_scenegen_textured(uint64_t seed, int32_t width, int32_t height, rt_scene_host **out)
 {
@@ -407,13 +407,10 @@ extern "C" int rt_scenegen_textured(uint64_t seed, int32_t width, int32_t height
     sc.AddPlane();
     const Vertex centre(0.0f, 1.4f, 0.5f);
     std::vector<Triangle> tris = make_icosphere(12, centre, 1.3f, 0.15f, (uint32_t)seed);
-    const double pi = 3.14159265358979323846;
-    for (Triangle &t : tris)
+    for (Triangle &t : tris)   // planar projection along z (arithmetic only: the same on every host)
         for (int k = 0; k < 3; ++k) {
             const Vertex d = t.points[k] - centre;
-            const double len = std::sqrt((double)d.x * d.x + (double)d.y * d.y + (double)d.z * d.z);
-            t.tcoords[k] = Coord2D((float)(0.5 + std::atan2((double)d.z, (double)d.x) / (2 * pi)),
-                                   (float)(0.5 + std::asin(std::max(-1.0, std::min(1.0, d.y / len))) / pi));
+            t.tcoords[k] = Coord2D(0.5f + d.x / 2.6f, 0.5f + d.y / 2.6f);
         }
     Material m = law_material(r);
     Model *model = new Model();
@@ -436,6 +433,32 @@ extern "C" int rt_scenegen_textured(uint64_t seed, int32_t width, int32_t height
     sc.EnvLight = Vertex(0.1f, 0.1f, 0.1f, 1.0f);
     set_camera(sc, Vertex(0, 2.5f, -8), Vertex(0, 1.0f, 0), width, height, 60.0f);
     *out = finish(sc, 1, 3, seed);
+    return RT_OK;
+}
+
+// a model read from OBJ/MTL files through the drop-in Scene::AddModel (the reference's loader:
+// quads split, materials inherited, map_Kd read as <name>.bmp from the working directory,
+// rescaled to extent 8; Model.cpp:14-349), two point lights and a camera facing the model
+extern "C" int rt_scenegen_obj(const char *obj_path, const char *mtl_path, int32_t width, int32_t height,
+                               rt_scene_host **out)
+{
+    if (!out || !obj_path || !mtl_path || width <= 0 || height <= 0) return RT_ERR_INVALID;
+    *out = nullptr;
+    Scene sc;
+    const std::string so(obj_path), sm(mtl_path);
+    const uint8_t id = sc.AddModel(std::wstring(so.begin(), so.end()), std::wstring(sm.begin(), sm.end()));
+    const Model *m = static_cast<const Model *>(sc.Objects[id]);
+    size_t n = 0;
+    for (const auto &part : m->parts) n += part.size();
+    if (n == 0) return RT_ERR_NOT_FOUND;   // no such file or no faces
+    Light l1(MY_LIGHT_POINT), l2(MY_LIGHT_POINT);
+    l1.position = Vertex(6.0f, 10.0f, -8.0f, 1.0f);
+    l2.position = Vertex(-8.0f, 6.0f, -4.0f, 1.0f);
+    sc.Lights.push_back(l1);
+    sc.Lights.push_back(l2);
+    sc.EnvLight = Vertex(0.1f, 0.1f, 0.1f, 1.0f);
+    set_camera(sc, Vertex(0, 3, -14), Vertex(0, 0, 0), width, height, 60.0f);
+    *out = finish(sc, 1, 3, 0);
     return RT_OK;
 }
 

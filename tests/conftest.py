@@ -35,6 +35,8 @@ def load_golden(name: str):
             g.pop("scene").tofile(p)
             scene = rt.SceneHost.load(p)
     else:
+        if meta["generator"] == "obj":
+            raise RuntimeError("OBJ fixtures embed their scene")
         gen = {"config": rt.SceneHost.config, "small": rt.SceneHost.small, "extras": rt.SceneHost.extras,
                "textured": rt.SceneHost.textured}[meta["generator"]]
         scene = gen(*meta["args"]).with_camera(meta["width"], meta["height"], meta["spp"], meta["max_level"], meta["seed"])

@@ -52,13 +52,23 @@ CASES = {
     "textured_128x64": ("textured", (6, 128, 64), 128, 64, 1, 3, 6),
     "textured_texture_128x64": ("textured", (6, 128, 64), 128, 64, 1, 3, 6, 0x4),
     "textured_material_128x64": ("textured", (6, 128, 64), 128, 64, 1, 3, 6, 0x5),
+    "obj_house_128x64": ("obj", ("model.obj", "model.mtl", 128, 64), 128, 64, 1, 3, 0),
+    "obj_house_texture_128x64": ("obj", ("model.obj", "model.mtl", 128, 64), 128, 64, 1, 3, 0, 0x4),
 }
 EMBED_LIMIT = 256 * 1024
 
 
 def make_scene(gen: str, args: tuple, w: int, h: int, spp: int, lvl: int, seed: int) -> rt.SceneHost:
-    base = {"config": rt.SceneHost.config, "small": rt.SceneHost.small, "extras": rt.SceneHost.extras,
-            "textured": rt.SceneHost.textured}[gen](*args)
+    if gen == "obj":   # the OBJ asset of tests/golden/obj (its texture is read relative to the cwd)
+        cwd = os.getcwd()
+        os.chdir(os.path.join(HERE, "obj"))
+        try:
+            base = rt.SceneHost.from_obj(*args)
+        finally:
+            os.chdir(cwd)
+    else:
+        base = {"config": rt.SceneHost.config, "small": rt.SceneHost.small, "extras": rt.SceneHost.extras,
+                "textured": rt.SceneHost.textured}[gen](*args)
     return base.with_camera(w, h, spp, lvl, seed)
 
 
