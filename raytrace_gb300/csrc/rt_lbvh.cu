@@ -148,27 +148,82 @@ __global__ void __launch_bounds__(kSortThreads) k_hist(int n, const unsigned *ke
     hist[threadIdx.x * tiles + tile] = h[threadIdx.x];
 }
 
-// exclusive scan of m values in one block of 1024 threads (chunked)
-__global__ void __launch_bounds__(1024) k_scan(unsigned *a, int m)
+// Exclusive scan of the digit-major tile histograms (m = 256 x tiles counts) in three steps:
+// block sums of 4096-count chunks, one block scanning those sums, then each chunk scanned in its
+// block with the chunk's offset added. Loads are coalesced (a block reads its chunk as 1024 x
+// uint4), so a pass costs a few microseconds instead of one block walking the whole array.
+constexpr int kScanThreads = 1024, kScanChunk = 4 * kScanThreads;
+__host__ __device__ constexpr int scan_chunks(int m) { return (m + kScanChunk - 1) / kScanChunk; }
+
+// the block's inclusive prefix of v (blockDim.x == kScanThreads); *total = the block's sum
+__device__ __forceinline__ unsigned block_inclusive_scan(unsigned v, unsigned *warp_sums, unsigned *total)
 {
-    __shared__ unsigned sums[1024];
-    const int per = (m + 1023) / 1024;
-    const int b = threadIdx.x * per, e = min(b + per, m);
-    unsigned s = 0;
-    for (int i = b; i < e; ++i) s += a[i];
-    sums[threadIdx.x] = s;
-    __syncthreads();
-    for (int off = 1; off < 1024; off <<= 1) {
-        unsigned v = threadIdx.x >= off ? sums[threadIdx.x - off] : 0u;
-        __syncthreads();
-        sums[threadIdx.x] += v;
-        __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int off = 1; off < 32; off <<= 1) {
+        const unsigned u = __shfl_up_sync(0xffffffffu, v, off);
+        if (lane >= off) v += u;
     }
-    unsigned run = sums[threadIdx.x] - s;
-    for (int i = b; i < e; ++i) {
-        unsigned v = a[i];
-        a[i] = run;
-        run += v;
+    if (lane == 31) warp_sums[warp] = v;
+    __syncthreads();
+    if (warp == 0) {
+        unsigned w = warp_sums[lane];
+        for (int off = 1; off < 32; off <<= 1) {
+            const unsigned u = __shfl_up_sync(0xffffffffu, w, off);
+            if (lane >= off) w += u;
+        }
+        warp_sums[lane] = w;   // inclusive over warps
+    }
+    __syncthreads();
+    if (total) *total = warp_sums[31];
+    return v + (warp > 0 ? warp_sums[warp - 1] : 0u);
+}
+
+// m is a multiple of 4 (256 counts per tile), so a thread's 4 counts are one aligned uint4
+__global__ void __launch_bounds__(kScanThreads) k_scan_reduce(const unsigned *a, int m, unsigned *part)
+{
+    __shared__ unsigned warp_sums[32];
+    const int i = blockIdx.x * kScanChunk + 4 * threadIdx.x;
+    unsigned v = 0;
+    if (i < m) {
+        const uint4 q = *reinterpret_cast<const uint4 *>(a + i);
+        v = q.x + q.y + q.z + q.w;
+    }
+    unsigned total = 0;
+    block_inclusive_scan(v, warp_sums, &total);
+    if (threadIdx.x == 0) part[blockIdx.x] = total;
+}
+
+// exclusive scan of the chunk sums in place (one block, any number of chunks)
+__global__ void __launch_bounds__(kScanThreads) k_scan_top(unsigned *part, int chunks)
+{
+    __shared__ unsigned warp_sums[32];
+    unsigned carry = 0;
+    for (int base = 0; base < chunks; base += kScanThreads) {
+        const int i = base + threadIdx.x;
+        const unsigned v = i < chunks ? part[i] : 0u;
+        unsigned total = 0;
+        const unsigned inc = block_inclusive_scan(v, warp_sums, &total);
+        if (i < chunks) part[i] = carry + inc - v;
+        carry += total;
+        __syncthreads();   // warp_sums is reused by the next round
+    }
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_down(unsigned *a, int m, const unsigned *part)
+{
+    __shared__ unsigned warp_sums[32];
+    const int i = blockIdx.x * kScanChunk + 4 * threadIdx.x;
+    uint4 q = make_uint4(0, 0, 0, 0);
+    if (i < m) q = *reinterpret_cast<const uint4 *>(a + i);
+    const unsigned t = q.x + q.y + q.z + q.w;
+    const unsigned excl = block_inclusive_scan(t, warp_sums, nullptr) - t + part[blockIdx.x];
+    if (i < m) {
+        uint4 o;
+        o.x = excl;
+        o.y = o.x + q.x;
+        o.z = o.y + q.y;
+        o.w = o.z + q.z;
+        *reinterpret_cast<uint4 *>(a + i) = o;
     }
 }
 
@@ -370,6 +425,7 @@ struct Scratch {
     unsigned *codes[2];   // n each
     unsigned *idx[2];     // n each
     unsigned *hist;       // 256 * tiles
+    unsigned *part;       // scan_chunks(256 * tiles) chunk sums of the histogram scan
     int *parent;          // 2n - 1
     int *flags;           // n - 1
 };
@@ -393,6 +449,8 @@ Scratch carve(void *base, int n)
     }
     s.hist = (unsigned *)p;
     p += align256(4 * 256 * (size_t)tiles);
+    s.part = (unsigned *)p;
+    p += align256(4 * (size_t)scan_chunks(256 * tiles));
     s.parent = (int *)p;
     p += align256(4 * (size_t)(2 * n));
     s.flags = (int *)p;
@@ -417,7 +475,10 @@ cudaError_t morton_and_sort(const LbvhInput &in, const Scratch &sc, cudaStream_t
     for (int pass = 0; pass < 4; ++pass) {
         const int src = pass & 1, dst = src ^ 1;
         k_hist<<<tiles, kSortThreads, 0, s>>>(n, sc.codes[src], 8 * pass, sc.hist, tiles);
-        k_scan<<<1, 1024, 0, s>>>(sc.hist, 256 * tiles);
+        const int m = 256 * tiles, chunks = scan_chunks(m);
+        k_scan_reduce<<<chunks, kScanThreads, 0, s>>>(sc.hist, m, sc.part);
+        k_scan_top<<<1, kScanThreads, 0, s>>>(sc.part, chunks);
+        k_scan_down<<<chunks, kScanThreads, 0, s>>>(sc.hist, m, sc.part);
         k_scatter<<<tiles, kSortThreads, 0, s>>>(n, sc.codes[src], sc.idx[src], sc.codes[dst], sc.idx[dst], 8 * pass,
                                                  sc.hist, tiles);
     }
@@ -450,7 +511,7 @@ size_t lbvh_scratch_bytes(int n)
 {
     const int tiles = (n + kTileKeys - 1) / kTileKeys;
     return 256 + align256(sizeof(float4) * (size_t)n) + 4 * align256(4 * (size_t)n) + align256(4 * 256 * (size_t)tiles) +
-           align256(4 * (size_t)(2 * n)) + align256(4 * (size_t)n) + 256;
+           align256(4 * (size_t)scan_chunks(256 * tiles)) + align256(4 * (size_t)(2 * n)) + align256(4 * (size_t)n) + 256;
 }
 
 cudaError_t lbvh_morton_sort(const LbvhInput &in, uint32_t *codes_out, uint32_t *perm_out, void *scratch, cudaStream_t s)
@@ -487,8 +548,9 @@ cudaError_t lbvh_build(const LbvhInput &in, const LbvhOutput &out, void *scratch
 // ---- allocation-free Morton sort -------------------------------------------------------------
 // Working memory of rt_morton_sort_noalloc: one fixed array in device memory, sized for
 // RT_NOALLOC_MAX_TRIS triangles (centroids 16 B, second sort buffer 8 B and zero object ids
-// 4 B per triangle, digit histograms 1 KB per 2048 triangles, the scene box and a zero object
-// position). Every GPU that loads the library holds it until the process exits.
+// 4 B per triangle, digit histograms 1 KB per 2048 triangles and 4 B per 4096 histogram counts
+// for their scan, the scene box and a zero object position). Every GPU that loads the library
+// holds it until the process exits.
 #include <cstdio>
 #include <mutex>
 
@@ -499,8 +561,9 @@ namespace {
 
 constexpr size_t kNoAllocN = (size_t)RT_NOALLOC_MAX_TRIS;
 constexpr size_t kNoAllocTiles = (kNoAllocN + kTileKeys - 1) / kTileKeys;
+constexpr size_t kNoAllocChunks = (256 * kNoAllocTiles + 4095) / 4096;   // histogram-scan chunk sums
 constexpr size_t kNoAllocBytes = 256 + 256 + 16 * kNoAllocN + 4 * kNoAllocN + 4 * kNoAllocN + 4 * kNoAllocN +
-                                 1024 * kNoAllocTiles;
+                                 1024 * kNoAllocTiles + 4 * kNoAllocChunks;
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 
 constexpr int kNoAllocMaxDevices = 64;
@@ -556,6 +619,7 @@ extern "C" int rt_morton_sort_noalloc(const float *d_tri_p, int64_t n_tris, uint
     sc.codes[1] = (unsigned *)(p + 512 + 20 * kNoAllocN);
     sc.idx[1] = (unsigned *)(p + 512 + 24 * kNoAllocN);
     sc.hist = (unsigned *)(p + 512 + 28 * kNoAllocN);
+    sc.part = (unsigned *)(p + 512 + 28 * kNoAllocN + 1024 * kNoAllocTiles);
     sc.codes[0] = d_codes;   // the caller's outputs are the other sort buffer: 4 passes end there
     sc.idx[0] = d_perm;
     // the array keeps the previous call's bytes: zero the object table this call reads
