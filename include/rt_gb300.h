@@ -255,7 +255,8 @@ int rt_batch_autotune(rt_ctx *ctx, int32_t n, const int32_t *scene_ids, const in
  * requests while frame slots and the HBM budget allow (LRU-evicting idle scenes, rebuilding
  * an evicted scene's LBVH on a miss), then traces one wave made of sample chunks of every
  * admitted request, so frames admitted at different times share the same kernels. A finished
- * frame is resolved and copied to pinned host memory on a copy stream. Each frame is the same
+ * frame is resolved and its uint8 image (and, with keep_images, its float colour) copied to
+ * pinned host memory on a copy stream. Each frame is the same
  * alone or in any mix: colours accumulate as exact fixed-point sums. */
 typedef struct rt_server rt_server;
 
@@ -265,7 +266,7 @@ typedef struct rt_server_config {
     int32_t max_level;           /* recursion depth of every request */
     int32_t spp;                 /* samples per pixel of every request (>= 1) */
     int32_t plain;               /* 1: one request at a time through rt_render (comparison path) */
-    int64_t queue_rays;          /* ray-queue entries of one wave (0 = 2^23) */
+    int64_t queue_rays;          /* ray-queue entries of one wave (0 = 2^24) */
     int64_t max_pixels;          /* largest width*height of a request (0 = 1920*1080) */
     int32_t keep_images;         /* 1: keep finished images in host memory until rt_server_result */
     int32_t stages;              /* waves the host may enqueue ahead of the device (0 = 2) */

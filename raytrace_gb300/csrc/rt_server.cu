@@ -287,7 +287,9 @@ static int finish(rt_server *srv, Request *r)
     CK(ctx, cudaEventRecord(resolved, ctx->stream));
     CK(ctx, cudaStreamWaitEvent(srv->copy, resolved, 0));
     srv->ev_pool.push_back(resolved);   // re-recording later does not affect the wait above
-    CK(ctx, cudaMemcpyAsync(hs.rgb, slot.fb.rgb, 12 * np, cudaMemcpyDeviceToHost, srv->copy));
+    // the frame a client receives is the uint8 image (Color::put); float colour only when the
+    // server keeps images for inspection
+    if (srv->cfg.keep_images) CK(ctx, cudaMemcpyAsync(hs.rgb, slot.fb.rgb, 12 * np, cudaMemcpyDeviceToHost, srv->copy));
     CK(ctx, cudaMemcpyAsync(hs.rgb8, slot.fb.rgb8, 3 * np, cudaMemcpyDeviceToHost, srv->copy));
     CK(ctx, cudaEventRecord(slot.copied, srv->copy));
     r->done_ev = take_event(srv);
@@ -384,7 +386,7 @@ static int step_plain(rt_server *srv)
         return RT_OK;
     }
     HostSlot &h = srv->hslots[(size_t)hs];
-    rc = rt_frame_download(ctx, it->second, h.rgb, h.rgb8, nullptr, nullptr, nullptr);
+    rc = rt_frame_download(ctx, it->second, srv->cfg.keep_images ? h.rgb : nullptr, h.rgb8, nullptr, nullptr, nullptr);
     if (rc) return rc;
     srv->plain_rays += (unsigned long long)st.rays_primary + st.rays_secondary + st.rays_shadow;
     r->wj.total = (long long)rd.width * rd.height * rd.spp;
@@ -533,7 +535,7 @@ static int server_init(rt_server *srv)
     rt_ctx *ctx = srv->ctx;
     rt_server_config &c = srv->cfg;
     if (c.max_inflight <= 0) c.max_inflight = 64;
-    if (c.queue_rays <= 0) c.queue_rays = 1ll << 23;
+    if (c.queue_rays <= 0) c.queue_rays = 1ll << 24;
     if (c.max_pixels <= 0) c.max_pixels = 1920ll * 1080;
     if (c.stages <= 0) c.stages = 2;
     if (c.spp < 1 || c.spp > 1024 || c.max_level < 0 || c.max_level > 4 || c.max_inflight > 4096 ||

@@ -215,3 +215,39 @@ def test_lbvh_invariants(ctx):
         sph = spheres[perm[k] & 0x7FFFFFFF]
         c, r = np.array(list(sph.position), np.float32), np.float32(sph.radius)
         assert np.all(c - r >= leaf_lo[k]) and np.all(c + r <= leaf_hi[k])
+
+
+def test_cancel_stops_a_render_and_the_next_render_is_whole(ctx):
+    """rt_cancel lands on the device flag while the render runs; the render reports
+    RT_ERR_CANCELLED and the next render is complete and unaffected."""
+    w, h = 1920, 1080
+    scene = rt.SceneHost.config(2)
+    sid = ctx.upload(scene)
+    fid = ctx.frame(w, h)
+    try:
+        small = ctx.render_desc(w, h, 1, 2, seed=3)
+        ctx.render(sid, fid, small)
+        want = ctx.download(fid, w, h, planes=False)["rgb"]
+        ctx.render(sid, fid, ctx.render_desc(w, h, 16, 4, seed=2), wait=False)   # ~40 ms of work
+        assert rt.lib.rt_cancel(ctx.handle) == 0
+        with pytest.raises(rt.RTError) as e:
+            ctx.wait()
+        assert e.value.code == rt.RT_ERR_CANCELLED
+        ctx.render(sid, fid, small)
+        np.testing.assert_array_equal(ctx.download(fid, w, h, planes=False)["rgb"], want)
+    finally:
+        ctx.release_frame(fid)
+        ctx.release_scene(sid)
+
+
+@pytest.mark.parametrize("mode", [rt.RT_MODE_DEPTH, rt.RT_MODE_NORMAL, rt.RT_MODE_TEXTURE, rt.RT_MODE_MATERIAL,
+                                  rt.RT_MODE_SHADOW, rt.RT_MODE_REFLECT, rt.RT_MODE_CHECK])
+def test_render_modes_full_frame_match_oracle(ctx, mode):
+    """Every test mode of the reference on the full frame (not only its 64x64 tiles)."""
+    w, h = 100, 70
+    scene = rt.SceneHost.textured(6, w, h)
+    out, _ = gpu_render(ctx, scene, w, h, 1, 3, 6, ref_tiles=False, mode=mode)
+    ref = port.render(scene, w, h, 1, 3, 6, ref_tiles=False, check=True, mode=mode)
+    a = ref["ambiguous"]
+    d = np.abs(out["rgb"] - ref["rgb"]).max(axis=2)
+    assert not ((d > TOL) & ~a).any(), (mode, float(d[~a].max()))

@@ -223,3 +223,38 @@ def test_server_poisson_stream(ctx):
         assert st["mrays_per_s"] > 0 and st["rays"] > 0, st
     assert out[False]["requests"] == out[True]["requests"]   # same seeded stream
     assert out[False]["pixels"] == out[True]["pixels"]
+
+
+def test_batch_mixes_render_modes(ctx):
+    """Jobs of different test modes (and depths) share waves and equal their plain renders."""
+    scene = rt.SceneHost.textured(6, 64, 64)
+    modes = [rt.RT_MODE_RAYTRACE, rt.RT_MODE_NORMAL, rt.RT_MODE_SHADOW, rt.RT_MODE_REFLECT, rt.RT_MODE_DEPTH,
+             rt.RT_MODE_CHECK]
+    sid = ctx.upload(scene)
+    fids = [ctx.frame(64, 48) for _ in modes]
+    rds = [ctx.render_desc(64, 48, 2, 3, mode=m, seed=5) for m in modes]
+    try:
+        ctx.batch([sid] * len(modes), fids, rds)
+        got = [ctx.download(f, 64, 48, planes=False)["rgb"] for f in fids]
+        for m, rd, g in zip(modes, rds, got):
+            ctx.render(sid, fids[0], rd)
+            assert np.array_equal(ctx.download(fids[0], 64, 48, planes=False)["rgb"], g), hex(m)
+    finally:
+        for f in fids:
+            ctx.release_frame(f)
+        ctx.release_scene(sid)
+
+
+def test_server_multi_sample_requests_equal_plain_renders(ctx):
+    scenes = small_scenes()[:2]
+    with rt.Server(ctx, 8 << 30, max_inflight=4, spp=4, max_level=4, queue_rays=1 << 15, max_pixels=96 * 96) as srv:
+        ids = [srv.add_scene(s) for s in scenes]
+        reqs = [(ids[k % 2], 80, 60, rt.orbit_camera(srv.camera(ids[k % 2]), 50.0 * k, 25.0, 80, 60), 900 + k)
+                for k in range(4)]
+        rids = [srv.submit(*r) for r in reqs]
+        srv.drain()
+        got = [srv.result(r)["rgb"] for r in rids]
+    for (sid, w, h, cam, seed), g in zip(reqs, got):
+        ref = plain_render(ctx, scenes[sid], w, h, camera=cam, spp=4, level=4, seed=seed)
+        assert np.array_equal(ref["rgb"], g)
+
