@@ -195,7 +195,7 @@ int wave_enqueue(rt_ctx *ctx, WaveRunner &R, const std::vector<WaveJob *> &jobs,
 // ---- batch ---------------------------------------------------------------------------------------------------
 
 namespace {
-// ray-queue entries of one batch wave by default: 2^24 entries hold 228 B each (two ray
+// ray-queue entries of one batch wave by default: 2^24 entries hold 232 B each (two ray
 // queues, shadow queue, hit record)
 constexpr long long kBatchQueue = 1ll << 24;
 } // namespace

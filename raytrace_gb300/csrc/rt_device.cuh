@@ -166,6 +166,7 @@ struct Counters {
     int s_count;                          // shadow queue size
     int overflow;                         // a queue ran out of space
     int work[16];                         // dynamic work counters (reset per pass)
+    int h_count[8];                       // hits listed by extend, per bounce
     unsigned long long rays_primary, rays_secondary, rays_shadow;
     unsigned long long nodes, tris, spheres;            // extend kernels (closest hit)
     unsigned long long s_nodes, s_tris, s_spheres;      // shadow kernels (any hit)

@@ -177,16 +177,30 @@ __global__ void __launch_bounds__(MINB ? 128 : 256, MINB ? MINB : 1) k_extend(Wa
     const RayQueue q = wf.q[sel];
     const int n = min(C->q_count[sel], q.capacity);
     WorkCount wc{0, 0, 0, 0};
+    const int level = wslot / 3;
+    const int lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1u;
     for_each_ray<DYN>(n, &C->work[wslot], tile, [&](int i, bool active) {
-        if (!active) return;
-        float4 o4 = q.o[i], d4 = q.d[i];
-        int4 m4 = q.m[i];
-        const DevScene &S = wf.scenes[wf.jobs[m4.w].scene];
-        Best best;
-        int newobj;
-        closest_hit<STACK, COUNT>(S, mk(o4), mk(d4), m4.x, ray_inside(m4.y) != 0, best, newobj, wc);
-        wf.hit[i] = make_float4(best.t, best.u, best.v, __int_as_float(best.key));
-        wf.newobj[i] = newobj;
+        bool is_hit = false;
+        if (active) {
+            float4 o4 = q.o[i], d4 = q.d[i];
+            int4 m4 = q.m[i];
+            const DevScene &S = wf.scenes[wf.jobs[m4.w].scene];
+            Best best;
+            int newobj;
+            closest_hit<STACK, COUNT>(S, mk(o4), mk(d4), m4.x, ray_inside(m4.y) != 0, best, newobj, wc);
+            wf.hit[i] = make_float4(best.t, best.u, best.v, __int_as_float(best.key));
+            wf.newobj[i] = newobj;
+            is_hit = best.key >= 0;
+        }
+        // list the hits (one atomic per warp): shading runs over hits only, misses cost it nothing
+        const unsigned hb = __ballot_sync(kFull, is_hit);
+        if (hb) {
+            int base = 0;
+            if (lane == 0) base = atomicAdd(&C->h_count[level], __popc(hb));
+            base = __shfl_sync(kFull, base, 0);
+            if (is_hit) wf.hitlist[base + __popc(hb & lt)] = i;
+        }
     });
     if (wc.err) atomicOr(&C->error, wc.err);
     if (COUNT) {
@@ -293,17 +307,20 @@ __device__ V3 mode_material(const DevScene &S, const DevMaterial &M, V3 P, V3 N,
 }
 
 // ---- shade ------------------------------------------------------------------------------------
+// 1024 resident threads per SM (64 registers): shading is latency-bound on its dependent loads
 template <bool DYN>
-__global__ void __launch_bounds__(256) k_shade(Wavefront wf, int sel, int wslot, int tile)
+__global__ void __launch_bounds__(256, 4) k_shade(Wavefront wf, int sel, int wslot, int tile)
 {
     if (cancelled(wf.cancel)) return;
     Counters *C = wf.C;
     const RayQueue q = wf.q[sel], qo = wf.q[sel ^ 1];
     const ShadowQueue sq = wf.sq;
-    const int n = min(C->q_count[sel], q.capacity);
+    // the hits extend listed (a miss needs no shading: the hit planes start as misses)
+    const int n = min(C->h_count[wslot / 3], q.capacity);
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
-    for_each_ray_guided<DYN>(n, &C->work[wslot], tile, [&](int i, bool active) {
+    for_each_ray_guided<DYN>(n, &C->work[wslot], tile, [&](int j, bool active) {
+        const int i = active ? wf.hitlist[j] : 0;
         bool emit = false;
         int nchild = 0;
         float4 c_o[2], c_d[2], c_w[2];

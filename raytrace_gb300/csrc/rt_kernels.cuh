@@ -29,6 +29,7 @@ struct Wavefront {
     ShadowQueue sq;
     float4 *hit;
     int *newobj;
+    int *hitlist;                     // queue indices of the rays that hit, per bounce (C->h_count)
     Counters *C;
     const volatile int *cancel;       // device cancel flag (NULL = not cancellable)
 };
