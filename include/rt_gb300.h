@@ -178,6 +178,10 @@ const char *rt_last_error(const rt_ctx *ctx);
 int         rt_ctx_synchronize(rt_ctx *ctx);
 /* stream used by every call of this context (NULL = the context's own stream) */
 int         rt_ctx_set_stream(rt_ctx *ctx, void *cuda_stream);
+/* Released scene and frame buffers stay with the context (at most 4, 8 GB) and are reused by
+ * the next upload or frame that fits, saving a cudaMalloc / cudaFree per scene and frame;
+ * this frees them now. */
+int rt_ctx_release_cached(rt_ctx *ctx);
 
 /* ---- scenes: upload + device LBVH build (replaces RTPrepare, Model.cpp:402-480) ------ */
 int rt_scene_upload(rt_ctx *ctx, const rt_scene_desc *desc, int32_t *scene_id);

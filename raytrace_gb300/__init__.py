@@ -134,6 +134,7 @@ _SIGS = {
     "rt_last_error": (C.c_char_p, [P]),
     "rt_ctx_synchronize": (C.c_int, [P]),
     "rt_ctx_set_stream": (C.c_int, [P, P]),
+    "rt_ctx_release_cached": (C.c_int, [P]),
     "rt_scene_upload": (C.c_int, [P, C.POINTER(SceneDesc), C.POINTER(C.c_int32)]),
     "rt_scene_update_camera": (C.c_int, [P, C.c_int32, C.POINTER(Camera)]),
     "rt_scene_rebuild": (C.c_int, [P, C.c_int32]),
@@ -444,6 +445,10 @@ class Context:
 
     def synchronize(self) -> None:
         self._ck(lib.rt_ctx_synchronize(self._h), "rt_ctx_synchronize")
+
+    def release_cached(self) -> None:
+        """Free the released scene and frame buffers the context keeps for reuse."""
+        self._ck(lib.rt_ctx_release_cached(self._h), "rt_ctx_release_cached")
 
     def morton_sort(self, tri_p: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
         tri_p = np.ascontiguousarray(tri_p, np.float32).reshape(-1, 9)

@@ -60,6 +60,56 @@ cudaError_t DevBuf::ensure(size_t need)
 
 static size_t a256(size_t x) { return (x + 255) & ~(size_t)255; }
 
+// ---- buffer reuse ----------------------------------------------------------------------------------
+// Released scene and frame buffers stay with the context (a few, up to kSpareBytes) and are
+// handed to the next upload or frame that fits, saving a cudaMalloc and a cudaFree (which
+// synchronises the device) per scene and frame. Reuse is ordered by the context stream: work
+// still reading a released buffer runs before anything the next owner enqueues.
+constexpr size_t kSpareBytes = 8ull << 30;
+constexpr size_t kSpareCount = 4;
+
+void spare_put(rt_ctx *ctx, DevBuf &&b)
+{
+    if (!b.p) return;
+    ctx->spare.push_back(std::move(b));
+    size_t total = 0;
+    for (const DevBuf &x : ctx->spare) total += x.bytes;
+    if (total > kSpareBytes || ctx->spare.size() > kSpareCount) {
+        cudaStreamSynchronize(ctx->stream);   // a freed buffer must not be in use
+        while (!ctx->spare.empty() && (total > kSpareBytes || ctx->spare.size() > kSpareCount)) {
+            total -= ctx->spare.front().bytes;
+            ctx->spare.erase(ctx->spare.begin());
+        }
+    }
+}
+
+size_t spare_bytes(const rt_ctx *ctx)
+{
+    size_t total = 0;
+    for (const DevBuf &x : ctx->spare) total += x.bytes;
+    return total;
+}
+
+void spare_trim(rt_ctx *ctx)
+{
+    if (ctx->spare.empty()) return;
+    cudaStreamSynchronize(ctx->stream);
+    ctx->spare.clear();
+}
+
+// the smallest spare buffer holding `need` bytes without wasting more than half of it
+void spare_take(rt_ctx *ctx, DevBuf &dst, size_t need)
+{
+    int best = -1;
+    for (size_t i = 0; i < ctx->spare.size(); ++i) {
+        const size_t b = ctx->spare[i].bytes;
+        if (b >= need && b <= 2 * need + (64u << 20) && (best < 0 || b < ctx->spare[(size_t)best].bytes)) best = (int)i;
+    }
+    if (best < 0) return;
+    dst = std::move(ctx->spare[(size_t)best]);
+    ctx->spare.erase(ctx->spare.begin() + best);
+}
+
 // ---- version / context -------------------------------------------------------------------------------
 // Cancel: rt_cancel writes 1 into a device word from page-locked memory on a side stream, which
 // runs beside the render; each render clears it on the same stream first and its kernels wait
@@ -101,6 +151,9 @@ extern "C" int rt_ctx_create(int device, rt_ctx **out)
     if (cudaMallocHost(&c->plain_stage, kPlainStageBytes) != cudaSuccess) return RT_ERR_CUDA;
     if (cudaEventCreateWithFlags(&c->ev_staged, cudaEventDisableTiming) != cudaSuccess) return RT_ERR_CUDA;
     if (cudaEventRecord(c->ev_staged, c->stream) != cudaSuccess) return RT_ERR_CUDA;
+    if (cudaEventCreateWithFlags(&c->ev_upload, cudaEventDisableTiming) != cudaSuccess) return RT_ERR_CUDA;
+    if (cudaMallocHost((void **)&c->build_flag, sizeof(int)) != cudaSuccess) return RT_ERR_CUDA;
+    if (cudaEventRecord(c->ev_upload, c->stream) != cudaSuccess) return RT_ERR_CUDA;
     *out = c.release();
     return RT_OK;
 }
@@ -114,7 +167,11 @@ extern "C" void rt_ctx_destroy(rt_ctx *ctx)
     ctx->frames.clear();
     ctx->batch.reset();
     ctx->plain_graphs.clear();
+    ctx->spare.clear();
     ctx->ws = Workspace();
+    if (ctx->upload_stage) cudaFreeHost(ctx->upload_stage);
+    if (ctx->build_flag) cudaFreeHost(ctx->build_flag);
+    if (ctx->ev_upload) cudaEventDestroy(ctx->ev_upload);
     if (ctx->side) cudaStreamSynchronize(ctx->side);
     if (ctx->cancel_dev) cudaFree(ctx->cancel_dev);
     if (ctx->cancel_vals) cudaFreeHost(ctx->cancel_vals);
@@ -138,9 +195,18 @@ extern "C" int rt_ctx_synchronize(rt_ctx *ctx)
     return RT_OK;
 }
 
+extern "C" int rt_ctx_release_cached(rt_ctx *ctx)
+{
+    if (!ctx) return RT_ERR_INVALID;
+    spare_trim(ctx);
+    return RT_OK;
+}
+
 extern "C" int rt_ctx_set_stream(rt_ctx *ctx, void *stream)
 {
     if (!ctx) return RT_ERR_INVALID;
+    // released buffers are reused in the order of the context stream: finish the old stream
+    CK(ctx, cudaStreamSynchronize(ctx->stream));
     ctx->stream = stream ? (cudaStream_t)stream : ctx->own_stream;
     return RT_OK;
 }
@@ -179,9 +245,7 @@ int validate_desc(rt_ctx *ctx, const rt_scene_desc *d)
     for (int i = 0; i < d->n_materials; ++i)
         if (d->materials[i].texture >= d->n_textures)
             return ctx_fail(ctx, RT_ERR_INVALID, "material %d texture out of range", i);
-    for (int64_t i = 0; i < d->n_tris; ++i)
-        if (d->tri_mtl[i] < 0 || d->tri_mtl[i] >= d->n_materials)
-            return ctx_fail(ctx, RT_ERR_INVALID, "triangle %lld material out of range", (long long)i);
+    // per-triangle material indices are checked on the device by the LBVH build
     return RT_OK;
 }
 
@@ -325,26 +389,31 @@ extern "C" int rt_scene_upload(rt_ctx *ctx, const rt_scene_desc *d, int32_t *sce
         off += a256(bytes);
         return o;
     };
+    // the small tables first (one staging copy covers [0, o_small)), then the triangle inputs
+    // (copied straight from the caller's arrays), then what the LBVH build writes
     const size_t o_prims = take(sizeof(DevPrim) * std::max<size_t>(1, h.prims.size()));
     const size_t o_mtl = take(sizeof(DevMaterial) * h.mtl.size());
     const size_t o_lights = take(sizeof(DevLight) * std::max<size_t>(1, h.lights.size()));
     const size_t o_tex = take(sizeof(DevTexture) * std::max<size_t>(1, h.tex.size()));
     const size_t o_texels = take(h.texels.size());
     const size_t o_objpos = take(sizeof(float) * h.obj_pos.size());
-    const bool has_uv = d->tri_uv != nullptr;
-    const size_t o_tp = take(sizeof(float) * 9 * (size_t)n), o_tn = take(sizeof(float) * 9 * (size_t)n);
-    const size_t o_tuv = has_uv ? take(sizeof(float) * 6 * (size_t)n) : 0;
-    const size_t o_tm = take(sizeof(int) * (size_t)n), o_ti = take(sizeof(int) * (size_t)n), o_to = take(sizeof(int) * (size_t)n);
     const size_t o_rng = take(sizeof(int) * 3 * std::max<size_t>(1, h.tri_ranges.size()));
     const int n_sph = (int)h.prims.size() - h.n_linear;
     const int64_t L = n + n_sph;   // LBVH leaves
     const size_t o_sph = take(sizeof(float4) * (size_t)std::max(1, n_sph)), o_sphr = take(sizeof(float) * (size_t)std::max(1, n_sph));
     const size_t o_sphp = take(sizeof(int) * (size_t)std::max(1, n_sph)), o_spho = take(sizeof(int) * (size_t)std::max(1, n_sph));
+    const size_t o_hdr = take(sizeof(DevScene));
+    const size_t o_bad = take(sizeof(int));   // material check flag of the build (staged as 0)
+    const size_t o_small = off;
+    const bool has_uv = d->tri_uv != nullptr;
+    const size_t o_tp = take(sizeof(float) * 9 * (size_t)n), o_tn = take(sizeof(float) * 9 * (size_t)n);
+    const size_t o_tuv = has_uv ? take(sizeof(float) * 6 * (size_t)n) : 0;
+    const size_t o_tm = take(sizeof(int) * (size_t)n), o_ti = take(sizeof(int) * (size_t)n), o_to = take(sizeof(int) * (size_t)n);
     const size_t o_nodes = take(sizeof(float4) * 2 * (size_t)std::max<int64_t>(1, 2 * L - 1));
     const size_t o_quads = take(sizeof(float4) * 8 * (size_t)std::max<int64_t>(1, L - 1));
     const size_t o_tri = take(sizeof(float4) * 3 * (size_t)L), o_trin = take(sizeof(float4) * 3 * (size_t)L);
     const size_t o_triuv = has_uv ? take(sizeof(float2) * 3 * (size_t)L) : 0;
-    const size_t o_hdr = take(sizeof(DevScene));
+    spare_take(ctx, sc->mem, off);
     CK(ctx, sc->mem.ensure(off));
     char *base = (char *)sc->mem.p;
     cudaStream_t s = ctx->stream;
@@ -397,32 +466,6 @@ extern "C" int rt_scene_upload(rt_ctx *ctx, const rt_scene_desc *d, int32_t *sce
             CK(ctx, cudaMemcpyAsync(base + o_ti, ti.data(), sizeof(int) * (size_t)n, cudaMemcpyHostToDevice, s));
             CK(ctx, cudaStreamSynchronize(s));   // the staging vectors go out of scope
         }
-        CK(ctx, cudaMemcpyAsync(base + o_rng, range_tab.data(), sizeof(int) * range_tab.size(), cudaMemcpyHostToDevice, s));
-        launch_tri_objects((const int *)(base + o_rng), (int)h.tri_ranges.size(), (int)n, (int *)(base + o_to),
-                           (direct && !d->tri_id) ? (int *)(base + o_ti) : nullptr, s);
-    }
-    CK(ctx, cudaMemcpyAsync(base + o_prims, h.prims.data(), sizeof(DevPrim) * h.prims.size(), cudaMemcpyHostToDevice, s));
-    CK(ctx, cudaMemcpyAsync(base + o_mtl, h.mtl.data(), sizeof(DevMaterial) * h.mtl.size(), cudaMemcpyHostToDevice, s));
-    CK(ctx, cudaMemcpyAsync(base + o_lights, h.lights.data(), sizeof(DevLight) * h.lights.size(), cudaMemcpyHostToDevice, s));
-    CK(ctx, cudaMemcpyAsync(base + o_tex, h.tex.data(), sizeof(DevTexture) * h.tex.size(), cudaMemcpyHostToDevice, s));
-    CK(ctx, cudaMemcpyAsync(base + o_texels, h.texels.data(), h.texels.size(), cudaMemcpyHostToDevice, s));
-    CK(ctx, cudaMemcpyAsync(base + o_objpos, h.obj_pos.data(), sizeof(float) * h.obj_pos.size(), cudaMemcpyHostToDevice, s));
-    if (n_sph > 0) {
-        std::vector<float4> sph((size_t)n_sph);
-        std::vector<float> sphr((size_t)n_sph);
-        std::vector<int> sphp((size_t)n_sph), spho((size_t)n_sph);
-        for (int j = 0; j < n_sph; ++j) {
-            const DevPrim &p = h.prims[(size_t)(h.n_linear + j)];
-            sph[(size_t)j] = p.a;
-            sphr[(size_t)j] = p.b.x;
-            sphp[(size_t)j] = h.n_linear + j;
-            spho[(size_t)j] = p.obj;
-        }
-        CK(ctx, cudaMemcpyAsync(base + o_sph, sph.data(), sizeof(float4) * sph.size(), cudaMemcpyHostToDevice, s));
-        CK(ctx, cudaMemcpyAsync(base + o_sphr, sphr.data(), sizeof(float) * sphr.size(), cudaMemcpyHostToDevice, s));
-        CK(ctx, cudaMemcpyAsync(base + o_sphp, sphp.data(), sizeof(int) * sphp.size(), cudaMemcpyHostToDevice, s));
-        CK(ctx, cudaMemcpyAsync(base + o_spho, spho.data(), sizeof(int) * spho.size(), cudaMemcpyHostToDevice, s));
-        CK(ctx, cudaStreamSynchronize(s));   // the staging vectors go out of scope
     }
     DevScene &H = sc->hdr;
     H.prims = (const DevPrim *)(base + o_prims);
@@ -443,7 +486,44 @@ extern "C" int rt_scene_upload(rt_ctx *ctx, const rt_scene_desc *d, int32_t *sce
     H.n_mtl = (int)h.mtl.size();
     for (int k = 0; k < 3; ++k) H.env[k] = d->env_light[k];
     sc->d_hdr = (DevScene *)(base + o_hdr);
-    CK(ctx, cudaMemcpyAsync(sc->d_hdr, &H, sizeof(DevScene), cudaMemcpyHostToDevice, s));
+    {   // the small tables, sphere leaves, model range table and header: one page-locked copy
+        CK(ctx, cudaEventSynchronize(ctx->ev_upload));   // the previous upload's copy has left the staging
+        if (ctx->upload_stage_bytes < o_small) {
+            if (ctx->upload_stage) CK(ctx, cudaFreeHost(ctx->upload_stage));
+            ctx->upload_stage = nullptr;
+            ctx->upload_stage_bytes = 0;
+            CK(ctx, cudaMallocHost(&ctx->upload_stage, o_small));
+            ctx->upload_stage_bytes = o_small;
+        }
+        char *st = (char *)ctx->upload_stage;
+        auto put = [&](size_t o, const void *src, size_t bytes) {
+            if (bytes) std::memcpy(st + o, src, bytes);
+        };
+        put(o_prims, h.prims.data(), sizeof(DevPrim) * h.prims.size());
+        put(o_mtl, h.mtl.data(), sizeof(DevMaterial) * h.mtl.size());
+        put(o_lights, h.lights.data(), sizeof(DevLight) * h.lights.size());
+        put(o_tex, h.tex.data(), sizeof(DevTexture) * h.tex.size());
+        put(o_texels, h.texels.data(), h.texels.size());
+        put(o_objpos, h.obj_pos.data(), sizeof(float) * h.obj_pos.size());
+        put(o_rng, range_tab.data(), sizeof(int) * range_tab.size());
+        for (int j = 0; j < n_sph; ++j) {
+            const DevPrim &p = h.prims[(size_t)(h.n_linear + j)];
+            const int prim = h.n_linear + j;
+            put(o_sph + sizeof(float4) * (size_t)j, &p.a, sizeof(float4));
+            put(o_sphr + sizeof(float) * (size_t)j, &p.b.x, sizeof(float));
+            put(o_sphp + sizeof(int) * (size_t)j, &prim, sizeof(int));
+            put(o_spho + sizeof(int) * (size_t)j, &p.obj, sizeof(int));
+        }
+        put(o_hdr, &H, sizeof(DevScene));
+        const int zero = 0;
+        put(o_bad, &zero, sizeof zero);
+        CK(ctx, cudaMemcpyAsync(base, st, o_small, cudaMemcpyHostToDevice, s));
+        CK(ctx, cudaEventRecord(ctx->ev_upload, s));
+    }
+    if (n > 0)   // per-triangle object (and model-local id) from the range table just copied
+        launch_tri_objects((const int *)(base + o_rng), (int)h.tri_ranges.size(), (int)n, (int *)(base + o_to),
+                           (direct && !d->tri_id) ? (int *)(base + o_ti) : nullptr, s);
+    CK(ctx, cudaGetLastError());
     sc->in.tri_p = (const float *)(base + o_tp);
     sc->in.tri_n = (const float *)(base + o_tn);
     sc->in.tri_uv = has_uv ? (const float *)(base + o_tuv) : nullptr;
@@ -457,6 +537,8 @@ extern "C" int rt_scene_upload(rt_ctx *ctx, const rt_scene_desc *d, int32_t *sce
     sc->in.sph_prim = (const int *)(base + o_sphp);
     sc->in.sph_obj = (const int *)(base + o_spho);
     sc->in.n_sph = n_sph;
+    sc->in.n_mtl = (int)h.mtl.size();
+    sc->in.bad = (int *)(base + o_bad);
     sc->out.nodes = (float4 *)(base + o_nodes);
     sc->out.quads = (float4 *)(base + o_quads);
     sc->out.tri = (float4 *)(base + o_tri);
@@ -488,15 +570,28 @@ extern "C" int rt_scene_rebuild(rt_ctx *ctx, int32_t id)
     cudaEvent_t a, b;
     CK(ctx, cudaEventCreate(&a));
     CK(ctx, cudaEventCreate(&b));
+    {   // an error left by an earlier unchecked call would be mistaken for a build failure
+        const cudaError_t stale = cudaGetLastError();
+        if (stale != cudaSuccess)
+            return ctx_fail(ctx, RT_ERR_CUDA, "CUDA error pending before the LBVH build: %s", cudaGetErrorString(stale));
+    }
+    if (sc.in.bad) CK(ctx, cudaMemsetAsync(sc.in.bad, 0, sizeof(int), ctx->stream));
+    g_build_step = "";
     cudaEventRecord(a, ctx->stream);
     cudaError_t e = lbvh_build(sc.in, sc.out, ctx->lbvh_scratch.p, ctx->stream);
     cudaEventRecord(b, ctx->stream);
+    int bad = 0;
+    if (e == cudaSuccess && sc.in.bad)
+        e = cudaMemcpyAsync(ctx->build_flag, sc.in.bad, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
     if (e == cudaSuccess) e = cudaEventSynchronize(b);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e == cudaSuccess && sc.in.bad) bad = *ctx->build_flag;
     float ms = 0.0f;
     if (e == cudaSuccess) cudaEventElapsedTime(&ms, a, b);
     cudaEventDestroy(a);
     cudaEventDestroy(b);
-    if (e != cudaSuccess) return ctx_fail(ctx, RT_ERR_CUDA, "LBVH build: %s", cudaGetErrorString(e));
+    if (e != cudaSuccess) return ctx_fail(ctx, RT_ERR_CUDA, "LBVH build (%s): %s", g_build_step, cudaGetErrorString(e));
+    if (bad) return ctx_fail(ctx, RT_ERR_INVALID, "a triangle's material is outside the material table");
     sc.build_ms = ms;
     return RT_OK;
 }
@@ -515,7 +610,7 @@ extern "C" int rt_scene_release(rt_ctx *ctx, int32_t id)
     if (!ctx) return RT_ERR_INVALID;
     auto it = ctx->scenes.find(id);
     if (it == ctx->scenes.end()) return ctx_fail(ctx, RT_ERR_NOT_FOUND, "unknown scene %d", id);
-    cudaStreamSynchronize(ctx->stream);
+    spare_put(ctx, std::move(it->second->mem));   // reused in stream order, freed only when spares overflow
     ctx->scenes.erase(it);
     return RT_OK;
 }
@@ -552,6 +647,7 @@ int frame_alloc(rt_ctx *ctx, int32_t w, int32_t h, FrameDev &f)
     };
     const size_t o_acc = take(24 * np), o_rgb = take(12 * np), o_rgb8 = take(3 * np), o_po = take(4 * np),
                  o_pp = take(4 * np), o_pt = take(4 * np);
+    spare_take(ctx, f.mem, off);
     CK(ctx, f.mem.ensure(off));
     char *b = (char *)f.mem.p;
     f.w = w, f.h = h;
@@ -584,7 +680,7 @@ extern "C" int rt_frame_release(rt_ctx *ctx, int32_t id)
     if (!ctx) return RT_ERR_INVALID;
     auto it = ctx->frames.find(id);
     if (it == ctx->frames.end()) return ctx_fail(ctx, RT_ERR_NOT_FOUND, "unknown frame %d", id);
-    cudaStreamSynchronize(ctx->stream);
+    spare_put(ctx, std::move(it->second->mem));
     ctx->frames.erase(it);
     return RT_OK;
 }

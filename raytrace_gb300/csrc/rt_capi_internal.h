@@ -214,11 +214,19 @@ struct rt_ctx {
     void *plain_graph_ws = nullptr;      // workspace the plain graphs point into
     void *plain_stage = nullptr;         // page-locked staging of the plain job tables
     cudaEvent_t ev_staged = nullptr;     // the last staging copy
+    std::vector<DevBuf> spare;           // released scene / frame buffers kept for reuse
+    void *upload_stage = nullptr;        // page-locked staging of a scene upload's small tables
+    size_t upload_stage_bytes = 0;
+    cudaEvent_t ev_upload = nullptr;     // the last upload's staging copy
+    int *build_flag = nullptr;           // page-locked: the LBVH build's material check
 };
 
 int ctx_fail(rt_ctx *ctx, int code, const char *fmt, ...);
 // clear the cancel flag for a render about to be enqueued on the context stream
 int cancel_arm(rt_ctx *ctx);
+// released scene / frame buffers the context keeps for reuse: their bytes, and freeing them
+size_t spare_bytes(const rt_ctx *ctx);
+void spare_trim(rt_ctx *ctx);
 #define CK(ctx, call)                                                                                             \
     do {                                                                                                          \
         cudaError_t e_ = (call);                                                                                  \

@@ -290,7 +290,12 @@ __global__ void k_gather(LbvhInput in, LbvhOutput out, const unsigned *perm, con
         if (i < in.n) {
             out.tri[3ll * k] = make_float4(w.p0[0], w.p0[1], w.p0[2], __int_as_float(in.tri_id[i]));
             out.tri[3ll * k + 1] = make_float4(w.e1[0], w.e1[1], w.e1[2], __int_as_float(in.tri_obj[i]));
-            out.tri[3ll * k + 2] = make_float4(w.e2[0], w.e2[1], w.e2[2], __int_as_float(in.tri_mtl[i]));
+            int m = in.tri_mtl[i];
+            if (in.bad && (m < 0 || m >= in.n_mtl)) {   // rejected by the caller; never read out of range
+                atomicOr(in.bad, 1);
+                m = 0;
+            }
+            out.tri[3ll * k + 2] = make_float4(w.e2[0], w.e2[1], w.e2[2], __int_as_float(m));
             const float *nn = in.tri_n + 9ll * i;
             for (int j = 0; j < 3; ++j) out.trin[3ll * k + j] = make_float4(nn[3 * j], nn[3 * j + 1], nn[3 * j + 2], 0.0f);
             if (out.triuv) {
@@ -472,6 +477,13 @@ cudaError_t morton_and_sort(const LbvhInput &in, const Scratch &sc, cudaStream_t
     cudaMemsetAsync(sc.box + 3, 0, 12, s);
     k_prep<<<grid_of(n, 256), 256, 0, s>>>(in, sc.centroid, sc.box);
     k_morton<<<grid_of(n, 256), 256, 0, s>>>(n, sc.centroid, sc.box, sc.codes[0], sc.idx[0]);
+    {
+        const cudaError_t r = cudaGetLastError();
+        if (r != cudaSuccess) {
+            g_build_step = "Morton codes";
+            return r;
+        }
+    }
     for (int pass = 0; pass < 4; ++pass) {
         const int src = pass & 1, dst = src ^ 1;
         k_hist<<<tiles, kSortThreads, 0, s>>>(n, sc.codes[src], 8 * pass, sc.hist, tiles);
@@ -481,8 +493,13 @@ cudaError_t morton_and_sort(const LbvhInput &in, const Scratch &sc, cudaStream_t
         k_scan_down<<<chunks, kScanThreads, 0, s>>>(sc.hist, m, sc.part);
         k_scatter<<<tiles, kSortThreads, 0, s>>>(n, sc.codes[src], sc.idx[src], sc.codes[dst], sc.idx[dst], 8 * pass,
                                                  sc.hist, tiles);
+        const cudaError_t r = cudaGetLastError();
+        if (r != cudaSuccess) {
+            g_build_step = "radix sort";
+            return r;
+        }
     }
-    return cudaGetLastError();
+    return cudaSuccess;
 }
 
 } // namespace
@@ -526,6 +543,8 @@ cudaError_t lbvh_morton_sort(const LbvhInput &in, uint32_t *codes_out, uint32_t 
     return cudaGetLastError();
 }
 
+const char *g_build_step = "";   // the build step that failed last (diagnostics)
+
 cudaError_t lbvh_build(const LbvhInput &in, const LbvhOutput &out, void *scratch, cudaStream_t s)
 {
     const int n = in.n + in.n_sph;
@@ -533,14 +552,23 @@ cudaError_t lbvh_build(const LbvhInput &in, const LbvhOutput &out, void *scratch
     Scratch sc = carve(scratch, n);
     cudaError_t e = morton_and_sort(in, sc, s);
     if (e != cudaSuccess) return e;
+    auto step = [&](const char *name) {
+        cudaError_t r = cudaGetLastError();
+        if (r != cudaSuccess) g_build_step = name;
+        return r;
+    };
     k_gather<<<grid_of(n, 256), 256, 0, s>>>(in, out, sc.idx[0], sc.box);
+    if ((e = step("gather")) != cudaSuccess) return e;
     if (n > 1) {
         k_karras<<<grid_of(n - 1, 256), 256, 0, s>>>(n, sc.codes[0], out.nodes, sc.parent);
+        if ((e = step("hierarchy")) != cudaSuccess) return e;
         cudaMemsetAsync(sc.flags, 0, 4 * (size_t)(n - 1), s);
         k_refit<<<grid_of(n, 256), 256, 0, s>>>(n, out.nodes, sc.parent, sc.flags);
+        if ((e = step("refit")) != cudaSuccess) return e;
         if (out.quads) k_quads<<<grid_of(n - 1, 256), 256, 0, s>>>(n, out.nodes, out.quads);
+        if ((e = step("4-wide nodes")) != cudaSuccess) return e;
     }
-    return cudaGetLastError();
+    return cudaSuccess;
 }
 
 } // namespace rtg

@@ -22,6 +22,10 @@ struct LbvhInput {
     const int *sph_prim;   // analytic primitive index = the hit key
     const int *sph_obj;    // object order
     int n_sph;
+    // material check of the gather: a triangle material outside [0, n_mtl) sets *bad (NULL =
+    // no check); the caller rejects the scene
+    int n_mtl;
+    int *bad;
 };
 
 // leaves = n + n_sph; leaf record k (Morton order), 3 float4:
@@ -34,6 +38,9 @@ struct LbvhOutput {
     float4 *trin;    // 3L (vertex normals; zero for spheres)
     float2 *triuv;   // 3L or NULL
 };
+
+// name of the build step whose launch failed last (for error messages)
+extern const char *g_build_step;
 
 // scratch bytes needed for n leaves (triangles + spheres)
 size_t lbvh_scratch_bytes(int n);

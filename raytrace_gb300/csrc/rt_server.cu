@@ -140,7 +140,8 @@ static int srv_fail(rt_server *srv, int code, const char *fmt, ...)
 
 static int64_t used_bytes(const rt_server *srv)
 {
-    int64_t b = srv->fixed_bytes + srv->plain_frame_bytes + (int64_t)srv->ctx->lbvh_scratch.bytes;
+    int64_t b = srv->fixed_bytes + srv->plain_frame_bytes + (int64_t)srv->ctx->lbvh_scratch.bytes +
+                (int64_t)spare_bytes(srv->ctx);
     for (const SrvScene &s : srv->scenes)
         if (s.ctx_id >= 0) b += s.bytes;
     return b;
@@ -179,6 +180,10 @@ static int make_resident(rt_server *srv, int k, int *rebuilt)
         return used_bytes(srv) + s.bytes + std::max<int64_t>(0, s.scratch - (int64_t)srv->ctx->lbvh_scratch.bytes);
     };
     while (need() > budget) {
+        if (spare_bytes(srv->ctx) > 0) {   // released buffers the context keeps go first
+            spare_trim(srv->ctx);
+            continue;
+        }
         SrvScene *victim = nullptr;
         for (SrvScene &o : srv->scenes)
             if (o.ctx_id >= 0 && o.users == 0 && (!victim || o.last_use < victim->last_use)) victim = &o;
@@ -656,6 +661,10 @@ int rt_server_add_scene(rt_server *srv, const rt_scene_desc *desc, int32_t *scen
     srv->scenes.push_back(s);
     // over the budget: evict idle scenes, oldest first (the new one last)
     while (used_bytes(srv) > srv->cfg.hbm_budget_bytes) {
+        if (spare_bytes(ctx) > 0) {
+            spare_trim(ctx);
+            continue;
+        }
         SrvScene *victim = nullptr;
         for (SrvScene &o : srv->scenes)
             if (o.ctx_id >= 0 && o.users == 0 && (!victim || o.last_use < victim->last_use)) victim = &o;

@@ -251,3 +251,18 @@ def test_render_modes_full_frame_match_oracle(ctx, mode):
     a = ref["ambiguous"]
     d = np.abs(out["rgb"] - ref["rgb"]).max(axis=2)
     assert not ((d > TOL) & ~a).any(), (mode, float(d[~a].max()))
+
+
+def test_out_of_range_triangle_material_is_rejected(ctx):
+    """The LBVH build checks every triangle's material index on the device; the upload fails."""
+    scene = rt.SceneHost.small(seed=40, n_spheres=2, ico_freq=3, width=32, height=32, refractive_every=0)
+    d = scene.desc
+    assert d.n_tris > 0
+    d.tri_mtl[5] = d.n_materials + 7
+    with pytest.raises(rt.RTError) as e:
+        ctx.upload(scene)
+    assert e.value.code == rt.RT_ERR_INVALID
+    d.tri_mtl[5] = 0
+    sid = ctx.upload(scene)   # a valid scene still uploads
+    ctx.release_scene(sid)
+

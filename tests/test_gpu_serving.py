@@ -169,9 +169,11 @@ def test_server_lru_eviction_and_rebuild(ctx):
             want.append(big.result(rid)["rgb"])
         assert big.stats()["evictions"] == 0
     srt = sorted(sizes)
+    ctx.release_cached()   # buffers kept from earlier releases would count against the budget
     with rt.Server(ctx, 64 << 30, max_inflight=2, max_pixels=96 * 96) as probe:
         base = probe.stats()["peak_bytes"]   # slots + queues + LBVH scratch
     budget = base + srt[-1] + srt[-2] + srt[0] // 2   # the two largest fit together, all four never
+    ctx.release_cached()
     with rt.Server(ctx, budget, max_inflight=2, max_pixels=96 * 96) as small:
         ids = [small.add_scene(s) for s in scenes]
         assert sum(small.resident(i) for i in ids) < 4
