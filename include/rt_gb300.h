@@ -180,7 +180,7 @@ int         rt_ctx_synchronize(rt_ctx *ctx);
 int         rt_ctx_set_stream(rt_ctx *ctx, void *cuda_stream);
 /* Released scene and frame buffers stay with the context (at most 4, 8 GB) and are reused by
  * the next upload or frame that fits, saving a cudaMalloc / cudaFree per scene and frame;
- * this frees them now. */
+ * this frees them now, together with the batch path's wave workspace (up to 31 GB). */
 int rt_ctx_release_cached(rt_ctx *ctx);
 
 /* ---- scenes: upload + device LBVH build (replaces RTPrepare, Model.cpp:402-480) ------ */
@@ -236,7 +236,7 @@ typedef struct rt_batch_tuning {
     int32_t min_blocks;          /* 0, 6, 8, 10 or 12: resident 128-thread blocks per SM the register
                                     budget of the traversal kernels must allow (0 = compiler's) */
     int32_t dynamic;             /* 0 or 1: pull ray tiles from a counter; 2: static grid stride */
-    int64_t wave_rays;           /* batch: ray-queue entries of one wave (0 = 2^24) */
+    int64_t wave_rays;           /* batch: ray-queue entries of one wave (0 = 2^26) */
 } rt_batch_tuning;
 
 /* kernel tuning of the plain per-scene path (rt_render); NULL restores the defaults */

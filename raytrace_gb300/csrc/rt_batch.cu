@@ -24,6 +24,11 @@ WaveRunner::~WaveRunner()
         }
         if (st.jobs) cudaFreeHost(st.jobs);
     }
+    if (ftab_copied) {
+        cudaEventSynchronize(ftab_copied);
+        cudaEventDestroy(ftab_copied);
+    }
+    if (ftab_host) cudaFreeHost(ftab_host);
 }
 
 // A sample's rays at bounce l number at most b^l (b = children per hit, one queue holds one
@@ -34,7 +39,7 @@ long long wave_weight(int branching, int max_level)
     return branching >= 2 ? 1ll << max_level : 1ll;
 }
 
-size_t wave_runner_bytes(const WaveRunner &R) { return R.ws.mem.bytes; }
+size_t wave_runner_bytes(const WaveRunner &R) { return R.ws.mem.bytes + R.ftab_dev.bytes; }
 
 static int stage_harvest(rt_ctx *ctx, WaveRunner &R, WaveStage &st, bool wait)
 {
@@ -195,9 +200,10 @@ int wave_enqueue(rt_ctx *ctx, WaveRunner &R, const std::vector<WaveJob *> &jobs,
 // ---- batch ---------------------------------------------------------------------------------------------------
 
 namespace {
-// ray-queue entries of one batch wave by default: 2^24 entries hold 232 B each (two ray
-// queues, shadow queue, hit record)
-constexpr long long kBatchQueue = 1ll << 24;
+// ray-queue entries of one batch wave by default: 2^26 entries of 232 B each (two ray queues,
+// shadow queue, hit record), 15.6 GB. Fewer, larger waves pay each bounce's tail (the longest
+// ray of the pass) fewer times.
+constexpr long long kBatchQueue = 1ll << 26;
 } // namespace
 
 // RT_FLAG_PROFILE on any job: launches go without the graph, bracketed by events per kernel
@@ -241,11 +247,29 @@ static int batch_core(rt_ctx *ctx, int32_t n, const int32_t *scene_ids, const in
     if (rc) return rc;
     R.rays_primary = R.rays_secondary = R.rays_shadow = 0;
     R.overflow = R.error = 0;
-    CK(ctx, cudaEventRecord(ctx->ev_start, s));
-    for (int i = 0; i < n; ++i) {
-        CK(ctx, cudaMemsetAsync(frames[i]->fb.acc, 0, 24 * (size_t)frames[i]->w * frames[i]->h, s));
-        if (jobs[i].job.plane_obj) launch_plane_init(frames[i]->fb, (long long)frames[i]->w * frames[i]->h, s);
+    // the frame table; its pinned host copy is rewritten once the previous copy out of it ran
+    if (!R.ftab_copied) CK(ctx, cudaEventCreateWithFlags(&R.ftab_copied, cudaEventDisableTiming));
+    CK(ctx, cudaEventSynchronize(R.ftab_copied));
+    if (R.ftab_cap < n) {
+        if (R.ftab_host) cudaFreeHost(R.ftab_host);
+        R.ftab_host = nullptr;
+        R.ftab_cap = 0;
+        CK(ctx, cudaMallocHost((void **)&R.ftab_host, sizeof(FrameJob) * (size_t)n));
+        R.ftab_cap = n;
     }
+    CK(ctx, R.ftab_dev.ensure(sizeof(FrameJob) * (size_t)n));
+    long long quads = 0;
+    for (int i = 0; i < n; ++i) {
+        FrameJob &F = R.ftab_host[i];
+        F = frame_job(frames[i]->fb, frames[i]->w, frames[i]->h, jobs[i].job);
+        quads += F.quad_end;
+        F.quad_end = quads;
+    }
+    const FrameJob *ftab = (const FrameJob *)R.ftab_dev.p;
+    CK(ctx, cudaEventRecord(ctx->ev_start, s));
+    CK(ctx, cudaMemcpyAsync(R.ftab_dev.p, R.ftab_host, sizeof(FrameJob) * (size_t)n, cudaMemcpyHostToDevice, s));
+    CK(ctx, cudaEventRecord(R.ftab_copied, s));
+    launch_frames_prepare(ftab, n, quads, s);
     std::vector<WaveJob *> order((size_t)n);
     for (int i = 0; i < n; ++i) order[i] = &jobs[i];
     for (;;) {
@@ -255,7 +279,7 @@ static int batch_core(rt_ctx *ctx, int32_t n, const int32_t *scene_ids, const in
         if (!got) break;
     }
     if (P) P->begin(RT_KERNEL_RESOLVE, s);
-    for (int i = 0; i < n; ++i) launch_resolve(frames[i]->fb, frames[i]->w, frames[i]->h, rds[i].spp, s);
+    launch_frames_resolve(ftab, n, quads, s);
     if (P) P->end(s);
     CK(ctx, cudaGetLastError());
     CK(ctx, cudaEventRecord(ctx->ev_stop, s));
@@ -316,20 +340,32 @@ extern "C" int rt_batch_autotune(rt_ctx *ctx, int32_t n, const int32_t *scene_id
     // tile 0 stands for the static grid stride; the stack depth is fixed (kStack)
     const int shapes[][2] = {{128, 8}, {128, 6}, {64, 8}, {256, 0}};
     const int tiles[] = {0, 32, 64, 128, 256};
+    // then the wave size (ray-queue entries per wave) for the best shape
+    const long long waves[] = {1ll << 25, 1ll << 27};
     double best = 1e30;
     rt_batch_tuning best_t{128, 32, 0, 1, 8, 1, 0};
+    auto trial = [&](const rt_batch_tuning &t) {
+        int rc = rt_batch_render(ctx, n, scene_ids, frame_ids, rds, &t);   // warm (captures the graph)
+        if (rc) return rc;
+        auto t0 = std::chrono::steady_clock::now();
+        rc = rt_batch_render(ctx, n, scene_ids, frame_ids, rds, &t);
+        if (rc) return rc;
+        cudaStreamSynchronize(ctx->stream);
+        double dt = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        if (dt < best) best = dt, best_t = t;
+        return RT_OK;
+    };
     for (const auto &sh : shapes)
         for (int tl : tiles) {
-            rt_batch_tuning t{sh[0], tl ? tl : 32, 0, 1, sh[1], tl ? 1 : 2, 0};
-            int rc = rt_batch_render(ctx, n, scene_ids, frame_ids, rds, &t);   // warm (captures the graph)
+            int rc = trial(rt_batch_tuning{sh[0], tl ? tl : 32, 0, 1, sh[1], tl ? 1 : 2, 0});
             if (rc) return rc;
-            auto t0 = std::chrono::steady_clock::now();
-            rc = rt_batch_render(ctx, n, scene_ids, frame_ids, rds, &t);
-            if (rc) return rc;
-            cudaStreamSynchronize(ctx->stream);
-            double dt = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
-            if (dt < best) best = dt, best_t = t;
         }
+    for (long long w : waves) {
+        rt_batch_tuning t = best_t;
+        t.wave_rays = w;
+        int rc = trial(t);
+        if (rc) return rc;
+    }
     *out = best_t;
     return RT_OK;
 }

@@ -199,6 +199,10 @@ extern "C" int rt_ctx_release_cached(rt_ctx *ctx)
 {
     if (!ctx) return RT_ERR_INVALID;
     spare_trim(ctx);
+    if (ctx->batch) {
+        CK(ctx, cudaStreamSynchronize(ctx->stream));
+        ctx->batch.reset();
+    }
     return RT_OK;
 }
 
@@ -646,7 +650,7 @@ int frame_alloc(rt_ctx *ctx, int32_t w, int32_t h, FrameDev &f)
         return o;
     };
     const size_t o_acc = take(24 * np), o_rgb = take(12 * np), o_rgb8 = take(3 * np), o_po = take(4 * np),
-                 o_pp = take(4 * np), o_pt = take(4 * np);
+                 o_pp = take(4 * np), o_pt = take(4 * np), o_ax = take(4 * ((size_t)w + h));
     spare_take(ctx, f.mem, off);
     CK(ctx, f.mem.ensure(off));
     char *b = (char *)f.mem.p;
@@ -657,6 +661,7 @@ int frame_alloc(rt_ctx *ctx, int32_t w, int32_t h, FrameDev &f)
     f.fb.plane_obj = (int *)(b + o_po);
     f.fb.plane_prim = (int *)(b + o_pp);
     f.fb.plane_t = (float *)(b + o_pt);
+    f.fb.axis = (float *)(b + o_ax);
     f.bytes = (int64_t)off;
     return RT_OK;
 }
@@ -796,6 +801,7 @@ int make_job(rt_ctx *ctx, const SceneDev &sc, FrameDev &f, const rt_render_desc 
     J.xlim = (rd->flags & RT_FLAG_REF_TILES) ? (W / 64) * 64 : W;
     J.ylim = (rd->flags & RT_FLAG_REF_TILES) ? (H / 64) * 64 : H;
     J.acc = f.fb.acc;
+    J.axis = rd->spp == 1 ? f.fb.axis : nullptr;
     if (rd->flags & RT_FLAG_HIT_PLANES) {
         J.plane_obj = f.fb.plane_obj, J.plane_prim = f.fb.plane_prim, J.plane_t = f.fb.plane_t;
     }
@@ -812,6 +818,19 @@ int make_job(rt_ctx *ctx, const SceneDev &sc, FrameDev &f, const rt_render_desc 
     return RT_OK;
 }
 
+FrameJob frame_job(const FrameBufs &fb, int w, int h, const DevJob &J)
+{
+    FrameJob F{};
+    F.fb = fb;
+    F.npix = (long long)w * h;
+    F.quad_end = (F.npix + 3) / 4;
+    F.scale_bits = resolve_scale_bits(J.spp);
+    if (J.axis) std::memcpy(&F.dp_bits, &J.dp, sizeof F.dp_bits);
+    F.w = w, F.h = h;
+    F.planes = J.plane_obj != nullptr;
+    return F;
+}
+
 // enqueue the level loop of one wave whose jobs are already in the workspace
 void enqueue_levels(rt_ctx *ctx, Workspace &ws, int max_level, const Tuning &t, cudaStream_t s, KernelProfiler *prof)
 {
@@ -822,14 +841,10 @@ void enqueue_levels(rt_ctx *ctx, Workspace &ws, int max_level, const Tuning &t, 
     auto E = [&]() {
         if (prof) prof->end(s);
     };
-    const int raygen_grid = sm_count() * 8;
-    B(RT_KERNEL_RAYGEN);
-    launch_raygen(ws.wf, raygen_grid, 256, s);
-    E();
     for (int level = 0; level <= max_level; ++level) {
         const int sel = level & 1;
         B(RT_KERNEL_EXTEND);
-        launch_extend(ws.wf, sel, level, t, s);
+        launch_extend(ws.wf, sel, level, level == 0, t, s);
         E();
         B(RT_KERNEL_SHADE);
         launch_shade(ws.wf, sel, level, t, s);
@@ -904,15 +919,12 @@ static int render_once(rt_ctx *ctx, SceneDev &sc, FrameDev &f, const rt_render_d
     CK(ctx, cudaEventRecord(ctx->ev_start, s));
     CK(ctx, cudaMemcpyAsync(dst, st, span, cudaMemcpyHostToDevice, s));
     CK(ctx, cudaEventRecord(ctx->ev_staged, s));
-    CK(ctx, cudaMemsetAsync(f.fb.acc, 0, 24 * (size_t)f.w * f.h, s));
     KernelProfiler &P = ctx->prof;
     const bool profile = (rd->flags & RT_FLAG_PROFILE) != 0;
     P.reset(profile);
-    if (rd->flags & RT_FLAG_HIT_PLANES) {
-        P.begin(RT_KERNEL_OTHER, s);
-        launch_plane_init(f.fb, (long long)f.w * f.h, s);
-        P.end(s);
-    }
+    P.begin(RT_KERNEL_OTHER, s);
+    launch_frame_prepare(frame_job(f.fb, f.w, f.h, J), s);
+    P.end(s);
     Tuning t = ctx->plain_tuning;
     t.count = (rd->flags & RT_FLAG_COUNT_WORK) != 0;
     if (profile) {   // kernels one by one between events
@@ -924,7 +936,6 @@ static int render_once(rt_ctx *ctx, SceneDev &sc, FrameDev &f, const rt_render_d
         if (rc) return rc;
         CK(ctx, cudaGraphLaunch(exec, s));
         // launches of the captured sequence, as the profiler would count them
-        P.launches[RT_KERNEL_RAYGEN] = 1;
         P.launches[RT_KERNEL_EXTEND] = P.launches[RT_KERNEL_SHADE] = P.launches[RT_KERNEL_SHADOW] = rd->max_level + 1;
     }
     P.begin(RT_KERNEL_RESOLVE, s);

@@ -170,6 +170,12 @@ struct WaveRunner {
     unsigned long long rays_primary = 0, rays_secondary = 0, rays_shadow = 0;
     int overflow = 0, error = 0;
     long long waves = 0, wave_jobs = 0;
+    // frame table of a batch (pinned host copy, device copy): prepared and resolved in one
+    // launch each
+    rtg::FrameJob *ftab_host = nullptr;
+    DevBuf ftab_dev;
+    int ftab_cap = 0;
+    cudaEvent_t ftab_copied = nullptr;   // the last copy out of ftab_host has run
     WaveRunner() = default;
     WaveRunner(const WaveRunner &) = delete;
     WaveRunner &operator=(const WaveRunner &) = delete;
@@ -240,6 +246,8 @@ int frame_alloc(rt_ctx *ctx, int32_t w, int32_t h, FrameDev &f);
 int ws_ensure(rt_ctx *ctx, Workspace &ws, long long qcap, int njobs);
 int make_job(rt_ctx *ctx, const SceneDev &sc, FrameDev &f, const rt_render_desc *rd, int scene_slot, rtg::DevJob &J,
              long long &samples);
+// the preparation / resolve record of a frame rendered by job J (w x h pixels)
+rtg::FrameJob frame_job(const rtg::FrameBufs &fb, int w, int h, const rtg::DevJob &J);
 // raygen + (extend, shade, shadow) per level; `prof` (may be NULL) brackets every launch
 int tuning_from(rt_ctx *ctx, const rt_batch_tuning *in, rtg::Tuning &t);
 void enqueue_levels(rt_ctx *ctx, Workspace &ws, int max_level, const rtg::Tuning &t, cudaStream_t s,

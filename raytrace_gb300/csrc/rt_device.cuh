@@ -123,6 +123,7 @@ struct DevJob {
     int *plane_obj;               // primary hit planes of sample 0 (NULL = not written)
     int *plane_prim;
     float *plane_t;
+    const float *axis;            // camera offsets per column, then per row (1 sample/pixel; NULL = computed)
     long long sample_base;        // first global sample index of this job
     float cam_pos[3], cam_u[3], cam_v[3], cam_n[3];
     double dp;                    // tan(fovy*pi/360) / (H/2) in double (RayTracer.cpp:14)

@@ -108,83 +108,136 @@ __device__ __forceinline__ void for_each_ray_guided(int n, int *work, int tile, 
 __device__ __forceinline__ bool cancelled(const volatile int *cancel) { return cancel && *cancel; }
 
 // ---- ray generation (parallelRT, RayTracer.cpp:13-27) -------------------------------------
-__global__ void k_raygen(Wavefront wf)
+// Primary rays are made inside the first extend pass, in registers: a ray queue entry is
+// written only for a ray that hits something, which is what shading reads.
+
+// the job that holds global sample gs. Lane 0 searches for the first sample of the warp's 32
+// (base), the lanes walk on from there: 32 consecutive samples span few jobs. All lanes call.
+__device__ __forceinline__ int job_of(const Wavefront &wf, long long gs, long long base, bool active)
 {
-    if (cancelled(wf.cancel)) return;
-    const long long total = *wf.total_samples, first = *wf.sample_offset;
-    const RayQueue q = wf.q[0];
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-        wf.C->q_count[0] = (int)min(total, (long long)q.capacity);
-        wf.C->rays_primary = (unsigned long long)total;
-        if (total > q.capacity) atomicExch(&wf.C->overflow, 1);
-    }
-    for (long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x; g < total && g < q.capacity;
-         g += (long long)gridDim.x * blockDim.x) {
-        const long long gs = first + g;
+    int j = 0;
+    if ((threadIdx.x & 31) == 0) {
         int lo = 0, hi = (int)*wf.n_jobs - 1;
         while (lo < hi) {
-            int mid = (lo + hi) >> 1;
-            if (wf.job_sample_end[mid] > gs) hi = mid;
+            const int mid = (lo + hi) >> 1;
+            if (wf.job_sample_end[mid] > base) hi = mid;
             else lo = mid + 1;
         }
-        const DevJob &J = wf.jobs[lo];
-        long long local = gs - J.sample_base;
-        long long p = local / J.spp;
-        int s = (int)(local - p * J.spp);
-        int row = (int)(p / J.xlim), col = (int)(p - (long long)row * J.xlim);
-        int xcur = col - J.width / 2, ycur = row - J.height / 2;
-        float a, b;
-        if (J.spp > 1) {   // sub-pixel jitter in [0,1) from a per-pixel Philox stream
-            unsigned pix = (unsigned)(row * J.width + col);
-            uint4 r = philox4x32_10(make_uint4(pix, 0u, (unsigned)s, 0u),
-                                    make_uint2((unsigned)J.seed, (unsigned)(J.seed >> 32)));
-            // (float)(((double)xcur + (r >> 8) * 2^-24) * dp): the sum is exact in 38 bits, so it
-            // is the integer xcur * 2^24 + (r >> 8) times dp * 2^-24
-            DSplit d = split_double_bits((unsigned long long)__double_as_longlong(J.dp));
-            d.e -= 24;
-            a = dmul_to_float((long long)xcur * 16777216ll + (long long)(r.x >> 8), d);
-            b = dmul_to_float((long long)ycur * 16777216ll + (long long)(r.y >> 8), d);
-        } else {   // (float)((double)xcur * dp)
-            const DSplit d = split_double_bits((unsigned long long)__double_as_longlong(J.dp));
-            a = dmul_to_float(xcur, d);
-            b = dmul_to_float(ycur, d);
-        }
-        V3 n = mk(J.cam_n[0], J.cam_n[1], J.cam_n[2]);
-        V3 u = mk(J.cam_u[0], J.cam_u[1], J.cam_u[2]);
-        V3 v = mk(J.cam_v[0], J.cam_v[1], J.cam_v[2]);
-        V3 dir = normalise(vadd(vadd(n, vscale(u, a)), vscale(v, b)));
-        int pixel = row * J.width + col;
-        if (J.mode == kModeCheck && ((row >> 6) & 1) == ((col >> 6) & 1))   // RTcheck: white 64x64 tiles
-            acc_add(J.acc, pixel, mk(1.0f, 1.0f, 1.0f));
-        q.o[g] = make_float4(J.cam_pos[0], J.cam_pos[1], J.cam_pos[2], 1.0f);
-        q.d[g] = make_float4(dir.x, dir.y, dir.z, 1.0f);
-        q.w[g] = make_float4(1.0f, 1.0f, 1.0f, __int_as_float(pixel));
-        q.m[g] = make_int4(-1, ray_flags(0, kRayBase, 0, s == 0 && J.plane_obj != nullptr), -1, lo);
+        j = lo;
     }
+    j = __shfl_sync(kFull, j, 0);
+    // ends: the last job's end is the number of samples of all jobs, above any active gs
+    if (active)
+        while (wf.job_sample_end[j] <= gs) ++j;
+    return j;
+}
+
+struct PrimaryRay {
+    V3 o, d;
+    int pixel, row, col;
+    int sample;   // sample index within the pixel
+};
+
+// camera ray of the job's sample `local` (pixel-major: local = pixel * spp + sample)
+__device__ __forceinline__ PrimaryRay primary_ray(const DevJob &J, long long local)
+{
+    PrimaryRay r;
+    long long p;
+    int s;
+    if (J.spp == 1) {
+        p = local;
+        s = 0;
+    } else if (local < (1ll << 32)) {   // 32-bit division where it suffices
+        const unsigned q = (unsigned)local / (unsigned)J.spp;
+        p = q;
+        s = (int)((unsigned)local - q * (unsigned)J.spp);
+    } else {
+        p = local / J.spp;
+        s = (int)(local - p * J.spp);
+    }
+    // p < 2^28: frames are at most 16384 x 16384
+    const unsigned row = (unsigned)p / (unsigned)J.xlim, col = (unsigned)p - row * (unsigned)J.xlim;
+    const int xcur = (int)col - J.width / 2, ycur = (int)row - J.height / 2;
+    float a, b;
+    DSplit d = split_double_bits((unsigned long long)__double_as_longlong(J.dp));
+    if (J.axis) {   // one sample per pixel: the offsets of the frame's table
+        a = J.axis[col];
+        b = J.axis[J.width + row];
+    } else if (J.spp > 1) {   // sub-pixel jitter in [0,1) from a per-pixel Philox stream
+        const unsigned pix = row * (unsigned)J.width + col;
+        const uint4 x = philox4x32_10(make_uint4(pix, 0u, (unsigned)s, 0u),
+                                      make_uint2((unsigned)J.seed, (unsigned)(J.seed >> 32)));
+        // (float)(((double)xcur + (x >> 8) * 2^-24) * dp): the sum is exact in 38 bits, so it
+        // is the integer xcur * 2^24 + (x >> 8) times dp * 2^-24
+        d.e -= 24;
+        a = dmul_to_float((long long)xcur * 16777216ll + (long long)(x.x >> 8), d);
+        b = dmul_to_float((long long)ycur * 16777216ll + (long long)(x.y >> 8), d);
+    } else {   // (float)((double)xcur * dp)
+        a = dmul_to_float(xcur, d);
+        b = dmul_to_float(ycur, d);
+    }
+    const V3 n = mk(J.cam_n[0], J.cam_n[1], J.cam_n[2]);
+    const V3 u = mk(J.cam_u[0], J.cam_u[1], J.cam_u[2]);
+    const V3 v = mk(J.cam_v[0], J.cam_v[1], J.cam_v[2]);
+    r.d = normalise(vadd(vadd(n, vscale(u, a)), vscale(v, b)));
+    r.o = mk(J.cam_pos[0], J.cam_pos[1], J.cam_pos[2]);
+    r.pixel = (int)(row * (unsigned)J.width + col);
+    r.row = (int)row, r.col = (int)col;
+    r.sample = s;
+    return r;
 }
 
 // ---- extend: closest hit -------------------------------------------------------------------
-// MINB > 0 caps registers so MINB blocks of 128 threads fit on an SM
-template <int STACK, bool DYN, bool COUNT, int MINB>
+// MINB > 0 caps registers so MINB blocks of 128 threads fit on an SM. GEN: the first pass of a
+// wave, which makes its primary rays instead of reading a queue.
+template <int STACK, bool DYN, bool COUNT, int MINB, bool GEN>
 __global__ void __launch_bounds__(MINB ? 128 : 256, MINB ? MINB : 1) k_extend(Wavefront wf, int sel, int wslot, int tile)
 {
     Counters *C = wf.C;
+    const RayQueue q = wf.q[sel];
+    const long long total = GEN ? *wf.total_samples : 0, first = GEN ? *wf.sample_offset : 0;
     if (blockIdx.x == 0 && threadIdx.x == 0) {   // the next queue and the shadow queue fill in shade
         C->q_count[sel ^ 1] = 0;
         C->s_count = 0;
+        if (GEN) {
+            C->q_count[sel] = (int)min(total, (long long)q.capacity);
+            C->rays_primary = (unsigned long long)total;
+            if (total > q.capacity) atomicExch(&C->overflow, 1);
+        }
     }
     if (cancelled(wf.cancel)) return;
-    const RayQueue q = wf.q[sel];
-    const int n = min(C->q_count[sel], q.capacity);
+    const int n = GEN ? (int)min(total, (long long)q.capacity) : min(C->q_count[sel], q.capacity);
     WorkCount wc{0, 0, 0, 0};
     const int level = wslot / 3;
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
     for_each_ray<DYN>(n, &C->work[wslot], tile, [&](int i, bool active) {
         bool is_hit = false;
-        if (active) {
-            float4 o4 = q.o[i], d4 = q.d[i];
-            int4 m4 = q.m[i];
+        if constexpr (GEN) {
+            const int job = job_of(wf, first + i, first + (i - lane), active);
+            if (active) {
+                const DevJob &J = wf.jobs[job];
+                const PrimaryRay pr = primary_ray(J, first + i - J.sample_base);
+                if (J.mode == kModeCheck && ((pr.row >> 6) & 1) == ((pr.col >> 6) & 1))
+                    acc_add(J.acc, pr.pixel, mk(1.0f, 1.0f, 1.0f));   // RTcheck: white 64x64 tiles
+                const int plane = pr.sample == 0 && J.plane_obj != nullptr;
+                const DevScene &S = wf.scenes[J.scene];
+                Best best;
+                int newobj;
+                closest_hit<STACK, COUNT>(S, pr.o, pr.d, -1, false, best, newobj, wc);
+                is_hit = best.key >= 0;
+                if (is_hit) {   // shading reads hits only
+                    wf.hit[i] = make_float4(best.t, best.u, best.v, __int_as_float(best.key));
+                    wf.newobj[i] = newobj;
+                    q.o[i] = make_float4(pr.o.x, pr.o.y, pr.o.z, 1.0f);
+                    q.d[i] = make_float4(pr.d.x, pr.d.y, pr.d.z, 1.0f);
+                    q.w[i] = make_float4(1.0f, 1.0f, 1.0f, __int_as_float(pr.pixel));
+                    q.m[i] = make_int4(-1, ray_flags(0, kRayBase, 0, plane), -1, job);
+                }
+            }
+        } else if (active) {
+            const float4 o4 = q.o[i], d4 = q.d[i];
+            const int4 m4 = q.m[i];
             const DevScene &S = wf.scenes[wf.jobs[m4.w].scene];
             Best best;
             int newobj;
@@ -614,22 +667,113 @@ __device__ __forceinline__ uint8_t put_channel(float c)
     return (uint8_t)(int)(c * 255);
 }
 // colour = (float)((double)acc * scale), scale = 2^-32 / spp in double (split on the host)
+__device__ __forceinline__ float resolve_channel(long long a, DSplit scale) { return a ? dmul_to_float(a, scale) : 0.0f; }
+
+// pixels 4q .. 4q+3 of a frame: 96 B of accumulator in six 16-B loads, 48 B of colour in three
+// 16-B stores, 12 B of bytes in three 4-B stores (frame buffers are 256-B aligned); a partial
+// last quad goes pixel by pixel
+__device__ __forceinline__ void resolve_quad(const FrameBufs &fb, long long q, long long npix, DSplit scale)
+{
+    if (4 * q + 4 > npix) {
+        for (long long p = 4 * q; p < npix; ++p)
+            for (int k = 0; k < 3; ++k) {
+                const float c = resolve_channel(fb.acc[3 * p + k], scale);
+                if (fb.rgb) fb.rgb[3 * p + k] = c;
+                if (fb.rgb8) fb.rgb8[3 * p + k] = put_channel(c);
+            }
+        return;
+    }
+    const longlong2 *a2 = reinterpret_cast<const longlong2 *>(fb.acc + 12 * q);
+    float c[12];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+        const longlong2 v = a2[k];
+        c[2 * k] = resolve_channel(v.x, scale);
+        c[2 * k + 1] = resolve_channel(v.y, scale);
+    }
+    if (fb.rgb) {
+        float4 *o = reinterpret_cast<float4 *>(fb.rgb + 12 * q);
+        o[0] = make_float4(c[0], c[1], c[2], c[3]);
+        o[1] = make_float4(c[4], c[5], c[6], c[7]);
+        o[2] = make_float4(c[8], c[9], c[10], c[11]);
+    }
+    if (fb.rgb8) {
+        unsigned *o = reinterpret_cast<unsigned *>(fb.rgb8 + 12 * q);
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+            o[k] = (unsigned)put_channel(c[4 * k]) | (unsigned)put_channel(c[4 * k + 1]) << 8 |
+                   (unsigned)put_channel(c[4 * k + 2]) << 16 | (unsigned)put_channel(c[4 * k + 3]) << 24;
+    }
+}
+
 __global__ void k_resolve(FrameBufs fb, long long npix, DSplit scale)
 {
-    for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < npix; p += (long long)gridDim.x * blockDim.x) {
-        float c[3];
-        for (int k = 0; k < 3; ++k) c[k] = dmul_to_float(fb.acc[3 * p + k], scale);
-        if (fb.rgb) {
-            fb.rgb[3 * p] = c[0];
-            fb.rgb[3 * p + 1] = c[1];
-            fb.rgb[3 * p + 2] = c[2];
-        }
-        if (fb.rgb8) {
-            fb.rgb8[3 * p] = put_channel(c[0]);
-            fb.rgb8[3 * p + 1] = put_channel(c[1]);
-            fb.rgb8[3 * p + 2] = put_channel(c[2]);
-        }
+    const long long nq = (npix + 3) >> 2;
+    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += (long long)gridDim.x * blockDim.x)
+        resolve_quad(fb, q, npix, scale);
+}
+
+// the frame of batch quad g: first frame whose quad_end is above g
+__device__ __forceinline__ int frame_of(const FrameJob *fj, int n, long long g)
+{
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (fj[mid].quad_end > g) hi = mid;
+        else lo = mid + 1;
     }
+    return lo;
+}
+
+__global__ void k_frames_resolve(const FrameJob *fj, int n, long long quads)
+{
+    for (long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x; g < quads; g += (long long)gridDim.x * blockDim.x) {
+        const int f = frame_of(fj, n, g);
+        const FrameJob &F = fj[f];
+        const long long q = g - (f ? fj[f - 1].quad_end : 0);
+        resolve_quad(F.fb, q, F.npix, split_double_bits(F.scale_bits));
+    }
+}
+
+// quad q of a frame with nq quads: zero its accumulators, reset its hit planes, and fill the
+// axis entries q, q + nq, ... (a frame has at least W + H quads unless it is tiny)
+__device__ __forceinline__ void prepare_quad(const FrameJob &F, long long q, long long nq)
+{
+    const long long p0 = 4 * q, p1 = min(p0 + 4, F.npix);
+    if (p1 - p0 == 4) {
+        longlong2 *a2 = reinterpret_cast<longlong2 *>(F.fb.acc + 12 * q);
+#pragma unroll
+        for (int k = 0; k < 6; ++k) a2[k] = make_longlong2(0, 0);
+    } else {
+        for (long long p = p0; p < p1; ++p) F.fb.acc[3 * p] = F.fb.acc[3 * p + 1] = F.fb.acc[3 * p + 2] = 0;
+    }
+    if (F.planes)
+        for (long long p = p0; p < p1; ++p) {
+            F.fb.plane_obj[p] = -1;
+            F.fb.plane_prim[p] = 0;
+            F.fb.plane_t[p] = kMiss;
+        }
+    if (F.dp_bits) {   // (float)((double)xcur * dp), xcur = col - W/2, then the rows (RayTracer.cpp:14-18)
+        const DSplit d = split_double_bits(F.dp_bits);
+        for (long long k = q; k < F.w + F.h; k += nq)
+            F.fb.axis[k] = dmul_to_float(k < F.w ? k - F.w / 2 : k - F.w - F.h / 2, d);
+    }
+}
+
+__global__ void k_frames_prepare(const FrameJob *fj, int n, long long quads)
+{
+    for (long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x; g < quads; g += (long long)gridDim.x * blockDim.x) {
+        const int f = frame_of(fj, n, g);
+        const long long q0 = f ? fj[f - 1].quad_end : 0;
+        prepare_quad(fj[f], g - q0, fj[f].quad_end - q0);
+    }
+}
+
+__global__ void k_frame_prepare(FrameJob F)
+{
+    const long long nq = (F.npix + 3) >> 2;
+    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += (long long)gridDim.x * blockDim.x)
+        prepare_quad(F, q, nq);
 }
 
 __global__ void k_selftest_conversions(const long long *x, int n, DSplit d, const float *v, float *out_mul,
@@ -646,15 +790,6 @@ void launch_selftest_conversions(const long long *x, int n, unsigned long long d
 {
     k_selftest_conversions<<<std::max(1, std::min((n + 255) / 256, sm_count() * 4)), 256, 0, s>>>(
         x, n, split_double_bits(d_bits), v, out_mul, out_fix);
-}
-
-__global__ void k_plane_init(FrameBufs fb, long long npix)
-{
-    for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < npix; p += (long long)gridDim.x * blockDim.x) {
-        fb.plane_obj[p] = -1;
-        fb.plane_prim[p] = 0;
-        fb.plane_t[p] = kMiss;
-    }
 }
 
 // ---- launchers ------------------------------------------------------------------------------------
@@ -688,33 +823,42 @@ static int grid_for(const Tuning &t, const void *kernel)
     return sm_count() * it->second;
 }
 
-void launch_raygen(const Wavefront &wf, int grid, int block, cudaStream_t s)
-{
-    k_raygen<<<grid, block, 0, s>>>(wf);
-}
-
-template <bool DYN, bool CNT>
+template <bool DYN, bool CNT, bool GEN>
 static void extend_launch(const Wavefront &wf, int sel, int wslot, const Tuning &t, cudaStream_t s)
 {
 #define RT_EXT(MB)                                                                                                \
     {                                                                                                             \
-        auto k = k_extend<kStack, DYN, CNT, MB>;                                                                      \
+        auto k = k_extend<kStack, DYN, CNT, MB, GEN>;                                                             \
         k<<<grid_for(t, (const void *)k), t.block, 0, s>>>(wf, sel, wslot, t.tile);                              \
     }
-    if (t.min_blocks == 8) RT_EXT(8) else if (t.min_blocks == 6) RT_EXT(6) else if (t.min_blocks == 10) RT_EXT(10)
+    if constexpr (CNT) RT_EXT(8)
+    else if (t.min_blocks == 8) RT_EXT(8) else if (t.min_blocks == 6) RT_EXT(6) else if (t.min_blocks == 10) RT_EXT(10)
     else if (t.min_blocks == 12) RT_EXT(12) else RT_EXT(0)
 #undef RT_EXT
 }
 
-void launch_extend(const Wavefront &wf, int sel, int level, const Tuning &t, cudaStream_t s)
+// The counting pass (an untimed statistics pass) runs in one configuration: what it counts
+// does not depend on the launch shape.
+static Tuning count_tuning(const Tuning &t)
+{
+    Tuning c = t;
+    c.block = 128, c.dynamic = true, c.min_blocks = 8;
+    return c;
+}
+
+void launch_extend(const Wavefront &wf, int sel, int level, bool gen, const Tuning &t, cudaStream_t s)
 {
     const int wslot = 3 * level;
-    if (t.dynamic) {
-        if (t.count) extend_launch<true, true>(wf, sel, wslot, t, s);
-        else extend_launch<true, false>(wf, sel, wslot, t, s);
+    if (t.count) {
+        const Tuning c = count_tuning(t);
+        if (gen) extend_launch<true, true, true>(wf, sel, wslot, c, s);
+        else extend_launch<true, true, false>(wf, sel, wslot, c, s);
+    } else if (t.dynamic) {
+        if (gen) extend_launch<true, false, true>(wf, sel, wslot, t, s);
+        else extend_launch<true, false, false>(wf, sel, wslot, t, s);
     } else {
-        if (t.count) extend_launch<false, true>(wf, sel, wslot, t, s);
-        else extend_launch<false, false>(wf, sel, wslot, t, s);
+        if (gen) extend_launch<false, false, true>(wf, sel, wslot, t, s);
+        else extend_launch<false, false, false>(wf, sel, wslot, t, s);
     }
 }
 
@@ -738,7 +882,8 @@ static void shadow_launch(const Wavefront &wf, int wslot, const Tuning &t, cudaS
         auto k = k_shadow<kStack, DYN, CNT, MB>;                                                                      \
         k<<<grid_for(t, (const void *)k), t.block, 0, s>>>(wf, wslot, t.tile);                                   \
     }
-    if (t.min_blocks == 8) RT_SHD(8) else if (t.min_blocks == 6) RT_SHD(6) else if (t.min_blocks == 10) RT_SHD(10)
+    if constexpr (CNT) RT_SHD(8)
+    else if (t.min_blocks == 8) RT_SHD(8) else if (t.min_blocks == 6) RT_SHD(6) else if (t.min_blocks == 10) RT_SHD(10)
     else if (t.min_blocks == 12) RT_SHD(12) else RT_SHD(0)
 #undef RT_SHD
 }
@@ -746,31 +891,46 @@ static void shadow_launch(const Wavefront &wf, int wslot, const Tuning &t, cudaS
 void launch_shadow(const Wavefront &wf, int level, const Tuning &t, cudaStream_t s)
 {
     const int wslot = 3 * level + 2;
-    if (t.dynamic) {
-        if (t.count) shadow_launch<true, true>(wf, wslot, t, s);
-        else shadow_launch<true, false>(wf, wslot, t, s);
-    } else {
-        if (t.count) shadow_launch<false, true>(wf, wslot, t, s);
-        else shadow_launch<false, false>(wf, wslot, t, s);
-    }
+    if (t.count) shadow_launch<true, true>(wf, wslot, count_tuning(t), s);
+    else if (t.dynamic) shadow_launch<true, false>(wf, wslot, t, s);
+    else shadow_launch<false, false>(wf, wslot, t, s);
 }
 
 void launch_resolve(const FrameBufs &fb, int width, int height, int spp, cudaStream_t s)
 {
     long long npix = (long long)width * height;
-    int grid = (int)std::min<long long>((npix + 255) / 256, (long long)sm_count() * 8);
+    int grid = (int)std::min<long long>(((npix + 3) / 4 + 255) / 256, (long long)sm_count() * 8);
     if (grid < 1) grid = 1;
+    k_resolve<<<grid, 256, 0, s>>>(fb, npix, split_double_bits(resolve_scale_bits(spp)));
+}
+
+unsigned long long resolve_scale_bits(int spp)
+{
     const double scale = 1.0 / 4294967296.0 / (double)spp;
     unsigned long long bits;
     std::memcpy(&bits, &scale, sizeof bits);
-    k_resolve<<<grid, 256, 0, s>>>(fb, npix, split_double_bits(bits));
+    return bits;
 }
 
-void launch_plane_init(const FrameBufs &fb, long long npix, cudaStream_t s)
+static int quad_grid(long long quads)
 {
-    int grid = (int)std::min<long long>((npix + 255) / 256, (long long)sm_count() * 8);
-    if (grid < 1) grid = 1;
-    k_plane_init<<<grid, 256, 0, s>>>(fb, npix);
+    return (int)std::max<long long>(1, std::min<long long>((quads + 255) / 256, (long long)sm_count() * 8));
 }
+
+void launch_frames_prepare(const FrameJob *jobs, int n, long long quads, cudaStream_t s)
+{
+    if (n > 0 && quads > 0) k_frames_prepare<<<quad_grid(quads), 256, 0, s>>>(jobs, n, quads);
+}
+
+void launch_frame_prepare(const FrameJob &job, cudaStream_t s)
+{
+    k_frame_prepare<<<quad_grid((job.npix + 3) / 4), 256, 0, s>>>(job);
+}
+
+void launch_frames_resolve(const FrameJob *jobs, int n, long long quads, cudaStream_t s)
+{
+    if (n > 0 && quads > 0) k_frames_resolve<<<quad_grid(quads), 256, 0, s>>>(jobs, n, quads);
+}
+
 
 } // namespace rtg

@@ -14,6 +14,21 @@ struct FrameBufs {
     int *plane_obj;     // primary hit object, sample 0
     int *plane_prim;
     float *plane_t;
+    float *axis;        // camera offsets of a 1-sample render: (float)((double)xcur * dp) for the
+                        // W columns, then (float)((double)ycur * dp) for the H rows
+};
+
+// one frame of a batch, for the batch-wide prepare and resolve launches. Pixels go in groups
+// of four (quads); the frame's quads are [quad_end of the previous frame, quad_end).
+struct FrameJob {
+    FrameBufs fb;
+    long long npix;
+    long long quad_end;             // inclusive prefix of quads over the batch's frames
+    unsigned long long scale_bits;  // resolve scale 2^-32 / spp as double bits
+    unsigned long long dp_bits;     // camera dp as double bits: fill fb.axis (0 = no table)
+    int w, h;
+    int planes;                     // reset the hit planes
+    int pad;
 };
 
 // everything one wavefront pass needs
@@ -51,12 +66,19 @@ struct Tuning {
 
 int sm_count();
 // kernels of one level; `sel` picks the input ray queue
-void launch_raygen(const Wavefront &wf, int grid, int block, cudaStream_t s);
-void launch_extend(const Wavefront &wf, int sel, int level, const Tuning &t, cudaStream_t s);
+// gen: the first extend of a wave, which makes the wave's primary rays itself
+void launch_extend(const Wavefront &wf, int sel, int level, bool gen, const Tuning &t, cudaStream_t s);
 void launch_shade(const Wavefront &wf, int sel, int level, const Tuning &t, cudaStream_t s);
 void launch_shadow(const Wavefront &wf, int level, const Tuning &t, cudaStream_t s);
 void launch_resolve(const FrameBufs &fb, int width, int height, int spp, cudaStream_t s);
-void launch_plane_init(const FrameBufs &fb, long long npix, cudaStream_t s);
+// zero the accumulators, reset the hit planes and fill the camera axis table (as each FrameJob
+// asks) / resolve the colours: n frames in one launch each
+void launch_frames_prepare(const FrameJob *jobs, int n, long long quads, cudaStream_t s);
+// the same preparation for one frame
+void launch_frame_prepare(const FrameJob &job, cudaStream_t s);
+void launch_frames_resolve(const FrameJob *jobs, int n, long long quads, cudaStream_t s);
+// the resolve scale of spp samples per pixel, as double bits
+unsigned long long resolve_scale_bits(int spp);
 // the integer-exact conversions of the kernels, on n inputs (a test hook)
 void launch_selftest_conversions(const long long *x, int n, unsigned long long d_bits, const float *v, float *out_mul,
                                  long long *out_fix, cudaStream_t s);

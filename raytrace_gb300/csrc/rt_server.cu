@@ -264,7 +264,7 @@ static int admit(rt_server *srv)
         r->wj.cursor = 0;
         r->wj.weight = wave_weight(sd.branching, srv->cfg.max_level);
         CK(ctx, cudaStreamWaitEvent(ctx->stream, slot.copied, 0));   // the previous image left the slot
-        CK(ctx, cudaMemsetAsync(slot.fb.acc, 0, 24 * (size_t)r->req.width * r->req.height, ctx->stream));
+        launch_frame_prepare(frame_job(slot.fb, r->req.width, r->req.height, r->wj.job), ctx->stream);
         slot.used = true;
         srv->hslots[(size_t)hs].used = true;
         r->dev_slot = ds, r->host_slot = hs;
@@ -554,12 +554,15 @@ static int server_init(rt_server *srv)
     const int n_slots = c.plain ? 1 : c.max_inflight;
     srv->dslots.resize(c.plain ? 0 : (size_t)n_slots);
     for (DevSlot &d : srv->dslots) {
+        // accumulators, colour, bytes, and the camera axis table (at most 16384 + 16384 entries)
         size_t o_rgb = (24 * P + 255) & ~(size_t)255, o_rgb8 = o_rgb + ((12 * P + 255) & ~(size_t)255);
-        CK(ctx, d.mem.ensure(o_rgb8 + 3 * P));
+        size_t o_axis = o_rgb8 + ((3 * P + 255) & ~(size_t)255);
+        CK(ctx, d.mem.ensure(o_axis + 4 * 32768));
         char *b = (char *)d.mem.p;
         d.fb.acc = (long long *)b;
         d.fb.rgb = (float *)(b + o_rgb);
         d.fb.rgb8 = (uint8_t *)(b + o_rgb8);
+        d.fb.axis = (float *)(b + o_axis);
         CK(ctx, cudaEventCreate(&d.copied));
         CK(ctx, cudaEventRecord(d.copied, srv->copy));
         srv->fixed_bytes += (int64_t)d.mem.bytes;
