@@ -739,7 +739,9 @@ int ws_ensure(rt_ctx *ctx, Workspace &ws, long long qcap, int njobs)
         for (int j = 0; j < 4; ++j) oq[k][j] = take(16 * q);
     size_t os[5];
     for (int j = 0; j < 5; ++j) os[j] = take(16 * q);
-    const size_t o_hit = take(16 * q), o_nob = take(4 * q), o_hl = take(4 * q), o_ctr = take(sizeof(Counters)),
+    size_t oh[5];
+    for (int j = 0; j < 5; ++j) oh[j] = take(16 * q);
+    const size_t o_nob = take(4 * q), o_ctr = take(sizeof(Counters)),
                  o_jobs = take(sizeof(DevJob) * (size_t)njobs), o_end = take(8 * (size_t)njobs), o_tot = take(32),
                  o_scn = take(sizeof(DevScene) * (size_t)njobs);
     CK(ctx, ws.mem.ensure(off));
@@ -757,9 +759,12 @@ int ws_ensure(rt_ctx *ctx, Workspace &ws, long long qcap, int njobs)
     ws.wf.sq.wc = (float4 *)(b + os[3]);
     ws.wf.sq.ws = (float4 *)(b + os[4]);
     ws.wf.sq.capacity = (int)q;
-    ws.wf.hit = (float4 *)(b + o_hit);
-    ws.wf.newobj = (int *)(b + o_nob);
-    ws.wf.hitlist = (int *)(b + o_hl);
+    ws.wf.hq.o = (float4 *)(b + oh[0]);
+    ws.wf.hq.d = (float4 *)(b + oh[1]);
+    ws.wf.hq.w = (float4 *)(b + oh[2]);
+    ws.wf.hq.m = (int4 *)(b + oh[3]);
+    ws.wf.hq.h = (float4 *)(b + oh[4]);
+    ws.wf.hq.nob = (int *)(b + o_nob);
     ws.wf.C = (Counters *)(b + o_ctr);
     ws.jobs = (DevJob *)(b + o_jobs);
     ws.job_end = (long long *)(b + o_end);

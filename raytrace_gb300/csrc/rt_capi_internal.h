@@ -193,6 +193,9 @@ int wave_harvest(rt_ctx *ctx, WaveRunner &R, bool wait);
 size_t wave_runner_bytes(const WaveRunner &R);
 
 constexpr size_t kPlainStageBytes = 4096;
+// workspace bytes per ray-queue entry: two ray queues (64 B each), the shadow queue (80 B) and
+// the hit queue (84 B)
+constexpr long long kWsBytesPerEntry = 292;
 
 struct rt_ctx {
     int device = 0;

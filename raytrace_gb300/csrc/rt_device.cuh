@@ -151,6 +151,15 @@ __device__ __forceinline__ int ray_flags(int level, int type, int inside, int pl
     return (level & 0xff) | (type & 0xff) << 8 | (inside & 0xff) << 16 | (plane & 1) << 24;
 }
 
+// the rays of one bounce that hit something, densely in the order extend found them: the ray
+// record as in RayQueue plus the hit, 84 B per hit, read by shading with coalesced loads
+struct HitQueue {
+    float4 *o, *d, *w;
+    int4 *m;
+    float4 *h;      // distance, barycentrics u v, primitive key (int bits)
+    int *nob;       // exclude key for the children (RTfrac's newobj)
+};
+
 // one hit point waiting for its shadow rays, 80 B
 struct ShadowQueue {
     float4 *p;      // hit position, pixel index in the frame (int bits)

@@ -211,48 +211,54 @@ __global__ void __launch_bounds__(MINB ? 128 : 256, MINB ? MINB : 1) k_extend(Wa
     const int level = wslot / 3;
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
+    const HitQueue hq = wf.hq;
     for_each_ray<DYN>(n, &C->work[wslot], tile, [&](int i, bool active) {
-        bool is_hit = false;
+        Best best;
+        best.key = -1;
+        int newobj = -1, job = 0, pixel = 0, plane = 0;
+        V3 o, d;
         if constexpr (GEN) {
-            const int job = job_of(wf, first + i, first + (i - lane), active);
+            job = job_of(wf, first + i, first + (i - lane), active);
             if (active) {
                 const DevJob &J = wf.jobs[job];
                 const PrimaryRay pr = primary_ray(J, first + i - J.sample_base);
                 if (J.mode == kModeCheck && ((pr.row >> 6) & 1) == ((pr.col >> 6) & 1))
                     acc_add(J.acc, pr.pixel, mk(1.0f, 1.0f, 1.0f));   // RTcheck: white 64x64 tiles
-                const int plane = pr.sample == 0 && J.plane_obj != nullptr;
-                const DevScene &S = wf.scenes[J.scene];
-                Best best;
-                int newobj;
-                closest_hit<STACK, COUNT>(S, pr.o, pr.d, -1, false, best, newobj, wc);
-                is_hit = best.key >= 0;
-                if (is_hit) {   // shading reads hits only
-                    wf.hit[i] = make_float4(best.t, best.u, best.v, __int_as_float(best.key));
-                    wf.newobj[i] = newobj;
-                    q.o[i] = make_float4(pr.o.x, pr.o.y, pr.o.z, 1.0f);
-                    q.d[i] = make_float4(pr.d.x, pr.d.y, pr.d.z, 1.0f);
-                    q.w[i] = make_float4(1.0f, 1.0f, 1.0f, __int_as_float(pr.pixel));
-                    q.m[i] = make_int4(-1, ray_flags(0, kRayBase, 0, plane), -1, job);
-                }
+                plane = pr.sample == 0 && J.plane_obj != nullptr;
+                pixel = pr.pixel;
+                o = pr.o, d = pr.d;
+                closest_hit<STACK, COUNT>(wf.scenes[J.scene], o, d, -1, false, best, newobj, wc);
             }
         } else if (active) {
             const float4 o4 = q.o[i], d4 = q.d[i];
             const int4 m4 = q.m[i];
-            const DevScene &S = wf.scenes[wf.jobs[m4.w].scene];
-            Best best;
-            int newobj;
-            closest_hit<STACK, COUNT>(S, mk(o4), mk(d4), m4.x, ray_inside(m4.y) != 0, best, newobj, wc);
-            wf.hit[i] = make_float4(best.t, best.u, best.v, __int_as_float(best.key));
-            wf.newobj[i] = newobj;
-            is_hit = best.key >= 0;
+            closest_hit<STACK, COUNT>(wf.scenes[wf.jobs[m4.w].scene], mk(o4), mk(d4), m4.x, ray_inside(m4.y) != 0, best,
+                                      newobj, wc);
         }
-        // list the hits (one atomic per warp): shading runs over hits only, misses cost it nothing
+        // the hits go to the hit queue densely (one atomic per warp): shading reads them with
+        // coalesced loads, and misses cost it nothing
+        const bool is_hit = best.key >= 0;
         const unsigned hb = __ballot_sync(kFull, is_hit);
         if (hb) {
             int base = 0;
             if (lane == 0) base = atomicAdd(&C->h_count[level], __popc(hb));
             base = __shfl_sync(kFull, base, 0);
-            if (is_hit) wf.hitlist[base + __popc(hb & lt)] = i;
+            if (is_hit) {
+                const int h = base + __popc(hb & lt);   // below the queue capacity: one per ray
+                hq.h[h] = make_float4(best.t, best.u, best.v, __int_as_float(best.key));
+                hq.nob[h] = newobj;
+                if constexpr (GEN) {
+                    hq.o[h] = make_float4(o.x, o.y, o.z, 1.0f);
+                    hq.d[h] = make_float4(d.x, d.y, d.z, 1.0f);
+                    hq.w[h] = make_float4(1.0f, 1.0f, 1.0f, __int_as_float(pixel));
+                    hq.m[h] = make_int4(-1, ray_flags(0, kRayBase, 0, plane), -1, job);
+                } else {   // the ray record again (its lines were read at the start of this tile)
+                    hq.o[h] = q.o[i];
+                    hq.d[h] = q.d[i];
+                    hq.w[h] = q.w[i];
+                    hq.m[h] = q.m[i];
+                }
+            }
         }
     });
     if (wc.err) atomicOr(&C->error, wc.err);
@@ -360,37 +366,40 @@ __device__ V3 mode_material(const DevScene &S, const DevMaterial &M, V3 P, V3 N,
 }
 
 // ---- shade ------------------------------------------------------------------------------------
-// 1024 resident threads per SM (64 registers): shading is latency-bound on its dependent loads
+// 640 resident threads per SM (up to 96 registers, no spills): shading is latency-bound on its
+// dependent loads, and 64-register builds spilled the records it writes
 template <bool DYN>
-__global__ void __launch_bounds__(256, 4) k_shade(Wavefront wf, int sel, int wslot, int tile)
+__global__ void __launch_bounds__(128, 5) k_shade(Wavefront wf, int sel, int wslot, int tile)
 {
     if (cancelled(wf.cancel)) return;
     Counters *C = wf.C;
     const RayQueue q = wf.q[sel], qo = wf.q[sel ^ 1];
+    const HitQueue hq = wf.hq;
     const ShadowQueue sq = wf.sq;
-    // the hits extend listed (a miss needs no shading: the hit planes start as misses)
+    // the hits of this bounce (a miss needs no shading: the hit planes start as misses)
     const int n = min(C->h_count[wslot / 3], q.capacity);
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
     for_each_ray_guided<DYN>(n, &C->work[wslot], tile, [&](int j, bool active) {
-        const int i = active ? wf.hitlist[j] : 0;
-        bool emit = false;
-        int nchild = 0;
-        float4 c_o[2], c_d[2], c_w[2];
-        int4 c_m[2];
-        float4 s_p, s_n, s_v, s_wc, s_ws;
-        const float4 h4 = active ? wf.hit[i] : make_float4(0.0f, 0.0f, 0.0f, __int_as_float(-1));
-        const int4 m4 = active ? q.m[i] : make_int4(0, 0, 0, 0);
-        // a miss of a ray that writes no hit plane has nothing to shade: skip its other loads
-        if (active && (__float_as_int(h4.w) >= 0 || ray_plane(m4.y))) {
-            const float4 o4 = q.o[i], d4 = q.d[i], w4 = q.w[i];
-            const int nob = wf.newobj[i];
+        // what the hit emits is decided first and written after the warp has reserved queue
+        // slots, so only the inputs of the records stay live across the ballots
+        bool emit = false, c_refl = false, c_refr = false;
+        V3 P, N, D, W, Wc;
+        float wl = 1.0f;   // the local terms' share of W (Wl = W x wl)
+        int pix = 0, mtl_id = 0, nob = 0, job = 0, level = 0, hit_inside = 0;
+        float r_bc = 0.0f, r_w = 0.0f, t_bc = 0.0f, t_f = 0.0f, eta = 0.0f, cosIn = 0.0f, cosOut2 = 0.0f, hit_rfr = 1.0f;
+        if (active) {
+            const float4 h4 = hq.h[j], o4 = hq.o[j], d4 = hq.d[j], w4 = hq.w[j];
+            const int4 m4 = hq.m[j];
+            nob = hq.nob[j];
+            job = m4.w;
             const DevJob &J = wf.jobs[m4.w];
             const DevScene &S = wf.scenes[J.scene];
-            const int flags = m4.y, level = ray_level(flags), type = ray_type(flags), inside = ray_inside(flags);
+            const int flags = m4.y, type = ray_type(flags), inside = ray_inside(flags);
+            level = ray_level(flags);
             const float t = h4.x;
             const int key = __float_as_int(h4.w);
-            const int pix = __float_as_int(w4.w);
+            pix = __float_as_int(w4.w);
             const bool is_tri = key >= 0 && (key & kTriFlag);
             const DevPrim *pr = (key >= 0 && !is_tri) ? &S.prims[key] : nullptr;
             const int tk = key & ~kTriFlag;
@@ -416,11 +425,11 @@ __global__ void __launch_bounds__(256, 4) k_shade(Wavefront wf, int sel, int wsl
             } else if (key >= 0 && mode != kModeCheck && !far && near && !traced) {
                 acc_add(J.acc, pix, mk(w4));   // Color(true)
             } else if (key >= 0 && mode != kModeCheck && !far && !near) {
-                const V3 O = mk(o4), D = mk(d4);
-                const V3 P = vadd(O, vscale(D, t));
-                int mtl_id, tex = -1, hit_inside = 0;
-                float hit_rfr = 1.0f, tu = 0.0f, tv = 0.0f;
-                V3 N;
+                const V3 O = mk(o4);
+                D = mk(d4);
+                P = vadd(O, vscale(D, t));
+                int tex = -1;
+                float tu = 0.0f, tv = 0.0f;
                 if (is_tri) {
                     const float4 e2 = S.tri[3 * tk + 2];
                     mtl_id = __float_as_int(e2.w);
@@ -470,7 +479,7 @@ __global__ void __launch_bounds__(256, 4) k_shade(Wavefront wf, int sel, int wsl
                 }
                 const DevMaterial &M = S.mtl[mtl_id];
                 const V3 vc = tex >= 0 ? tex_color(S, tex, tu, tv) : mk(1.0f, 1.0f, 1.0f);
-                V3 W = mk(w4);
+                W = mk(w4);
                 if (mode == kModeNormal || mode == kModeTexture || mode == kModeMaterial) {
                     V3 c;
                     if (mode == kModeNormal)   // Color(Normal): 0.5 * (n + 1), exact in one rounding
@@ -494,7 +503,8 @@ __global__ void __launch_bounds__(256, 4) k_shade(Wavefront wf, int sel, int wsl
                 const bool refr = M.refract > 0.01f && (mode == kModeRaytrace || mode == kModeRefract);
                 const float a1 = refl ? __fsub_rn(1.0f, M.reflect) : 1.0f;
                 const float a2 = refr ? __fsub_rn(1.0f, M.refract) : 1.0f;
-                const V3 Wl = vscale(W, __fmul_rn(a1, a2));
+                wl = __fmul_rn(a1, a2);
+                const V3 Wl = vscale(W, wl);
                 // ambient: environment plus every switched-on light, shadowed or not (RTshd adds
                 // the environment last, RTfrac and RTflec first)
                 const V3 ka = mk(M.ka[0], M.ka[1], M.ka[2]);
@@ -511,49 +521,22 @@ __global__ void __launch_bounds__(256, 4) k_shade(Wavefront wf, int sel, int wsl
                     mix_va = vadd(mix_va, vmul(ka, la));
                 }
                 if (mode == kModeShadow) mix_va = vadd(mix_va, env);
-                const V3 Wc = vmul(Wl, vc);
+                Wc = vmul(Wl, vc);
                 acc_add(J.acc, pix, vmul(Wc, mix_va));
-                if (lights_on > 0) {
-                    emit = true;
-                    s_p = make_float4(P.x, P.y, P.z, __int_as_float(pix));
-                    s_n = make_float4(N.x, N.y, N.z, __int_as_float(mtl_id));
-                    s_v = make_float4(D.x, D.y, D.z, __int_as_float(nob));
-                    s_wc = make_float4(Wc.x, Wc.y, Wc.z, __int_as_float(m4.w));
-                    s_ws = make_float4(Wl.x, Wl.y, Wl.z, 0.0f);
-                }
+                emit = lights_on > 0;
                 const float bwc = o4.w;
                 if (refl && level + 1 <= J.max_level) {
-                    const float r = M.reflect, bc = __fmul_rn(bwc, r);
-                    if (!(bc < 1e-5f)) {
-                        const float nn = __fmul_rn(2.0f, dot3(D, N));
-                        const V3 R = normalise(vsub(D, vscale(N, nn)));
-                        const V3 Wr = vscale(W, __fmul_rn(r, a2));
-                        c_o[nchild] = make_float4(P.x, P.y, P.z, bc);
-                        c_d[nchild] = make_float4(R.x, R.y, R.z, 1.0f);
-                        c_w[nchild] = make_float4(Wr.x, Wr.y, Wr.z, __int_as_float(pix));
-                        c_m[nchild] = make_int4(nob, ray_flags(level + 1, kRayReflect, 0, 0), -1, m4.w);
-                        ++nchild;
-                    }
+                    r_bc = __fmul_rn(bwc, M.reflect);
+                    r_w = __fmul_rn(M.reflect, a2);
+                    c_refl = !(r_bc < 1e-5f);
                 }
                 if (refr && level + 1 <= J.max_level) {
-                    const float f = M.refract;
-                    const float eta = __fdiv_rn(d4.w, hit_rfr);
-                    const float cosIn = -dot3(D, N);
-                    const float cosOut2 =
-                        __fsub_rn(1.0f, __fmul_rn(__fmul_rn(eta, eta), __fsub_rn(1.0f, __fmul_rn(cosIn, cosIn))));
-                    const float bc = __fmul_rn(bwc, f);
-                    if (!(cosOut2 < 0.0f) && !(bc < 1e-5f)) {
-                        const V3 l2 = vscale(D, eta);
-                        const V3 l1 = vscale(N, __fsub_rn(__fmul_rn(eta, cosIn), __fsqrt_rn(cosOut2)));
-                        const V3 T = normalise(vadd(l1, l2));
-                        const V3 Wt = vscale(W, f);
-                        c_o[nchild] = make_float4(P.x, P.y, P.z, bc);
-                        c_d[nchild] = make_float4(T.x, T.y, T.z, hit_rfr);
-                        c_w[nchild] = make_float4(Wt.x, Wt.y, Wt.z, __int_as_float(pix));
-                        c_m[nchild] = make_int4(nob, ray_flags(level + 1, kRayRefract, hit_inside, 0), hit_inside ? mtl_id : -1,
-                                                m4.w);
-                        ++nchild;
-                    }
+                    t_f = M.refract;
+                    eta = __fdiv_rn(d4.w, hit_rfr);
+                    cosIn = -dot3(D, N);
+                    cosOut2 = __fsub_rn(1.0f, __fmul_rn(__fmul_rn(eta, eta), __fsub_rn(1.0f, __fmul_rn(cosIn, cosIn))));
+                    t_bc = __fmul_rn(bwc, t_f);
+                    c_refr = !(cosOut2 < 0.0f) && !(t_bc < 1e-5f);
                 }
                 }
             }
@@ -567,16 +550,18 @@ __global__ void __launch_bounds__(256, 4) k_shade(Wavefront wf, int sel, int wsl
             if (emit) {
                 const int slot = base + __popc(bs & lt);
                 if (slot < sq.capacity) {
-                    sq.p[slot] = s_p;
-                    sq.n[slot] = s_n;
-                    sq.v[slot] = s_v;
-                    sq.wc[slot] = s_wc;
-                    sq.ws[slot] = s_ws;
+                    sq.p[slot] = make_float4(P.x, P.y, P.z, __int_as_float(pix));
+                    sq.n[slot] = make_float4(N.x, N.y, N.z, __int_as_float(mtl_id));
+                    sq.v[slot] = make_float4(D.x, D.y, D.z, __int_as_float(nob));
+                    sq.wc[slot] = make_float4(Wc.x, Wc.y, Wc.z, __int_as_float(job));
+                    const V3 Wl = vscale(W, wl);
+                    sq.ws[slot] = make_float4(Wl.x, Wl.y, Wl.z, 0.0f);
                 } else
                     atomicExch(&C->overflow, 1);
             }
         }
-        const unsigned b1 = __ballot_sync(kFull, nchild >= 1), b2 = __ballot_sync(kFull, nchild == 2);
+        // children: the reflected rays of the warp, then its refracted rays
+        const unsigned b1 = __ballot_sync(kFull, c_refl), b2 = __ballot_sync(kFull, c_refr);
         const int tot = __popc(b1) + __popc(b2);
         if (tot) {
             int base = 0;
@@ -585,14 +570,31 @@ __global__ void __launch_bounds__(256, 4) k_shade(Wavefront wf, int sel, int wsl
                 atomicAdd(&C->rays_secondary, (unsigned long long)tot);
             }
             base = __shfl_sync(kFull, base, 0);
-            const int off = base + __popc(b1 & lt) + __popc(b2 & lt);
-            for (int c = 0; c < nchild; ++c) {
-                const int slot = off + c;
+            if (c_refl) {
+                const int slot = base + __popc(b1 & lt);
                 if (slot < qo.capacity) {
-                    qo.o[slot] = c_o[c];
-                    qo.d[slot] = c_d[c];
-                    qo.w[slot] = c_w[c];
-                    qo.m[slot] = c_m[c];
+                    const float nn = __fmul_rn(2.0f, dot3(D, N));
+                    const V3 R = normalise(vsub(D, vscale(N, nn)));
+                    const V3 Wr = vscale(W, r_w);
+                    qo.o[slot] = make_float4(P.x, P.y, P.z, r_bc);
+                    qo.d[slot] = make_float4(R.x, R.y, R.z, 1.0f);
+                    qo.w[slot] = make_float4(Wr.x, Wr.y, Wr.z, __int_as_float(pix));
+                    qo.m[slot] = make_int4(nob, ray_flags(level + 1, kRayReflect, 0, 0), -1, job);
+                } else
+                    atomicExch(&C->overflow, 1);
+            }
+            if (c_refr) {
+                const int slot = base + __popc(b1) + __popc(b2 & lt);
+                if (slot < qo.capacity) {
+                    const V3 l2 = vscale(D, eta);
+                    const V3 l1 = vscale(N, __fsub_rn(__fmul_rn(eta, cosIn), __fsqrt_rn(cosOut2)));
+                    const V3 T = normalise(vadd(l1, l2));
+                    const V3 Wt = vscale(W, t_f);
+                    qo.o[slot] = make_float4(P.x, P.y, P.z, t_bc);
+                    qo.d[slot] = make_float4(T.x, T.y, T.z, hit_rfr);
+                    qo.w[slot] = make_float4(Wt.x, Wt.y, Wt.z, __int_as_float(pix));
+                    qo.m[slot] = make_int4(nob, ray_flags(level + 1, kRayRefract, hit_inside, 0), hit_inside ? mtl_id : -1,
+                                           job);
                 } else
                     atomicExch(&C->overflow, 1);
             }
@@ -865,12 +867,14 @@ void launch_extend(const Wavefront &wf, int sel, int level, bool gen, const Tuni
 void launch_shade(const Wavefront &wf, int sel, int level, const Tuning &t, cudaStream_t s)
 {
     const int wslot = 3 * level + 1;
+    Tuning ts = t;   // shading runs in 128-thread blocks whatever the traversal kernels use
+    ts.block = 128;
     if (t.dynamic) {
         auto k = k_shade<true>;
-        k<<<grid_for(t, (const void *)k), t.block, 0, s>>>(wf, sel, wslot, t.tile);
+        k<<<grid_for(ts, (const void *)k), 128, 0, s>>>(wf, sel, wslot, t.tile);
     } else {
         auto k = k_shade<false>;
-        k<<<grid_for(t, (const void *)k), t.block, 0, s>>>(wf, sel, wslot, t.tile);
+        k<<<grid_for(ts, (const void *)k), 128, 0, s>>>(wf, sel, wslot, t.tile);
     }
 }
 

@@ -42,9 +42,7 @@ struct Wavefront {
     const long long *max_lights;      // device scalar: most lights of any scene in the wave
     RayQueue q[2];
     ShadowQueue sq;
-    float4 *hit;
-    int *newobj;
-    int *hitlist;                     // queue indices of the rays that hit, per bounce (C->h_count)
+    HitQueue hq;                      // the rays that hit, densely, per bounce (C->h_count)
     Counters *C;
     const volatile int *cancel;       // device cancel flag (NULL = not cancellable)
 };

@@ -286,7 +286,9 @@ static int finish(rt_server *srv, Request *r)
     DevSlot &slot = srv->dslots[(size_t)r->dev_slot];
     HostSlot &hs = srv->hslots[(size_t)r->host_slot];
     const size_t np = (size_t)r->req.width * r->req.height;
-    launch_resolve(slot.fb, r->req.width, r->req.height, srv->cfg.spp, ctx->stream);
+    FrameBufs out = slot.fb;
+    if (!srv->cfg.keep_images) out.rgb = nullptr;   // the client gets bytes: no float colour written
+    launch_resolve(out, r->req.width, r->req.height, srv->cfg.spp, ctx->stream);
     CK(ctx, cudaGetLastError());
     cudaEvent_t resolved = take_event(srv);
     CK(ctx, cudaEventRecord(resolved, ctx->stream));
@@ -540,7 +542,10 @@ static int server_init(rt_server *srv)
     rt_ctx *ctx = srv->ctx;
     rt_server_config &c = srv->cfg;
     if (c.max_inflight <= 0) c.max_inflight = 64;
-    if (c.queue_rays <= 0) c.queue_rays = 1ll << 24;
+    if (c.queue_rays <= 0) {   // 2^26 entries, halved until the wave queues take at most a quarter of the budget
+        c.queue_rays = 1ll << 26;
+        while (c.queue_rays > (1ll << 16) && kWsBytesPerEntry * c.queue_rays > c.hbm_budget_bytes / 4) c.queue_rays >>= 1;
+    }
     if (c.max_pixels <= 0) c.max_pixels = 1920ll * 1080;
     if (c.stages <= 0) c.stages = 2;
     if (c.spp < 1 || c.spp > 1024 || c.max_level < 0 || c.max_level > 4 || c.max_inflight > 4096 ||

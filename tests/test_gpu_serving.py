@@ -158,7 +158,7 @@ def test_server_lru_eviction_and_rebuild(ctx):
         sid = ctx.upload(s)
         sizes.append(ctx.device_bytes(sid))
         ctx.release_scene(sid)
-    with rt.Server(ctx, 64 << 30, max_inflight=2, max_pixels=96 * 96) as big:
+    with rt.Server(ctx, 64 << 30, max_inflight=2, max_pixels=96 * 96, queue_rays=1 << 16) as big:
         ids = [big.add_scene(s) for s in scenes]
         reqs = [(ids[k % 4], 96, 64, rt.orbit_camera(big.camera(ids[k % 4]), 45.0 * k, 20.0, 96, 64), k)
                 for k in range(10)]
@@ -170,11 +170,12 @@ def test_server_lru_eviction_and_rebuild(ctx):
         assert big.stats()["evictions"] == 0
     srt = sorted(sizes)
     ctx.release_cached()   # buffers kept from earlier releases would count against the budget
-    with rt.Server(ctx, 64 << 30, max_inflight=2, max_pixels=96 * 96) as probe:
+    # the same wave queue size in both servers (the default one follows the budget)
+    with rt.Server(ctx, 64 << 30, max_inflight=2, max_pixels=96 * 96, queue_rays=1 << 16) as probe:
         base = probe.stats()["peak_bytes"]   # slots + queues + LBVH scratch
     budget = base + srt[-1] + srt[-2] + srt[0] // 2   # the two largest fit together, all four never
     ctx.release_cached()
-    with rt.Server(ctx, budget, max_inflight=2, max_pixels=96 * 96) as small:
+    with rt.Server(ctx, budget, max_inflight=2, max_pixels=96 * 96, queue_rays=1 << 16) as small:
         ids = [small.add_scene(s) for s in scenes]
         assert sum(small.resident(i) for i in ids) < 4
         got, rebuilt = [], 0
