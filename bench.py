@@ -242,7 +242,7 @@ def run_served(ctx, seconds: float) -> dict:
             "rays", "waves", "mean_wave_requests", "admitted_busy", "evictions", "rebuilds", "peak_bytes")
     for plain in (False, True):
         arm = "plain" if plain else "batched"
-        with rt.Server(ctx, 120 << 30, max_inflight=128, plain=plain, keep_images=False) as srv:
+        with rt.Server(ctx, 120 << 30, max_inflight=256, plain=plain, keep_images=False) as srv:
             for sc in scenes:
                 srv.add_scene(sc)
             for lam in (50, 200, 800):
@@ -275,7 +275,7 @@ def run_served_replicas(ctx, seconds: float, rank: int, world: int) -> dict | No
     mine = [s for s, o in zip(scenes, owner) if o == rank]
     out = {"workload": "config4 replicas: scenes split by the owner map, one continuous-batching server per GPU",
            "scenes_per_rank": [owner.count(r) for r in range(world)]}
-    with rt.Server(ctx, 120 << 30, max_inflight=128, keep_images=False) as srv:
+    with rt.Server(ctx, 120 << 30, max_inflight=256, keep_images=False) as srv:
         for sc in mine:
             srv.add_scene(sc)
         for lam in (50, 200, 800, 20000):

@@ -6,6 +6,7 @@
 // (Model.cpp:402-480); one render = the parallelRT tile loop (RayTracer.cpp:5-45) over every
 // pixel, as a wavefront of raygen -> (extend -> shade -> shadow) x (maxLevel+1) -> resolve.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -727,6 +728,8 @@ int ws_ensure(rt_ctx *ctx, Workspace &ws, long long qcap, int njobs)
     qcap = std::max(qcap, ws.qcap);
     njobs = std::max(njobs, ws.jobcap);
     cudaStreamSynchronize(ctx->stream);
+    static std::atomic<unsigned long long> layouts{0};   // process-wide: no two layouts share a number
+    ws.gen = ++layouts;
     size_t off = 0;
     auto take = [&](size_t bytes) {
         size_t o = off;
@@ -865,9 +868,9 @@ void enqueue_levels(rt_ctx *ctx, Workspace &ws, int max_level, const Tuning &t, 
 static int plain_graph(rt_ctx *ctx, int max_level, const Tuning &t, cudaGraphExec_t &exec)
 {
     Workspace &ws = ctx->ws;
-    if (ctx->plain_graph_ws != ws.mem.p) {
+    if (ctx->plain_graph_gen != ws.gen) {
         ctx->plain_graphs.clear();
-        ctx->plain_graph_ws = ws.mem.p;
+        ctx->plain_graph_gen = ws.gen;
     }
     const long long key = ((long long)max_level << 40) ^ ((long long)t.block << 24) ^ ((long long)t.tile << 8) ^
                           (long long)t.stack ^ ((long long)t.dynamic << 50) ^ ((long long)t.min_blocks << 52) ^

@@ -64,6 +64,9 @@ struct Workspace {
     rtg::DevScene *scenes = nullptr;
     long long qcap = 0;
     int jobcap = 0;
+    // layout generation: bumped whenever the arrays move. A reallocation can return the old
+    // address, so graphs captured against the workspace are keyed on this, not on mem.p.
+    unsigned long long gen = 0;
 };
 
 struct Pending {
@@ -220,7 +223,7 @@ struct rt_ctx {
     KernelProfiler prof;
     std::unique_ptr<WaveRunner> batch;   // workspace + graphs of rt_batch_render
     std::map<long long, std::unique_ptr<GraphEntry>> plain_graphs;   // level loops of rt_render
-    void *plain_graph_ws = nullptr;      // workspace the plain graphs point into
+    unsigned long long plain_graph_gen = 0;   // workspace layout the plain graphs point into (0 = none)
     void *plain_stage = nullptr;         // page-locked staging of the plain job tables
     cudaEvent_t ev_staged = nullptr;     // the last staging copy
     std::vector<DevBuf> spare;           // released scene / frame buffers kept for reuse

@@ -90,6 +90,17 @@ struct SplitMix {
 
 const int kServeRes[4][2] = {{256, 256}, {512, 512}, {1024, 768}, {1920, 1080}};
 
+// Frame tables of the per-step prepare and resolve launches (every request admitted in a step
+// is prepared by one launch, every request finished in a step is resolved by one): pinned host
+// copies in a small ring, each rewritten once the copy out of it has run.
+struct TableRing {
+    static constexpr int kSlots = 4;
+    FrameJob *host[kSlots] = {};
+    DevBuf dev[kSlots];
+    cudaEvent_t copied[kSlots] = {};
+    int cap = 0, next = 0;
+};
+
 } // namespace
 
 struct rt_server {
@@ -109,6 +120,9 @@ struct rt_server {
     std::deque<Request *> resolving;    // enqueue order
     std::unordered_map<int64_t, std::unique_ptr<Request>> reqs;
     std::vector<cudaEvent_t> ev_pool;
+    TableRing tables;
+    std::vector<FrameJob> to_prepare, to_resolve;   // this step's frames
+    std::vector<Request *> resolved;                // requests of to_resolve
     int64_t next_id = 0;
     uint64_t tick = 0;
     int64_t fixed_bytes = 0, peak_bytes = 0;
@@ -264,7 +278,7 @@ static int admit(rt_server *srv)
         r->wj.cursor = 0;
         r->wj.weight = wave_weight(sd.branching, srv->cfg.max_level);
         CK(ctx, cudaStreamWaitEvent(ctx->stream, slot.copied, 0));   // the previous image left the slot
-        launch_frame_prepare(frame_job(slot.fb, r->req.width, r->req.height, r->wj.job), ctx->stream);
+        srv->to_prepare.push_back(frame_job(slot.fb, r->req.width, r->req.height, r->wj.job));
         slot.used = true;
         srv->hslots[(size_t)hs].used = true;
         r->dev_slot = ds, r->host_slot = hs;
@@ -279,33 +293,78 @@ static int admit(rt_server *srv)
     return RT_OK;
 }
 
-// the last chunk of r is enqueued: resolve, copy out on the copy stream, free the device slot
-static int finish(rt_server *srv, Request *r)
+// one launch over this step's frames of `jobs` (prepare, or resolve), its table staged through
+// the ring
+static int launch_frames(rt_server *srv, std::vector<FrameJob> &jobs, bool resolve)
 {
     rt_ctx *ctx = srv->ctx;
-    DevSlot &slot = srv->dslots[(size_t)r->dev_slot];
-    HostSlot &hs = srv->hslots[(size_t)r->host_slot];
-    const size_t np = (size_t)r->req.width * r->req.height;
-    FrameBufs out = slot.fb;
-    if (!srv->cfg.keep_images) out.rgb = nullptr;   // the client gets bytes: no float colour written
-    launch_resolve(out, r->req.width, r->req.height, srv->cfg.spp, ctx->stream);
+    if (jobs.empty()) return RT_OK;
+    TableRing &T = srv->tables;
+    const int k = T.next;
+    T.next = (k + 1) % TableRing::kSlots;
+    if (!T.copied[k]) CK(ctx, cudaEventCreateWithFlags(&T.copied[k], cudaEventDisableTiming));
+    CK(ctx, cudaEventSynchronize(T.copied[k]));   // the previous copy out of this host table ran
+    if ((int)jobs.size() > T.cap) return srv_fail(srv, RT_ERR_INVALID, "%zu frames in one step", jobs.size());
+    long long quads = 0;
+    for (size_t i = 0; i < jobs.size(); ++i) {
+        quads += jobs[i].quad_end;   // frame_job sets quad_end to the frame's own quads
+        jobs[i].quad_end = quads;
+        T.host[k][i] = jobs[i];
+    }
+    CK(ctx, cudaMemcpyAsync(T.dev[k].p, T.host[k], sizeof(FrameJob) * jobs.size(), cudaMemcpyHostToDevice, ctx->stream));
+    CK(ctx, cudaEventRecord(T.copied[k], ctx->stream));
+    const FrameJob *d = (const FrameJob *)T.dev[k].p;
+    if (resolve) launch_frames_resolve(d, (int)jobs.size(), quads, ctx->stream);
+    else launch_frames_prepare(d, (int)jobs.size(), quads, ctx->stream);
     CK(ctx, cudaGetLastError());
+    jobs.clear();
+    return RT_OK;
+}
+
+// the last chunk of r is enqueued: free its device slot; its resolve and copy-out follow in
+// resolve_finished
+static int finish(rt_server *srv, Request *r)
+{
+    DevSlot &slot = srv->dslots[(size_t)r->dev_slot];
+    FrameJob F = frame_job(slot.fb, r->req.width, r->req.height, r->wj.job);
+    F.dp_bits = 0;
+    if (!srv->cfg.keep_images) F.fb.rgb = nullptr;   // the client gets bytes: no float colour written
+    srv->to_resolve.push_back(F);
+    srv->resolved.push_back(r);
+    return RT_OK;
+}
+
+// resolve the frames finished in this step with one launch, then copy each out on the copy
+// stream; a slot is reused only after its copy (slot.copied)
+static int resolve_finished(rt_server *srv)
+{
+    rt_ctx *ctx = srv->ctx;
+    if (srv->resolved.empty()) return RT_OK;
+    int rc = launch_frames(srv, srv->to_resolve, true);
+    if (rc) return rc;
     cudaEvent_t resolved = take_event(srv);
     CK(ctx, cudaEventRecord(resolved, ctx->stream));
     CK(ctx, cudaStreamWaitEvent(srv->copy, resolved, 0));
     srv->ev_pool.push_back(resolved);   // re-recording later does not affect the wait above
-    // the frame a client receives is the uint8 image (Color::put); float colour only when the
-    // server keeps images for inspection
-    if (srv->cfg.keep_images) CK(ctx, cudaMemcpyAsync(hs.rgb, slot.fb.rgb, 12 * np, cudaMemcpyDeviceToHost, srv->copy));
-    CK(ctx, cudaMemcpyAsync(hs.rgb8, slot.fb.rgb8, 3 * np, cudaMemcpyDeviceToHost, srv->copy));
-    CK(ctx, cudaEventRecord(slot.copied, srv->copy));
-    r->done_ev = take_event(srv);
-    CK(ctx, cudaEventRecord(r->done_ev, srv->copy));
-    slot.used = false;   // reuse waits on slot.copied
-    r->dev_slot = -1;
-    srv->scenes[(size_t)r->scene].users--;
-    r->state = kResolving;
-    srv->resolving.push_back(r);
+    for (Request *r : srv->resolved) {
+        DevSlot &slot = srv->dslots[(size_t)r->dev_slot];
+        HostSlot &hs = srv->hslots[(size_t)r->host_slot];
+        const size_t np = (size_t)r->req.width * r->req.height;
+        // the frame a client receives is the uint8 image (Color::put); float colour only when
+        // the server keeps images for inspection
+        if (srv->cfg.keep_images)
+            CK(ctx, cudaMemcpyAsync(hs.rgb, slot.fb.rgb, 12 * np, cudaMemcpyDeviceToHost, srv->copy));
+        CK(ctx, cudaMemcpyAsync(hs.rgb8, slot.fb.rgb8, 3 * np, cudaMemcpyDeviceToHost, srv->copy));
+        CK(ctx, cudaEventRecord(slot.copied, srv->copy));
+        r->done_ev = take_event(srv);
+        CK(ctx, cudaEventRecord(r->done_ev, srv->copy));
+        slot.used = false;   // reuse waits on slot.copied
+        r->dev_slot = -1;
+        srv->scenes[(size_t)r->scene].users--;
+        r->state = kResolving;
+        srv->resolving.push_back(r);
+    }
+    srv->resolved.clear();
     return RT_OK;
 }
 
@@ -434,6 +493,8 @@ static int step_batched(rt_server *srv)
         if (rc) return rc;
         wave_order(srv, order);
     }
+    rc = launch_frames(srv, srv->to_prepare, false);   // the admitted frames, before their first wave
+    if (rc) return rc;
     if (!order.empty()) {
         long long got = 0;
         rc = wave_enqueue(ctx, srv->runner, order, srv->tuning, true, ctx->stream, &got);
@@ -447,6 +508,8 @@ static int step_batched(rt_server *srv)
                 still.push_back(r);
         }
         srv->inflight.swap(still);
+        rc = resolve_finished(srv);
+        if (rc) return rc;
         note_peak(srv);
     }
     return RT_OK;
@@ -558,14 +621,16 @@ static int server_init(rt_server *srv)
     const size_t P = (size_t)c.max_pixels;
     const int n_slots = c.plain ? 1 : c.max_inflight;
     srv->dslots.resize(c.plain ? 0 : (size_t)n_slots);
+    // a server that keeps no images hands out bytes only: its slots hold no float colour
+    const bool keep = c.keep_images != 0;
     for (DevSlot &d : srv->dslots) {
         // accumulators, colour, bytes, and the camera axis table (at most 16384 + 16384 entries)
-        size_t o_rgb = (24 * P + 255) & ~(size_t)255, o_rgb8 = o_rgb + ((12 * P + 255) & ~(size_t)255);
+        size_t o_rgb = (24 * P + 255) & ~(size_t)255, o_rgb8 = o_rgb + (keep ? (12 * P + 255) & ~(size_t)255 : 0);
         size_t o_axis = o_rgb8 + ((3 * P + 255) & ~(size_t)255);
         CK(ctx, d.mem.ensure(o_axis + 4 * 32768));
         char *b = (char *)d.mem.p;
         d.fb.acc = (long long *)b;
-        d.fb.rgb = (float *)(b + o_rgb);
+        d.fb.rgb = keep ? (float *)(b + o_rgb) : nullptr;
         d.fb.rgb8 = (uint8_t *)(b + o_rgb8);
         d.fb.axis = (float *)(b + o_axis);
         CK(ctx, cudaEventCreate(&d.copied));
@@ -574,11 +639,18 @@ static int server_init(rt_server *srv)
     }
     srv->hslots.resize((size_t)n_slots);
     for (HostSlot &h : srv->hslots) {
-        CK(ctx, cudaHostAlloc(&h.mem, 15 * P, cudaHostAllocDefault));
-        h.rgb = (float *)h.mem;
-        h.rgb8 = (uint8_t *)h.mem + 12 * P;
+        CK(ctx, cudaHostAlloc(&h.mem, (keep ? 15 : 3) * P, cudaHostAllocDefault));
+        h.rgb = keep ? (float *)h.mem : nullptr;
+        h.rgb8 = (uint8_t *)h.mem + (keep ? 12 * P : 0);
     }
     if (!c.plain) {
+        TableRing &T = srv->tables;
+        T.cap = c.max_inflight;
+        for (int k = 0; k < TableRing::kSlots; ++k) {
+            CK(ctx, cudaHostAlloc((void **)&T.host[k], sizeof(FrameJob) * (size_t)T.cap, cudaHostAllocDefault));
+            CK(ctx, T.dev[k].ensure(sizeof(FrameJob) * (size_t)T.cap));
+            srv->fixed_bytes += (int64_t)T.dev[k].bytes;
+        }
         int rc = wave_runner_init(ctx, srv->runner, c.queue_rays, c.max_inflight, c.stages);
         if (rc) return rc;
         srv->fixed_bytes += (int64_t)wave_runner_bytes(srv->runner);
@@ -631,6 +703,10 @@ void rt_server_destroy(rt_server *srv)
     for (auto &kv : srv->reqs)
         if (kv.second->done_ev) cudaEventDestroy(kv.second->done_ev);
     for (cudaEvent_t e : srv->ev_pool) cudaEventDestroy(e);
+    for (int k = 0; k < TableRing::kSlots; ++k) {
+        if (srv->tables.copied[k]) cudaEventDestroy(srv->tables.copied[k]);
+        if (srv->tables.host[k]) cudaFreeHost(srv->tables.host[k]);
+    }
     if (srv->base_ev) cudaEventDestroy(srv->base_ev);
     if (srv->copy) cudaStreamDestroy(srv->copy);
     delete srv;

@@ -57,6 +57,39 @@ def test_batch_equals_plain_renders(ctx):
             ctx.release_scene(s)
 
 
+def test_plain_render_after_workspace_growth():
+    """A render whose frame needs a larger ray workspace than the last one re-lays the
+    workspace out; the cached launch graph must follow even when the new allocation comes back
+    at the old address. Each frame rendered after others must equal its render in a fresh
+    context."""
+    scenes = small_scenes()[:3]
+    sizes = [(48, 32), (160, 120), (64, 48)]
+
+    def render_all(c, order):
+        out = {}
+        for k in order:
+            sid = c.upload(scenes[k])
+            fid = c.frame(*sizes[k])
+            c.render(sid, fid, c.render_desc(*sizes[k], 1, 3))
+            out[k] = c.download(fid, *sizes[k], planes=False)["rgb"].copy()
+            c.release_frame(fid)
+            c.release_scene(sid)
+        return out
+
+    seq = rt.Context(0)
+    try:
+        got = render_all(seq, [0, 1, 2, 0])   # grows at 1; 2 and the second 0 reuse the grown layout
+    finally:
+        seq.close()
+    for k in range(3):
+        fresh = rt.Context(0)
+        try:
+            want = render_all(fresh, [k])[k]
+        finally:
+            fresh.close()
+        assert np.array_equal(got[k], want), k
+
+
 def test_batch_jittered_depth4_equals_plain(ctx):
     scenes = small_scenes()[:2]
     sids = [ctx.upload(s) for s in scenes]
