@@ -1079,11 +1079,11 @@ int orc_morton_sort(const float *tri_p, int64_t n, uint32_t *codes, uint32_t *pe
             smx[k] = std::fmax(smx[k], mx);
         }
     }
-    float scale[3];
-    for (int k = 0; k < 3; ++k) {
-        float ext = smx[k] - smn[k];
-        scale[k] = ext > 0.0f ? 1024.0f / ext : 0.0f;
-    }
+    // one scale for all axes: the largest extent of the box / 1024 (cubic cells)
+    float emax = 0.0f;
+    for (int k = 0; k < 3; ++k) emax = std::fmax(emax, smx[k] - smn[k]);
+    const float s = emax > 0.0f ? 1024.0f / emax : 0.0f;
+    const float scale[3] = {s, s, s};
     std::vector<uint32_t> code((size_t)n);
     for (int64_t i = 0; i < n; ++i) {
         uint32_t q[3];

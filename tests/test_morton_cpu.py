@@ -12,8 +12,8 @@ def numpy_morton(tri):
     mx = np.maximum(a, np.maximum(b, c))
     cen = (mn + mx) * np.float32(0.5)
     smn, smx = mn.min(axis=0), mx.max(axis=0)
-    ext = smx - smn
-    scale = np.where(ext > 0, np.float32(1024) / np.where(ext > 0, ext, 1), 0).astype(np.float32)
+    emax = (smx - smn).max()   # one scale for all axes: cubic cells over the scene box
+    scale = np.float32(1024) / emax if emax > 0 else np.float32(0)
     q = np.clip(((cen - smn) * scale).astype(np.int64), 0, 1023).astype(np.uint32)
 
     def expand(v):
