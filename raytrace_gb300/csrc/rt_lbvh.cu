@@ -389,37 +389,63 @@ __global__ void k_refit(int n, float4 *nodes, const int *parent, int *flags)
 }
 
 // A 4-wide node for every internal node i: the slots are i's grandchildren — each child's two
-// children when the child is internal, the child itself when it is a leaf — so 2 to 4 slots.
-// Traversal starts at the root and steps from a node to its grandchildren, so it only ever
-// visits even depths: the binary tree collapsed two levels at a time, with no depth pass.
+// children when the child is internal, the child itself when it is a leaf — and when a leaf
+// child leaves a slot free, the internal grandchild with the largest surface area is replaced
+// by its two children. Every internal slot is thus two or three binary levels below i: a path
+// of at most 63 binary levels takes at most 32 four-wide steps of at most 3 pushes each.
+// Traversal starts at the root and steps from a node to its slots (every internal node has a
+// record, so any descendant can be a slot).
 // Record (128 B, one line): float4 lo.x[4], hi.x[4], lo.y[4], hi.y[4], lo.z[4], hi.z[4], then
 // int4 refs (>= 0 internal node, < 0 leaf ~k, kEmptySlot unused), then padding. An unused
 // slot's box is the point (1e38, 1e38, 1e38), which no ray reaches within a cull distance.
+__device__ __forceinline__ float half_area(const float4 *nodes, int x)
+{
+    const float4 l = __ldcg(&nodes[2ll * x]), h = __ldcg(&nodes[2ll * x + 1]);
+    const float dx = h.x - l.x, dy = h.y - l.y, dz = h.z - l.z;
+    return dx * dy + dy * dz + dz * dx;
+}
+
 __global__ void k_quads(int n, const float4 *nodes, float4 *quads)
 {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n - 1; i += gridDim.x * blockDim.x) {
-        float lo[3][4], hi[3][4];
-        int ref[4];
+        int slot[4];
         int k = 0;
         const int c[2] = {__float_as_int(nodes[2ll * i].w), __float_as_int(nodes[2ll * i + 1].w)};
-        auto put = [&](int x) {
-            const float4 l = __ldcg(&nodes[2ll * x]), h = __ldcg(&nodes[2ll * x + 1]);
-            lo[0][k] = l.x, lo[1][k] = l.y, lo[2][k] = l.z;
-            hi[0][k] = h.x, hi[1][k] = h.y, hi[2][k] = h.z;
-            ref[k] = x >= n - 1 ? ~(x - (n - 1)) : x;
-            ++k;
-        };
         for (int j = 0; j < 2; ++j) {
             if (c[j] >= n - 1) {
-                put(c[j]);
+                slot[k++] = c[j];
             } else {
-                put(__float_as_int(__ldcg(&nodes[2ll * c[j]]).w));
-                put(__float_as_int(__ldcg(&nodes[2ll * c[j] + 1]).w));
+                slot[k++] = __float_as_int(__ldcg(&nodes[2ll * c[j]]).w);
+                slot[k++] = __float_as_int(__ldcg(&nodes[2ll * c[j] + 1]).w);
             }
         }
-        for (; k < 4; ++k) {   // a point at 1e38: its entry distance exceeds every cull (<= 1e20)
-            for (int a = 0; a < 3; ++a) lo[a][k] = hi[a][k] = 1e38f;
-            ref[k] = kEmptySlot;
+        if (k == 3) {   // one leaf child: split the largest internal grandchild
+            int best = -1;
+            float area = -1.0f;
+            for (int j = 0; j < 3; ++j)
+                if (slot[j] < n - 1) {
+                    const float a = half_area(nodes, slot[j]);
+                    if (a > area) area = a, best = j;
+                }
+            if (best >= 0) {
+                const int x = slot[best];
+                slot[best] = __float_as_int(__ldcg(&nodes[2ll * x]).w);
+                slot[k++] = __float_as_int(__ldcg(&nodes[2ll * x + 1]).w);
+            }
+        }
+        float lo[3][4], hi[3][4];
+        int ref[4];
+        for (int j = 0; j < 4; ++j) {
+            if (j < k) {
+                const int x = slot[j];
+                const float4 l = __ldcg(&nodes[2ll * x]), h = __ldcg(&nodes[2ll * x + 1]);
+                lo[0][j] = l.x, lo[1][j] = l.y, lo[2][j] = l.z;
+                hi[0][j] = h.x, hi[1][j] = h.y, hi[2][j] = h.z;
+                ref[j] = x >= n - 1 ? ~(x - (n - 1)) : x;
+            } else {   // a point at 1e38: its entry distance exceeds every cull (<= 1e20)
+                for (int a = 0; a < 3; ++a) lo[a][j] = hi[a][j] = 1e38f;
+                ref[j] = kEmptySlot;
+            }
         }
         float4 *q = quads + 8ll * i;
         for (int a = 0; a < 3; ++a) {
