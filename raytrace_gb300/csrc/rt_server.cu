@@ -114,6 +114,10 @@ struct rt_server {
     Tuning tuning;
     std::vector<SrvScene> scenes;
     std::vector<DevSlot> dslots;
+    // free frame slots, oldest freed first: a slot's image copy to the host must finish before
+    // the next request's resolve writes it, and the oldest copy is the likeliest to have
+    // finished (waiting for the copies of the slots freed last had stalled the compute stream)
+    std::deque<int> free_dslots;
     std::vector<HostSlot> hslots;
     std::deque<Request *> queue;
     std::vector<Request *> inflight;    // admission order
@@ -219,12 +223,6 @@ static int make_resident(rt_server *srv, int k, int *rebuilt)
     return RT_OK;
 }
 
-static int find_free(const std::vector<DevSlot> &v)
-{
-    for (size_t i = 0; i < v.size(); ++i)
-        if (!v[i].used) return (int)i;
-    return -1;
-}
 static int find_free(const std::vector<HostSlot> &v)
 {
     for (size_t i = 0; i < v.size(); ++i)
@@ -246,7 +244,7 @@ static int admit(rt_server *srv)
     rt_ctx *ctx = srv->ctx;
     while (!srv->queue.empty()) {
         Request *r = srv->queue.front();
-        const int ds = find_free(srv->dslots), hs = find_free(srv->hslots);
+        const int ds = srv->free_dslots.empty() ? -1 : srv->free_dslots.front(), hs = find_free(srv->hslots);
         if (ds < 0 || hs < 0) break;
         int rebuilt = 0;
         int rc = make_resident(srv, r->scene, &rebuilt);
@@ -277,9 +275,9 @@ static int admit(rt_server *srv)
         r->wj.total = samples;
         r->wj.cursor = 0;
         r->wj.weight = wave_weight(sd.branching, srv->cfg.max_level);
-        CK(ctx, cudaStreamWaitEvent(ctx->stream, slot.copied, 0));   // the previous image left the slot
         srv->to_prepare.push_back(frame_job(slot.fb, r->req.width, r->req.height, r->wj.job));
         slot.used = true;
+        srv->free_dslots.pop_front();
         srv->hslots[(size_t)hs].used = true;
         r->dev_slot = ds, r->host_slot = hs;
         r->rebuilt = rebuilt;
@@ -340,6 +338,9 @@ static int resolve_finished(rt_server *srv)
 {
     rt_ctx *ctx = srv->ctx;
     if (srv->resolved.empty()) return RT_OK;
+    // the resolve writes the slots' images: the previous images must have left them (the
+    // prepare at admission writes only accumulators and axis tables, which no copy reads)
+    for (Request *r : srv->resolved) CK(ctx, cudaStreamWaitEvent(ctx->stream, srv->dslots[(size_t)r->dev_slot].copied, 0));
     int rc = launch_frames(srv, srv->to_resolve, true);
     if (rc) return rc;
     cudaEvent_t resolved = take_event(srv);
@@ -359,6 +360,7 @@ static int resolve_finished(rt_server *srv)
         r->done_ev = take_event(srv);
         CK(ctx, cudaEventRecord(r->done_ev, srv->copy));
         slot.used = false;   // reuse waits on slot.copied
+        srv->free_dslots.push_back(r->dev_slot);
         r->dev_slot = -1;
         srv->scenes[(size_t)r->scene].users--;
         r->state = kResolving;
@@ -621,6 +623,7 @@ static int server_init(rt_server *srv)
     const size_t P = (size_t)c.max_pixels;
     const int n_slots = c.plain ? 1 : c.max_inflight;
     srv->dslots.resize(c.plain ? 0 : (size_t)n_slots);
+    for (size_t i = 0; i < srv->dslots.size(); ++i) srv->free_dslots.push_back((int)i);
     // a server that keeps no images hands out bytes only: its slots hold no float colour
     const bool keep = c.keep_images != 0;
     for (DevSlot &d : srv->dslots) {
