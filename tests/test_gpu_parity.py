@@ -73,6 +73,42 @@ def test_gpu_matches_oracle_small(ctx, seed, n_spheres, ico, refr):
     assert not ((d > TOL) & ~a).any(), d[~a].max()
 
 
+def _without_planes(scene: rt.SceneHost, camera: rt.Camera) -> rt.SceneHost:
+    """A copy of `scene` seen through `camera`, with its planes hidden: every primitive is then
+    inside the LBVH, and rays that leave the scene miss everything."""
+    d = rt.SceneDesc.from_buffer_copy(scene.desc)
+    objs = (rt.Object * d.n_objects)()
+    for k in range(d.n_objects):
+        objs[k] = d.objects[k]
+        if objs[k].type == rt.RT_OBJECT_PLANE:
+            objs[k].show = 0
+    d.objects = objs
+    d.camera = camera
+    out = rt.SceneHost.from_desc(d, *scene.params)
+    return out
+
+
+@pytest.mark.parametrize("dist,az,el", [(1.0, 0.0, 11.3), (3.5, 130.0, 35.0), (0.15, 250.0, 20.0)])
+def test_cameras_outside_and_inside_the_scene_match_oracle(ctx, dist, az, el):
+    """A plane-free scene (all primitives in the LBVH) from orbit cameras: the scene's own
+    distance, a far camera (a small object, most rays leave the scene at once) and a camera
+    inside the scene's box. Full frames against the brute-force oracle."""
+    w, h = 96, 64
+    base = rt.SceneHost.small(5, 10, 6, w, h, 3)
+    cam = rt.orbit_camera(base.desc.camera, az, el, w, h)
+    for k in range(3):
+        cam.position[k] *= dist
+    scene = _without_planes(base, cam)
+    out, _ = gpu_render(ctx, scene, w, h, 1, 3, 0, ref_tiles=False)
+    ref = port.render(scene, w, h, 1, 3, 0, ref_tiles=False, check=True)
+    a = ref["ambiguous"]
+    ids_equal = (out["obj"] == ref["obj"]) & (out["prim"] == ref["prim"])
+    assert not (~ids_equal & ~a).any()
+    d = np.abs(out["rgb"] - ref["rgb"]).max(axis=2)
+    assert not ((d > TOL) & ~a).any(), d[~a].max()
+    assert (ref["obj"] >= 0).any() and (ref["obj"] < 0).any()   # both hits and misses in the frame
+
+
 def test_gpu_matches_oracle_jitter_depth4(ctx):
     w, h = 64, 64
     scene = rt.SceneHost.small(21, 14, 5, w, h, 2)
