@@ -173,7 +173,7 @@ struct ShadowQueue {
 // device counters of one wavefront pass
 struct Counters {
     int q_count[2];                       // ping-pong ray queue sizes
-    int s_count;                          // shadow queue size
+    int pad0;
     int overflow;                         // a queue ran out of space
     int work[16];                         // dynamic work counters (reset per pass)
     int h_count[8];                       // hits listed by extend, per bounce

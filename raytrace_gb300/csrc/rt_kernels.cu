@@ -196,9 +196,8 @@ __global__ void __launch_bounds__(MINB ? 128 : 256, MINB ? MINB : 1) k_extend(Wa
     Counters *C = wf.C;
     const RayQueue q = wf.q[sel];
     const long long total = GEN ? *wf.total_samples : 0, first = GEN ? *wf.sample_offset : 0;
-    if (blockIdx.x == 0 && threadIdx.x == 0) {   // the next queue and the shadow queue fill in shade
+    if (blockIdx.x == 0 && threadIdx.x == 0) {   // the next queue fills in shade
         C->q_count[sel ^ 1] = 0;
-        C->s_count = 0;
         if (GEN) {
             C->q_count[sel] = (int)min(total, (long long)q.capacity);
             C->rays_primary = (unsigned long long)total;
@@ -541,24 +540,19 @@ __global__ void __launch_bounds__(128, 5) k_shade(Wavefront wf, int sel, int wsl
                 }
             }
         }
-        // warp-aggregated appends: one atomic per warp for the shadow queue and one for the rays
-        const unsigned bs = __ballot_sync(kFull, emit);
-        if (bs) {
-            int base = 0;
-            if (lane == 0) base = atomicAdd(&C->s_count, __popc(bs));
-            base = __shfl_sync(kFull, base, 0);
+        // the shadow record of hit j goes to slot j, with no atomic: a single counter that every
+        // warp reserves from serialises at one L2 slice. A hit without a record marks its slot
+        // empty (job -1) and the shadow kernel skips it.
+        if (active) {
             if (emit) {
-                const int slot = base + __popc(bs & lt);
-                if (slot < sq.capacity) {
-                    sq.p[slot] = make_float4(P.x, P.y, P.z, __int_as_float(pix));
-                    sq.n[slot] = make_float4(N.x, N.y, N.z, __int_as_float(mtl_id));
-                    sq.v[slot] = make_float4(D.x, D.y, D.z, __int_as_float(nob));
-                    sq.wc[slot] = make_float4(Wc.x, Wc.y, Wc.z, __int_as_float(job));
-                    const V3 Wl = vscale(W, wl);
-                    sq.ws[slot] = make_float4(Wl.x, Wl.y, Wl.z, 0.0f);
-                } else
-                    atomicExch(&C->overflow, 1);
-            }
+                sq.p[j] = make_float4(P.x, P.y, P.z, __int_as_float(pix));
+                sq.n[j] = make_float4(N.x, N.y, N.z, __int_as_float(mtl_id));
+                sq.v[j] = make_float4(D.x, D.y, D.z, __int_as_float(nob));
+                sq.wc[j] = make_float4(Wc.x, Wc.y, Wc.z, __int_as_float(job));
+                const V3 Wl = vscale(W, wl);
+                sq.ws[j] = make_float4(Wl.x, Wl.y, Wl.z, 0.0f);
+            } else
+                sq.wc[j] = make_float4(0.0f, 0.0f, 0.0f, __int_as_float(-1));
         }
         // children: the reflected rays of the warp, then its refracted rays
         const unsigned b1 = __ballot_sync(kFull, c_refl), b2 = __ballot_sync(kFull, c_refr);
@@ -609,7 +603,8 @@ __global__ void __launch_bounds__(MINB ? 128 : 256, MINB ? MINB : 1) k_shadow(Wa
     if (cancelled(wf.cancel)) return;
     Counters *C = wf.C;
     const ShadowQueue sq = wf.sq;
-    const int n = min(C->s_count, sq.capacity);
+    // slot i holds the shadow record of hit i of this bounce, or is empty (job -1)
+    const int n = min(C->h_count[wslot / 3], sq.capacity);
     const int nl = (int)*wf.max_lights;
     WorkCount wc{0, 0, 0, 0};
     unsigned long long rays = 0;
@@ -619,6 +614,7 @@ __global__ void __launch_bounds__(MINB ? 128 : 256, MINB ? MINB : 1) k_shadow(Wa
         if (!active) return;
         const int l = w / n, i = w - l * n;
         const int job = __float_as_int(sq.wc[i].w);
+        if (job < 0) return;
         const DevScene &S = wf.scenes[wf.jobs[job].scene];
         if (l >= S.n_lights) return;
         const DevLight &L = S.lights[l];
