@@ -198,6 +198,9 @@ __global__ void __launch_bounds__(MINB ? 128 : 256, MINB ? MINB : 1) k_extend(Wa
     const long long total = GEN ? *wf.total_samples : 0, first = GEN ? *wf.sample_offset : 0;
     if (blockIdx.x == 0 && threadIdx.x == 0) {   // the next queue fills in shade
         C->q_count[sel ^ 1] = 0;
+        // the rays of this queue are the children the last shading spawned (counted once here,
+        // not by an atomic per warp on one address)
+        if (!GEN) C->rays_secondary += (unsigned long long)C->q_count[sel];
         if (GEN) {
             C->q_count[sel] = (int)min(total, (long long)q.capacity);
             C->rays_primary = (unsigned long long)total;
@@ -559,10 +562,7 @@ __global__ void __launch_bounds__(128, 5) k_shade(Wavefront wf, int sel, int wsl
         const int tot = __popc(b1) + __popc(b2);
         if (tot) {
             int base = 0;
-            if (lane == 0) {
-                base = atomicAdd(&C->q_count[sel ^ 1], tot);
-                atomicAdd(&C->rays_secondary, (unsigned long long)tot);
-            }
+            if (lane == 0) base = atomicAdd(&C->q_count[sel ^ 1], tot);
             base = __shfl_sync(kFull, base, 0);
             if (c_refl) {
                 const int slot = base + __popc(b1 & lt);
