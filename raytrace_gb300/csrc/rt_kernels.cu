@@ -80,28 +80,29 @@ __device__ __forceinline__ void for_each_ray(int n, int *work, int tile, F &&bod
     }
 }
 
-// for_each_ray_guided: for cheap, even work (shading). Chunks take a share of what is left
-// (left / (2 x warps), at least `tile` rays): few atomics on the one counter address, where
-// they serialise. The counter ends below 1.5 n + 32 x warps.
+// Block-uniform loop over [0, n) in steps of blockDim.x items, one per thread: every thread of a
+// block runs the body the same number of times, so the body may synchronise the block. Chunks
+// come from a counter, a share of what is left (DYN), or by grid stride.
 template <bool DYN, class F>
-__device__ __forceinline__ void for_each_ray_guided(int n, int *work, int tile, F &&body)
+__device__ __forceinline__ void for_each_block_step(int n, int *work, F &&body)
 {
+    __shared__ int s_start;
+    const int B = blockDim.x;
     if (!DYN) {
-        for_each_ray<false>(n, work, tile, body);
+        for (long long base = (long long)blockIdx.x * B; base < n; base += (long long)gridDim.x * B)
+            body((int)base + (int)threadIdx.x, base + threadIdx.x < n);
         return;
     }
-    const int lane = threadIdx.x & 31;
-    const int nw = gridDim.x * (blockDim.x >> 5);
-    int chunk = max(tile, ((n / (2 * nw)) + 31) & ~31);
+    int chunk = max(B, ((n / (2 * (int)gridDim.x)) + B - 1) / B * B);
     while (true) {
-        int start = 0;
-        if (lane == 0) start = atomicAdd(work, chunk);
-        start = __shfl_sync(kFull, start, 0);
+        if (threadIdx.x == 0) s_start = atomicAdd(work, chunk);
+        __syncthreads();
+        const int start = s_start;
+        __syncthreads();   // s_start is written again by the next round
         if (start >= n) break;
         const int end = min(start + chunk, n);
-        for (int base = start; base < end; base += 32)
-            body(base + lane, base + lane < end);
-        chunk = max(tile, (((n - end) / (2 * nw)) + 31) & ~31);
+        for (int base = start; base < end; base += B) body(base + (int)threadIdx.x, base + (int)threadIdx.x < end);
+        chunk = max(B, (((n - end) / (2 * (int)gridDim.x)) + B - 1) / B * B);
     }
 }
 
@@ -380,11 +381,17 @@ __global__ void __launch_bounds__(128, 5) k_shade(Wavefront wf, int sel, int wsl
     const ShadowQueue sq = wf.sq;
     // the hits of this bounce (a miss needs no shading: the hit planes start as misses)
     const int n = min(C->h_count[wslot / 3], q.capacity);
-    const int lane = threadIdx.x & 31;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, warps = blockDim.x >> 5;
     const unsigned lt = (1u << lane) - 1u;
-    for_each_ray_guided<DYN>(n, &C->work[wslot], tile, [&](int j, bool active) {
-        // what the hit emits is decided first and written after the warp has reserved queue
-        // slots, so only the inputs of the records stay live across the ballots
+    // children of a block step: per-warp counts (reflected, refracted) and the block's base,
+    // double-buffered by step parity
+    __shared__ int s_cnt[2][8][2];
+    __shared__ int s_base[2];
+    int step = 0;
+    (void)tile;
+    for_each_block_step<DYN>(n, &C->work[wslot], [&](int j, bool active) {
+        // what the hit emits is decided first and written after the block has reserved queue
+        // slots, so only the inputs of the records stay live across the reservation
         bool emit = false, c_refl = false, c_refr = false;
         V3 P, N, D, W, Wc;
         float wl = 1.0f;   // the local terms' share of W (Wl = W x wl)
@@ -557,15 +564,26 @@ __global__ void __launch_bounds__(128, 5) k_shade(Wavefront wf, int sel, int wsl
             } else
                 sq.wc[j] = make_float4(0.0f, 0.0f, 0.0f, __int_as_float(-1));
         }
-        // children: the reflected rays of the warp, then its refracted rays
+        // children: one reservation per block step (an atomic per warp on the one queue counter
+        // serialised at its L2 slice): the block's reflected rays in warp order, then its
+        // refracted rays
         const unsigned b1 = __ballot_sync(kFull, c_refl), b2 = __ballot_sync(kFull, c_refr);
-        const int tot = __popc(b1) + __popc(b2);
-        if (tot) {
-            int base = 0;
-            if (lane == 0) base = atomicAdd(&C->q_count[sel ^ 1], tot);
-            base = __shfl_sync(kFull, base, 0);
+        const int par = step & 1;
+        ++step;
+        if (lane == 0) s_cnt[par][warp][0] = __popc(b1), s_cnt[par][warp][1] = __popc(b2);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            int tot = 0;
+            for (int k = 0; k < warps; ++k) tot += s_cnt[par][k][0] + s_cnt[par][k][1];
+            s_base[par] = tot ? atomicAdd(&C->q_count[sel ^ 1], tot) : 0;
+        }
+        __syncthreads();
+        int off_r = s_base[par], off_t = s_base[par];
+        for (int k = 0; k < warps; ++k) off_t += s_cnt[par][k][0];
+        for (int k = 0; k < warp; ++k) off_r += s_cnt[par][k][0], off_t += s_cnt[par][k][1];
+        {
             if (c_refl) {
-                const int slot = base + __popc(b1 & lt);
+                const int slot = off_r + __popc(b1 & lt);
                 if (slot < qo.capacity) {
                     const float nn = __fmul_rn(2.0f, dot3(D, N));
                     const V3 R = normalise(vsub(D, vscale(N, nn)));
@@ -578,7 +596,7 @@ __global__ void __launch_bounds__(128, 5) k_shade(Wavefront wf, int sel, int wsl
                     atomicExch(&C->overflow, 1);
             }
             if (c_refr) {
-                const int slot = base + __popc(b1) + __popc(b2 & lt);
+                const int slot = off_t + __popc(b2 & lt);
                 if (slot < qo.capacity) {
                     const V3 l2 = vscale(D, eta);
                     const V3 l1 = vscale(N, __fsub_rn(__fmul_rn(eta, cosIn), __fsqrt_rn(cosOut2)));
