@@ -153,6 +153,10 @@ extern "C" int rt_ctx_create(int device, rt_ctx **out)
     if (cudaEventCreateWithFlags(&c->ev_staged, cudaEventDisableTiming) != cudaSuccess) return RT_ERR_CUDA;
     if (cudaEventRecord(c->ev_staged, c->stream) != cudaSuccess) return RT_ERR_CUDA;
     if (cudaEventCreateWithFlags(&c->ev_upload, cudaEventDisableTiming) != cudaSuccess) return RT_ERR_CUDA;
+    if (cudaStreamCreateWithFlags(&c->upload_side, cudaStreamNonBlocking) != cudaSuccess) return RT_ERR_CUDA;
+    if (cudaEventCreateWithFlags(&c->ev_upload_go, cudaEventDisableTiming) != cudaSuccess) return RT_ERR_CUDA;
+    if (cudaEventCreateWithFlags(&c->ev_shading, cudaEventDisableTiming) != cudaSuccess) return RT_ERR_CUDA;
+    if (cudaEventRecord(c->ev_shading, c->stream) != cudaSuccess) return RT_ERR_CUDA;
     if (cudaMallocHost((void **)&c->build_flag, sizeof(int)) != cudaSuccess) return RT_ERR_CUDA;
     if (cudaEventRecord(c->ev_upload, c->stream) != cudaSuccess) return RT_ERR_CUDA;
     *out = c.release();
@@ -173,6 +177,12 @@ extern "C" void rt_ctx_destroy(rt_ctx *ctx)
     if (ctx->upload_stage) cudaFreeHost(ctx->upload_stage);
     if (ctx->build_flag) cudaFreeHost(ctx->build_flag);
     if (ctx->ev_upload) cudaEventDestroy(ctx->ev_upload);
+    if (ctx->upload_side) {
+        cudaStreamSynchronize(ctx->upload_side);
+        cudaStreamDestroy(ctx->upload_side);
+    }
+    if (ctx->ev_upload_go) cudaEventDestroy(ctx->ev_upload_go);
+    if (ctx->ev_shading) cudaEventDestroy(ctx->ev_shading);
     if (ctx->side) cudaStreamSynchronize(ctx->side);
     if (ctx->cancel_dev) cudaFree(ctx->cancel_dev);
     if (ctx->cancel_vals) cudaFreeHost(ctx->cancel_vals);
@@ -444,11 +454,19 @@ extern "C" int rt_scene_upload(rt_ctx *ctx, const rt_scene_desc *d, int32_t *sce
     }
     if (n > 0) {
         if (direct) {
+            // the points go first on the render stream: the LBVH build starts from them. The
+            // shading data (normals, uvs, materials, ids) follows on a second stream and arrives
+            // while the build sorts; only its gather step waits for it. That stream first waits
+            // for the render stream's earlier work, which may still use this (reused) memory.
             CK(ctx, cudaMemcpyAsync(base + o_tp, d->tri_p, sizeof(float) * 9 * (size_t)n, cudaMemcpyHostToDevice, s));
-            CK(ctx, cudaMemcpyAsync(base + o_tn, d->tri_n, sizeof(float) * 9 * (size_t)n, cudaMemcpyHostToDevice, s));
-            if (has_uv) CK(ctx, cudaMemcpyAsync(base + o_tuv, d->tri_uv, sizeof(float) * 6 * (size_t)n, cudaMemcpyHostToDevice, s));
-            CK(ctx, cudaMemcpyAsync(base + o_tm, d->tri_mtl, sizeof(int) * (size_t)n, cudaMemcpyHostToDevice, s));
-            if (d->tri_id) CK(ctx, cudaMemcpyAsync(base + o_ti, d->tri_id, sizeof(int) * (size_t)n, cudaMemcpyHostToDevice, s));
+            cudaStream_t s2 = ctx->upload_side;
+            CK(ctx, cudaEventRecord(ctx->ev_upload_go, s));
+            CK(ctx, cudaStreamWaitEvent(s2, ctx->ev_upload_go, 0));
+            CK(ctx, cudaMemcpyAsync(base + o_tn, d->tri_n, sizeof(float) * 9 * (size_t)n, cudaMemcpyHostToDevice, s2));
+            if (has_uv) CK(ctx, cudaMemcpyAsync(base + o_tuv, d->tri_uv, sizeof(float) * 6 * (size_t)n, cudaMemcpyHostToDevice, s2));
+            CK(ctx, cudaMemcpyAsync(base + o_tm, d->tri_mtl, sizeof(int) * (size_t)n, cudaMemcpyHostToDevice, s2));
+            if (d->tri_id) CK(ctx, cudaMemcpyAsync(base + o_ti, d->tri_id, sizeof(int) * (size_t)n, cudaMemcpyHostToDevice, s2));
+            CK(ctx, cudaEventRecord(ctx->ev_shading, s2));
         } else {
             std::vector<float> tp((size_t)n * 9), tn((size_t)n * 9), tuv(has_uv ? (size_t)n * 6 : 0);
             std::vector<int> tm((size_t)n), ti((size_t)n);
@@ -583,7 +601,7 @@ extern "C" int rt_scene_rebuild(rt_ctx *ctx, int32_t id)
     if (sc.in.bad) CK(ctx, cudaMemsetAsync(sc.in.bad, 0, sizeof(int), ctx->stream));
     g_build_step = "";
     cudaEventRecord(a, ctx->stream);
-    cudaError_t e = lbvh_build(sc.in, sc.out, ctx->lbvh_scratch.p, ctx->stream);
+    cudaError_t e = lbvh_build(sc.in, sc.out, ctx->lbvh_scratch.p, ctx->stream, ctx->ev_shading);
     cudaEventRecord(b, ctx->stream);
     int bad = 0;
     if (e == cudaSuccess && sc.in.bad)

@@ -578,7 +578,8 @@ cudaError_t lbvh_morton_sort(const LbvhInput &in, uint32_t *codes_out, uint32_t 
 
 const char *g_build_step = "";   // the build step that failed last (diagnostics)
 
-cudaError_t lbvh_build(const LbvhInput &in, const LbvhOutput &out, void *scratch, cudaStream_t s)
+cudaError_t lbvh_build(const LbvhInput &in, const LbvhOutput &out, void *scratch, cudaStream_t s,
+                       cudaEvent_t shading_ready)
 {
     const int n = in.n + in.n_sph;
     if (n <= 0) return cudaSuccess;
@@ -590,6 +591,7 @@ cudaError_t lbvh_build(const LbvhInput &in, const LbvhOutput &out, void *scratch
         if (r != cudaSuccess) g_build_step = name;
         return r;
     };
+    if (shading_ready && (e = cudaStreamWaitEvent(s, shading_ready, 0)) != cudaSuccess) return e;
     k_gather<<<grid_of(n, 256), 256, 0, s>>>(in, out, sc.idx[0], sc.box);
     if ((e = step("gather")) != cudaSuccess) return e;
     if (n > 1) {

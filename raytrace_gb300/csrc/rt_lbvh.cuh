@@ -44,8 +44,11 @@ extern const char *g_build_step;
 
 // scratch bytes needed for n leaves (triangles + spheres)
 size_t lbvh_scratch_bytes(int n);
-// build into `out` using `scratch` (lbvh_scratch_bytes(n) bytes, 256-byte aligned)
-cudaError_t lbvh_build(const LbvhInput &in, const LbvhOutput &out, void *scratch, cudaStream_t s);
+// build into `out` using `scratch` (lbvh_scratch_bytes(n) bytes, 256-byte aligned). The boxes,
+// codes and sort read only tri_p, tri_obj, obj_pos and the sphere arrays; when `shading_ready`
+// is not NULL the gather (which reads the normals, uvs, materials and ids) waits for it.
+cudaError_t lbvh_build(const LbvhInput &in, const LbvhOutput &out, void *scratch, cudaStream_t s,
+                       cudaEvent_t shading_ready = nullptr);
 // Morton codes of the triangle centroids over the scene box, then a stable radix sort;
 // codes_out / perm_out receive the sorted codes and triangle indices (device pointers)
 cudaError_t lbvh_morton_sort(const LbvhInput &in, uint32_t *codes_out, uint32_t *perm_out, void *scratch,
