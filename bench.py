@@ -188,12 +188,15 @@ def run_batched(ctx, n_scenes: int, reps: int) -> dict:
     scenes = gen_scenes(3, n_scenes)
     gen_s = time.perf_counter() - t0
     sids, fids, rds, pixels = [], [], [], 0
+    # resident scenes rendered many times: the clustering hierarchy (both arms trace the same trees)
+    ctx.set_build(rt.RT_BUILD_CLUSTER)
     for sc in scenes:
         cam = sc.desc.camera
         sids.append(ctx.upload(sc))
         fids.append(ctx.frame(cam.width, cam.height))
         rds.append(ctx.render_desc(cam.width, cam.height, 1, 3))
         pixels += cam.width * cam.height
+    ctx.set_build(rt.RT_BUILD_RADIX)
     tris = sum(int(sc.desc.n_tris) for sc in scenes)
 
     def timed(fn) -> tuple[float, int]:
@@ -240,6 +243,7 @@ def run_served(ctx, seconds: float) -> dict:
                        "1 spp, depth 3, 120 GB budget with LRU eviction", "seconds_per_stream": seconds}
     keys = ("requests", "completed", "rejected", "p50_ms", "p99_ms", "mean_ms", "max_ms", "mrays_per_s", "wall_s",
             "rays", "waves", "mean_wave_requests", "admitted_busy", "evictions", "rebuilds", "peak_bytes")
+    ctx.set_build(rt.RT_BUILD_CLUSTER)   # resident scenes: the clustering hierarchy, in both arms
     for plain in (False, True):
         arm = "plain" if plain else "batched"
         with rt.Server(ctx, 120 << 30, max_inflight=256, plain=plain, keep_images=False) as srv:
@@ -252,6 +256,7 @@ def run_served(ctx, seconds: float) -> dict:
             st = srv.run_poisson(20000.0, 0.2, seed=5)   # ~4000 requests at once: sustained peak throughput
             out.setdefault("saturated", {})[arm] = {k: (round(st[k], 3) if isinstance(st[k], float) else st[k])
                                                     for k in keys}
+    ctx.set_build(rt.RT_BUILD_RADIX)
     for k in [k for k in out if k.startswith("lambda_") or k == "saturated"]:
         b, p = out[k]["batched"], out[k]["plain"]
         out[k]["speedup_mrays"] = round(b["mrays_per_s"] / max(p["mrays_per_s"], 1e-9), 3)
@@ -275,6 +280,7 @@ def run_served_replicas(ctx, seconds: float, rank: int, world: int) -> dict | No
     mine = [s for s, o in zip(scenes, owner) if o == rank]
     out = {"workload": "config4 replicas: scenes split by the owner map, one continuous-batching server per GPU",
            "scenes_per_rank": [owner.count(r) for r in range(world)]}
+    ctx.set_build(rt.RT_BUILD_CLUSTER)
     with rt.Server(ctx, 120 << 30, max_inflight=256, keep_images=False) as srv:
         for sc in mine:
             srv.add_scene(sc)
@@ -290,6 +296,7 @@ def run_served_replicas(ctx, seconds: float, rank: int, world: int) -> dict | No
             merged = replicas.gather(res)
             if rank == 0:
                 out[f"lambda_{lam}" if lam < 20000 else "saturated"] = merged
+    ctx.set_build(rt.RT_BUILD_RADIX)
     return out if rank == 0 else None
 
 

@@ -24,6 +24,7 @@ RT_LIGHT_PARALLEL, RT_LIGHT_POINT, RT_LIGHT_SPOT = 1, 2, 3
 RT_MODE_CHECK, RT_MODE_DEPTH, RT_MODE_NORMAL, RT_MODE_TEXTURE = 0x1, 0x2, 0x3, 0x4
 RT_MODE_MATERIAL, RT_MODE_SHADOW, RT_MODE_REFLECT, RT_MODE_REFRACT, RT_MODE_RAYTRACE = 0x5, 0x6, 0x7, 0x8, 0x80
 RT_FLAG_REF_TILES, RT_FLAG_HIT_PLANES, RT_FLAG_COUNT_WORK, RT_FLAG_PROFILE = 0x1, 0x2, 0x4, 0x8
+RT_BUILD_RADIX, RT_BUILD_CLUSTER = 0, 1
 KERNEL_KINDS = ("raygen", "extend", "shade", "shadow", "resolve", "other")
 
 F3 = C.c_float * 3
@@ -135,6 +136,7 @@ _SIGS = {
     "rt_ctx_synchronize": (C.c_int, [P]),
     "rt_ctx_set_stream": (C.c_int, [P, P]),
     "rt_ctx_release_cached": (C.c_int, [P]),
+    "rt_ctx_set_build": (C.c_int, [P, C.c_int32]),
     "rt_scene_upload": (C.c_int, [P, C.POINTER(SceneDesc), C.POINTER(C.c_int32)]),
     "rt_scene_update_camera": (C.c_int, [P, C.c_int32, C.POINTER(Camera)]),
     "rt_scene_rebuild": (C.c_int, [P, C.c_int32]),
@@ -449,6 +451,10 @@ class Context:
     def release_cached(self) -> None:
         """Free the released scene and frame buffers the context keeps for reuse."""
         self._ck(lib.rt_ctx_release_cached(self._h), "rt_ctx_release_cached")
+
+    def set_build(self, mode: int) -> None:
+        """Hierarchy of the scenes built from now on: RT_BUILD_RADIX or RT_BUILD_CLUSTER."""
+        self._ck(lib.rt_ctx_set_build(self._h, mode), "rt_ctx_set_build")
 
     def morton_sort(self, tri_p: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
         tri_p = np.ascontiguousarray(tri_p, np.float32).reshape(-1, 9)

@@ -206,6 +206,14 @@ extern "C" int rt_ctx_synchronize(rt_ctx *ctx)
     return RT_OK;
 }
 
+extern "C" int rt_ctx_set_build(rt_ctx *ctx, int32_t mode)
+{
+    if (!ctx) return RT_ERR_INVALID;
+    if (mode != RT_BUILD_RADIX && mode != RT_BUILD_CLUSTER) return ctx_fail(ctx, RT_ERR_INVALID, "build mode %d", mode);
+    ctx->build_mode = mode;
+    return RT_OK;
+}
+
 extern "C" int rt_ctx_release_cached(rt_ctx *ctx)
 {
     if (!ctx) return RT_ERR_INVALID;
@@ -601,6 +609,9 @@ extern "C" int rt_scene_rebuild(rt_ctx *ctx, int32_t id)
     if (sc.in.bad) CK(ctx, cudaMemsetAsync(sc.in.bad, 0, sizeof(int), ctx->stream));
     g_build_step = "";
     cudaEventRecord(a, ctx->stream);
+    // the clustering build reads each round's survivor count through the page-locked flag buffer
+    sc.in.cluster_count =
+        ctx->build_mode == RT_BUILD_CLUSTER ? reinterpret_cast<int *>(reinterpret_cast<char *>(ctx->build_flag) + 48) : nullptr;
     cudaError_t e = lbvh_build(sc.in, sc.out, ctx->lbvh_scratch.p, ctx->stream, ctx->ev_shading);
     cudaEventRecord(b, ctx->stream);
     int bad = 0;

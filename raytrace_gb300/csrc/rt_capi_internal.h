@@ -231,6 +231,7 @@ struct rt_ctx {
     size_t upload_stage_bytes = 0;
     cudaEvent_t ev_upload = nullptr;     // the last upload's staging copy
     cudaStream_t upload_side = nullptr;  // copies of the triangle shading data, beside the build
+    int build_mode = RT_BUILD_RADIX;     // hierarchy of the next builds (rt_ctx_set_build)
     cudaEvent_t ev_upload_go = nullptr;  // the render stream's work before an upload
     cudaEvent_t ev_shading = nullptr;    // the shading data of the last upload has arrived
     int *build_flag = nullptr;           // page-locked: the LBVH build's material check

@@ -457,6 +457,125 @@ __global__ void k_quads(int n, const float4 *nodes, float4 *quads)
     }
 }
 
+// ---- clustering build (PLOC: Meister & Bittner, "Parallel Locally-Ordered Clustering for
+// Bounding Volume Hierarchy Construction", 2018) ----------------------------------------------
+// Clusters start as the leaves in Morton order. Each round every cluster finds its nearest
+// neighbour among the kPlocRadius clusters on either side (distance: half the surface area of
+// the union of the two boxes; equal distances go to the lower index, which orders all pairs by
+// (distance, lower index, higher index), so the closest pair of a round is always mutual), each
+// mutual pair merges into a new internal node in the lower cluster's place, and the survivors
+// are compacted in order. Internal nodes are numbered L-2, L-3, ... in merge order, so the last
+// merge — the root — is node 0, as in the Karras layout; no refit is needed.
+constexpr int kPlocRadius = 16;
+constexpr int kPlocThreads = 256;
+
+__device__ __forceinline__ float union_half_area(float4 alo, float4 ahi, float4 blo, float4 bhi)
+{
+    const float dx = fmaxf(ahi.x, bhi.x) - fminf(alo.x, blo.x);
+    const float dy = fmaxf(ahi.y, bhi.y) - fminf(alo.y, blo.y);
+    const float dz = fmaxf(ahi.z, bhi.z) - fminf(alo.z, blo.z);
+    return dx * dy + dy * dz + dz * dx;
+}
+
+__global__ void k_ploc_init(int L, const float4 *nodes, int *id, float4 *lo, float4 *hi)
+{
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < L; k += gridDim.x * blockDim.x) {
+        const long long x = (long long)(L - 1) + k;
+        id[k] = (int)x;
+        lo[k] = __ldcg(&nodes[2 * x]);
+        hi[k] = __ldcg(&nodes[2 * x + 1]);
+    }
+}
+
+__global__ void __launch_bounds__(kPlocThreads) k_ploc_nn(int m, const float4 *lo, const float4 *hi, int *nn)
+{
+    constexpr int W = kPlocThreads + 2 * kPlocRadius;
+    __shared__ float4 slo[W], shi[W];
+    const int base = blockIdx.x * kPlocThreads - kPlocRadius;
+    for (int k = threadIdx.x; k < W; k += kPlocThreads) {
+        const int g = base + k;
+        if (g >= 0 && g < m) slo[k] = lo[g], shi[k] = hi[g];
+    }
+    __syncthreads();
+    const int i = blockIdx.x * kPlocThreads + threadIdx.x;
+    if (i >= m) return;
+    const int si = threadIdx.x + kPlocRadius;
+    float best = INFINITY;
+    int bj = -1;
+    for (int r = -kPlocRadius; r <= kPlocRadius; ++r) {   // increasing j: the first of equals wins
+        const int j = i + r;
+        if (r == 0 || j < 0 || j >= m) continue;
+        const float d = union_half_area(slo[si], shi[si], slo[si + r], shi[si + r]);
+        if (d < best) best = d, bj = j;
+    }
+    nn[i] = bj;
+}
+
+// merge mutual pairs into `out` (uncompacted, the pair in its lower slot); pos[i] = survives
+__global__ void k_ploc_merge(int m, int m4, int L, const int *nn, const int *id, const float4 *lo, const float4 *hi,
+                             int *oid, float4 *olo, float4 *ohi, unsigned *valid, unsigned *pos, int *counts, float4 *nodes,
+                             int *parent)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m4; i += gridDim.x * blockDim.x) {
+        if (i >= m) {
+            pos[i] = 0;
+            continue;
+        }
+        const int j = nn[i];
+        const bool mutual = j >= 0 && nn[j] == i;
+        if (mutual && i > j) {   // merged into j
+            valid[i] = pos[i] = 0;
+            continue;
+        }
+        if (mutual) {
+            const int x = L - 2 - atomicAdd(&counts[0], 1);
+            const float4 a = lo[i], b = lo[j], c = hi[i], d = hi[j];
+            const float4 l = make_float4(fminf(a.x, b.x), fminf(a.y, b.y), fminf(a.z, b.z), __int_as_float(id[i]));
+            const float4 h = make_float4(fmaxf(c.x, d.x), fmaxf(c.y, d.y), fmaxf(c.z, d.z), __int_as_float(id[j]));
+            nodes[2ll * x] = l;
+            nodes[2ll * x + 1] = h;
+            parent[id[i]] = x;
+            parent[id[j]] = x;
+            oid[i] = x;
+            olo[i] = l;
+            ohi[i] = h;
+        } else {
+            oid[i] = id[i];
+            olo[i] = lo[i];
+            ohi[i] = hi[i];
+        }
+        valid[i] = pos[i] = 1;
+    }
+}
+
+__global__ void k_ploc_compact(int m, const unsigned *valid, const unsigned *pos, const int *id, const float4 *lo,
+                               const float4 *hi, int *oid, float4 *olo, float4 *ohi, int *counts)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) {
+        if (valid[i]) {
+            const unsigned p = pos[i];
+            oid[p] = id[i];
+            olo[p] = lo[i];
+            ohi[p] = hi[i];
+        }
+        if (i == m - 1) counts[1] = (int)(pos[i] + valid[i]);
+    }
+}
+
+// the deepest leaf of a clustered tree (root = node 0), into counts[2]; a walk longer than 4096
+// steps (no tree built here is) counts as 4096
+__global__ void k_ploc_depth(int L, const int *parent, int *counts)
+{
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < L; k += gridDim.x * blockDim.x) {
+        int x = L - 1 + k, d = 0;
+        while (x != 0 && d < 4096) {
+            x = parent[x];
+            ++d;
+        }
+        atomicMax(&counts[2], d);
+    }
+}
+
 struct Scratch {
     unsigned *box;        // 8
     float4 *centroid;     // n
@@ -466,6 +585,13 @@ struct Scratch {
     unsigned *part;       // scan_chunks(256 * tiles) chunk sums of the histogram scan
     int *parent;          // 2n - 1
     int *flags;           // n - 1
+    // clustering build: clusters (node id, box) double-buffered, nearest neighbours, survivor
+    // flags and their scan, the scan's chunk sums, the merge counter and the survivor count
+    int *cl_id[2];
+    float4 *cl_lo[2], *cl_hi[2];
+    int *nn;
+    unsigned *valid, *pos, *pos_part;
+    int *counts;          // [0] merges so far, [1] survivors of the last round
 };
 
 size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
@@ -492,6 +618,24 @@ Scratch carve(void *base, int n)
     s.parent = (int *)p;
     p += align256(4 * (size_t)(2 * n));
     s.flags = (int *)p;
+    p += align256(4 * (size_t)n);
+    for (int k = 0; k < 2; ++k) {
+        s.cl_id[k] = (int *)p;
+        p += align256(4 * (size_t)n);
+        s.cl_lo[k] = (float4 *)p;
+        p += align256(16 * (size_t)n);
+        s.cl_hi[k] = (float4 *)p;
+        p += align256(16 * (size_t)n);
+    }
+    s.nn = (int *)p;
+    p += align256(4 * (size_t)n);
+    s.valid = (unsigned *)p;
+    p += align256(4 * (size_t)n);
+    s.pos = (unsigned *)p;
+    p += align256(4 * ((size_t)n + 4));
+    s.pos_part = (unsigned *)p;
+    p += align256(4 * (size_t)scan_chunks(n + 4));
+    s.counts = (int *)p;
     return s;
 }
 
@@ -561,7 +705,9 @@ size_t lbvh_scratch_bytes(int n)
 {
     const int tiles = (n + kTileKeys - 1) / kTileKeys;
     return 256 + align256(sizeof(float4) * (size_t)n) + 4 * align256(4 * (size_t)n) + align256(4 * 256 * (size_t)tiles) +
-           align256(4 * (size_t)scan_chunks(256 * tiles)) + align256(4 * (size_t)(2 * n)) + align256(4 * (size_t)n) + 256;
+           align256(4 * (size_t)scan_chunks(256 * tiles)) + align256(4 * (size_t)(2 * n)) + align256(4 * (size_t)n) +
+           2 * (align256(4 * (size_t)n) + 2 * align256(16 * (size_t)n)) + 2 * align256(4 * (size_t)n) +
+           align256(4 * ((size_t)n + 4)) + align256(4 * (size_t)scan_chunks(n + 4)) + 256 + 256;
 }
 
 cudaError_t lbvh_morton_sort(const LbvhInput &in, uint32_t *codes_out, uint32_t *perm_out, void *scratch, cudaStream_t s)
@@ -594,6 +740,50 @@ cudaError_t lbvh_build(const LbvhInput &in, const LbvhOutput &out, void *scratch
     if (shading_ready && (e = cudaStreamWaitEvent(s, shading_ready, 0)) != cudaSuccess) return e;
     k_gather<<<grid_of(n, 256), 256, 0, s>>>(in, out, sc.idx[0], sc.box);
     if ((e = step("gather")) != cudaSuccess) return e;
+    if (n > 1 && in.cluster_count) {
+        // clustering build: one round trip per round for the survivor count
+        k_ploc_init<<<grid_of(n, 256), 256, 0, s>>>(n, out.nodes, sc.cl_id[0], sc.cl_lo[0], sc.cl_hi[0]);
+        cudaMemsetAsync(sc.counts, 0, 12, s);
+        int m = n;
+        for (int round = 0; m > 1; ++round) {
+            if (round > 4 * 64 + 64) {   // every round merges its closest pair; this is far beyond any tree
+                g_build_step = "clustering (no progress)";
+                return cudaErrorUnknown;
+            }
+            const int m4 = (m + 3) & ~3;
+            k_ploc_nn<<<(m + kPlocThreads - 1) / kPlocThreads, kPlocThreads, 0, s>>>(m, sc.cl_lo[0], sc.cl_hi[0], sc.nn);
+            k_ploc_merge<<<grid_of(m4, 256), 256, 0, s>>>(m, m4, n, sc.nn, sc.cl_id[0], sc.cl_lo[0], sc.cl_hi[0], sc.cl_id[1],
+                                                          sc.cl_lo[1], sc.cl_hi[1], sc.valid, sc.pos, sc.counts, out.nodes,
+                                                          sc.parent);
+            const int chunks = scan_chunks(m4);
+            k_scan_reduce<<<chunks, kScanThreads, 0, s>>>(sc.pos, m4, sc.pos_part);
+            k_scan_top<<<1, kScanThreads, 0, s>>>(sc.pos_part, chunks);
+            k_scan_down<<<chunks, kScanThreads, 0, s>>>(sc.pos, m4, sc.pos_part);
+            k_ploc_compact<<<grid_of(m, 256), 256, 0, s>>>(m, sc.valid, sc.pos, sc.cl_id[1], sc.cl_lo[1], sc.cl_hi[1],
+                                                           sc.cl_id[0], sc.cl_lo[0], sc.cl_hi[0], sc.counts);
+            if ((e = step("clustering")) != cudaSuccess) return e;
+            if ((e = cudaMemcpyAsync(in.cluster_count, sc.counts + 1, sizeof(int), cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+                (e = cudaStreamSynchronize(s)) != cudaSuccess)
+                return e;
+            const int m2 = *in.cluster_count;
+            if (m2 >= m || m2 < 1) {
+                g_build_step = "clustering (no progress)";
+                return cudaErrorUnknown;
+            }
+            m = m2;
+        }
+        // traversal keeps 96 stack entries, enough for trees of depth 63: a deeper clustered tree
+        // is replaced by the radix tree, which never is
+        k_ploc_depth<<<grid_of(n, 256), 256, 0, s>>>(n, sc.parent, sc.counts);
+        if ((e = step("clustering depth")) != cudaSuccess) return e;
+        if ((e = cudaMemcpyAsync(in.cluster_count, sc.counts + 2, sizeof(int), cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+            (e = cudaStreamSynchronize(s)) != cudaSuccess)
+            return e;
+        if (*in.cluster_count <= 63) {
+            if (out.quads) k_quads<<<grid_of(n - 1, 256), 256, 0, s>>>(n, out.nodes, out.quads);
+            return step("4-wide nodes");
+        }
+    }
     if (n > 1) {
         k_karras<<<grid_of(n - 1, 256), 256, 0, s>>>(n, sc.codes[0], out.nodes, sc.parent);
         if ((e = step("hierarchy")) != cudaSuccess) return e;

@@ -26,6 +26,9 @@ struct LbvhInput {
     // no check); the caller rejects the scene
     int n_mtl;
     int *bad;
+    // clustering build instead of the Karras hierarchy when not NULL: a page-locked int the
+    // build reads each round's survivor count through (NULL = Karras radix tree)
+    int *cluster_count;
 };
 
 // leaves = n + n_sph; leaf record k (Morton order), 3 float4:

@@ -109,6 +109,25 @@ def test_cameras_outside_and_inside_the_scene_match_oracle(ctx, dist, az, el):
     assert (ref["obj"] >= 0).any() and (ref["obj"] < 0).any()   # both hits and misses in the frame
 
 
+@pytest.mark.parametrize("seed,n_spheres,ico,refr", [(6, 12, 8, 3), (7, 9, 12, 0)])
+def test_clustered_hierarchy_matches_oracle(ctx, seed, n_spheres, ico, refr):
+    """The clustering build gives another tree over the same leaves: the frame must still be
+    the oracle's, pixel for pixel."""
+    w, h = 96, 80
+    scene = rt.SceneHost.small(seed, n_spheres, ico, w, h, refr)
+    ctx.set_build(rt.RT_BUILD_CLUSTER)
+    try:
+        out, _ = gpu_render(ctx, scene, w, h, 1, 3, seed, ref_tiles=False)
+    finally:
+        ctx.set_build(rt.RT_BUILD_RADIX)
+    ref = port.render(scene, w, h, 1, 3, seed, ref_tiles=False, check=True)
+    a = ref["ambiguous"]
+    ids_equal = (out["obj"] == ref["obj"]) & (out["prim"] == ref["prim"])
+    assert not (~ids_equal & ~a).any()
+    d = np.abs(out["rgb"] - ref["rgb"]).max(axis=2)
+    assert not ((d > TOL) & ~a).any(), d[~a].max()
+
+
 def test_gpu_matches_oracle_jitter_depth4(ctx):
     w, h = 64, 64
     scene = rt.SceneHost.small(21, 14, 5, w, h, 2)
@@ -209,11 +228,17 @@ def test_morton_sort_bit_exact(ctx):
         np.testing.assert_array_equal(p_gpu, p_cpu)
 
 
-def test_lbvh_invariants(ctx):
-    """Leaves (triangles and spheres) all reachable exactly once, child boxes inside parent
-    boxes, depth <= 64, and every leaf box contains its primitive."""
+@pytest.mark.parametrize("build", [rt.RT_BUILD_RADIX, rt.RT_BUILD_CLUSTER])
+def test_lbvh_invariants(ctx, build):
+    """Both hierarchies: leaves (triangles and spheres) all reachable exactly once, child boxes
+    inside parent boxes, depth <= 63 (the traversal stack's bound), and every leaf box contains
+    its primitive."""
     scene = rt.SceneHost.config(3, 5)
-    sid = ctx.upload(scene)
+    ctx.set_build(build)
+    try:
+        sid = ctx.upload(scene)
+    finally:
+        ctx.set_build(rt.RT_BUILD_RADIX)
     nodes, perm = ctx.bvh(sid)
     ctx.release_scene(sid)
     d = scene.desc
@@ -241,7 +266,7 @@ def test_lbvh_invariants(ctx):
             depth[c] = depth[k] + 1
             stack.append(c)
     assert np.all(seen == 1), "every node reachable exactly once"
-    assert max(depth.values()) <= 64
+    assert max(depth.values()) <= 63
     tri = scene.tri_points().reshape(-1, 3, 3)
     leaf_lo, leaf_hi = lo[L - 1:], hi[L - 1:]
     t_idx = np.nonzero(~is_sph)[0]
