@@ -246,14 +246,14 @@ def run_served(ctx, seconds: float) -> dict:
     ctx.set_build(rt.RT_BUILD_CLUSTER)   # resident scenes: the clustering hierarchy, in both arms
     for plain in (False, True):
         arm = "plain" if plain else "batched"
-        with rt.Server(ctx, 120 << 30, max_inflight=256, plain=plain, keep_images=False) as srv:
+        with rt.Server(ctx, 120 << 30, max_inflight=512, plain=plain, keep_images=False) as srv:
             for sc in scenes:
                 srv.add_scene(sc)
             for lam in (50, 200, 800):
                 st = srv.run_poisson(float(lam), seconds, seed=4)
                 out.setdefault(f"lambda_{lam}", {})[arm] = {k: (round(st[k], 3) if isinstance(st[k], float) else st[k])
                                                             for k in keys}
-            st = srv.run_poisson(20000.0, 0.2, seed=5)   # ~4000 requests at once: sustained peak throughput
+            st = srv.run_poisson(20000.0, 0.5, seed=5)   # ~10000 requests at once: sustained peak throughput
             out.setdefault("saturated", {})[arm] = {k: (round(st[k], 3) if isinstance(st[k], float) else st[k])
                                                     for k in keys}
     ctx.set_build(rt.RT_BUILD_RADIX)
@@ -281,11 +281,11 @@ def run_served_replicas(ctx, seconds: float, rank: int, world: int) -> dict | No
     out = {"workload": "config4 replicas: scenes split by the owner map, one continuous-batching server per GPU",
            "scenes_per_rank": [owner.count(r) for r in range(world)]}
     ctx.set_build(rt.RT_BUILD_CLUSTER)
-    with rt.Server(ctx, 120 << 30, max_inflight=256, keep_images=False) as srv:
+    with rt.Server(ctx, 120 << 30, max_inflight=512, keep_images=False) as srv:
         for sc in mine:
             srv.add_scene(sc)
         for lam in (50, 200, 800, 20000):
-            dur = seconds if lam < 20000 else 0.2
+            dur = seconds if lam < 20000 else 0.5
             dist.barrier()
             t0 = _t.time()
             st = srv.run_poisson(lam * len(mine) / 64.0, dur, seed=4 + 1000 * rank) if mine else None
