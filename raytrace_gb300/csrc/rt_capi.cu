@@ -4,7 +4,8 @@
 // Scene flattening into device tables replaces the per-pixel virtual calls over
 // Scene::Objects (RayTracer.cpp:458-465); the LBVH replaces Model::RTPrepare
 // (Model.cpp:402-480); one render = the parallelRT tile loop (RayTracer.cpp:5-45) over every
-// pixel, as a wavefront of raygen -> (extend -> shade -> shadow) x (maxLevel+1) -> resolve.
+// pixel, as a wavefront of prepare -> (extend -> shade -> shadow) x (maxLevel+1) -> resolve, the
+// first extend making the primary rays.
 #include <algorithm>
 #include <atomic>
 #include <cmath>

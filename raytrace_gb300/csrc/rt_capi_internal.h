@@ -258,7 +258,8 @@ int make_job(rt_ctx *ctx, const SceneDev &sc, FrameDev &f, const rt_render_desc 
              long long &samples);
 // the preparation / resolve record of a frame rendered by job J (w x h pixels)
 rtg::FrameJob frame_job(const rtg::FrameBufs &fb, int w, int h, const rtg::DevJob &J);
-// raygen + (extend, shade, shadow) per level; `prof` (may be NULL) brackets every launch
 int tuning_from(rt_ctx *ctx, const rt_batch_tuning *in, rtg::Tuning &t);
+// (extend, shade, shadow) per level, the first extend making the primary rays; `prof` (may be
+// NULL) brackets every launch
 void enqueue_levels(rt_ctx *ctx, Workspace &ws, int max_level, const rtg::Tuning &t, cudaStream_t s,
                     KernelProfiler *prof);
