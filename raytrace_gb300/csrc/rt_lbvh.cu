@@ -469,11 +469,12 @@ __global__ void k_quads(int n, const float4 *nodes, float4 *quads)
 constexpr int kPlocRadius = 16;
 constexpr int kPlocThreads = 256;
 
-__device__ __forceinline__ float union_half_area(float4 alo, float4 ahi, float4 blo, float4 bhi)
+// in units of the scene's largest extent (inv = its reciprocal), so that no product overflows
+__device__ __forceinline__ float union_half_area(float4 alo, float4 ahi, float4 blo, float4 bhi, float inv)
 {
-    const float dx = fmaxf(ahi.x, bhi.x) - fminf(alo.x, blo.x);
-    const float dy = fmaxf(ahi.y, bhi.y) - fminf(alo.y, blo.y);
-    const float dz = fmaxf(ahi.z, bhi.z) - fminf(alo.z, blo.z);
+    const float dx = (fmaxf(ahi.x, bhi.x) - fminf(alo.x, blo.x)) * inv;
+    const float dy = (fmaxf(ahi.y, bhi.y) - fminf(alo.y, blo.y)) * inv;
+    const float dz = (fmaxf(ahi.z, bhi.z) - fminf(alo.z, blo.z)) * inv;
     return dx * dy + dy * dz + dz * dx;
 }
 
@@ -487,8 +488,12 @@ __global__ void k_ploc_init(int L, const float4 *nodes, int *id, float4 *lo, flo
     }
 }
 
-__global__ void __launch_bounds__(kPlocThreads) k_ploc_nn(int m, const float4 *lo, const float4 *hi, int *nn)
+__global__ void __launch_bounds__(kPlocThreads) k_ploc_nn(int m, const unsigned *box, const float4 *lo, const float4 *hi,
+                                                          int *nn)
 {
+    float emax = 0.0f;
+    for (int k = 0; k < 3; ++k) emax = fmaxf(emax, ord2f(box[3 + k]) - ord2f(box[k]));
+    const float inv = emax > 0.0f && emax < INFINITY ? 1.0f / emax : 1.0f;
     constexpr int W = kPlocThreads + 2 * kPlocRadius;
     __shared__ float4 slo[W], shi[W];
     const int base = blockIdx.x * kPlocThreads - kPlocRadius;
@@ -505,7 +510,7 @@ __global__ void __launch_bounds__(kPlocThreads) k_ploc_nn(int m, const float4 *l
     for (int r = -kPlocRadius; r <= kPlocRadius; ++r) {   // increasing j: the first of equals wins
         const int j = i + r;
         if (r == 0 || j < 0 || j >= m) continue;
-        const float d = union_half_area(slo[si], shi[si], slo[si + r], shi[si + r]);
+        const float d = union_half_area(slo[si], shi[si], slo[si + r], shi[si + r], inv);
         if (d < best) best = d, bj = j;
     }
     nn[i] = bj;
@@ -745,13 +750,11 @@ cudaError_t lbvh_build(const LbvhInput &in, const LbvhOutput &out, void *scratch
         k_ploc_init<<<grid_of(n, 256), 256, 0, s>>>(n, out.nodes, sc.cl_id[0], sc.cl_lo[0], sc.cl_hi[0]);
         cudaMemsetAsync(sc.counts, 0, 12, s);
         int m = n;
-        for (int round = 0; m > 1; ++round) {
-            if (round > 4 * 64 + 64) {   // every round merges its closest pair; this is far beyond any tree
-                g_build_step = "clustering (no progress)";
-                return cudaErrorUnknown;
-            }
+        bool stuck = false;   // a round without a merge (distances that do not order, e.g. NaN)
+        for (int round = 0; m > 1 && !stuck; ++round) {
             const int m4 = (m + 3) & ~3;
-            k_ploc_nn<<<(m + kPlocThreads - 1) / kPlocThreads, kPlocThreads, 0, s>>>(m, sc.cl_lo[0], sc.cl_hi[0], sc.nn);
+            k_ploc_nn<<<(m + kPlocThreads - 1) / kPlocThreads, kPlocThreads, 0, s>>>(m, sc.box, sc.cl_lo[0], sc.cl_hi[0],
+                                                                                   sc.nn);
             k_ploc_merge<<<grid_of(m4, 256), 256, 0, s>>>(m, m4, n, sc.nn, sc.cl_id[0], sc.cl_lo[0], sc.cl_hi[0], sc.cl_id[1],
                                                           sc.cl_lo[1], sc.cl_hi[1], sc.valid, sc.pos, sc.counts, out.nodes,
                                                           sc.parent);
@@ -766,20 +769,17 @@ cudaError_t lbvh_build(const LbvhInput &in, const LbvhOutput &out, void *scratch
                 (e = cudaStreamSynchronize(s)) != cudaSuccess)
                 return e;
             const int m2 = *in.cluster_count;
-            if (m2 >= m || m2 < 1) {
-                g_build_step = "clustering (no progress)";
-                return cudaErrorUnknown;
-            }
-            m = m2;
+            if (m2 >= m || m2 < 1) stuck = true;
+            else m = m2;
         }
         // traversal keeps 96 stack entries, enough for trees of depth 63: a deeper clustered tree
-        // is replaced by the radix tree, which never is
-        k_ploc_depth<<<grid_of(n, 256), 256, 0, s>>>(n, sc.parent, sc.counts);
+        // (or one the rounds could not finish) is replaced by the radix tree, which never is
+        if (!stuck) k_ploc_depth<<<grid_of(n, 256), 256, 0, s>>>(n, sc.parent, sc.counts);
         if ((e = step("clustering depth")) != cudaSuccess) return e;
         if ((e = cudaMemcpyAsync(in.cluster_count, sc.counts + 2, sizeof(int), cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
             (e = cudaStreamSynchronize(s)) != cudaSuccess)
             return e;
-        if (*in.cluster_count <= 63) {
+        if (!stuck && *in.cluster_count <= 63) {
             if (out.quads) k_quads<<<grid_of(n - 1, 256), 256, 0, s>>>(n, out.nodes, out.quads);
             return step("4-wide nodes");
         }

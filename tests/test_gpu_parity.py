@@ -278,6 +278,42 @@ def test_lbvh_invariants(ctx, build):
         assert np.all(c - r >= leaf_lo[k]) and np.all(c + r <= leaf_hi[k])
 
 
+def _tree_depth(nodes: np.ndarray, L: int) -> int:
+    left, right = nodes[:, 3].view(np.int32), nodes[:, 7].view(np.int32)
+    seen = np.zeros(2 * L - 1, np.int32)
+    stack, deepest = [(0, 0)], 0
+    while stack:
+        k, dpt = stack.pop()
+        seen[k] += 1
+        deepest = max(deepest, dpt)
+        if k < L - 1:
+            stack += [(int(left[k]), dpt + 1), (int(right[k]), dpt + 1)]
+    assert np.all(seen == 1)
+    return deepest
+
+
+def test_clustering_deeper_than_the_stack_falls_back_to_the_radix_tree(ctx):
+    """Triangles at x = 2^k: each clustering round merges only the lowest pair, which would
+    make a chain as deep as the triangle count, beyond the traversal stack's bound of 63 levels.
+    The build must hand back the radix tree instead, a valid tree of bounded depth."""
+    scene = rt.SceneHost.small(seed=41, n_spheres=0, ico_freq=2, width=32, height=32, refractive_every=0)
+    d = scene.desc
+    n = d.n_tris
+    assert 64 < n < 120
+    p = np.ctypeslib.as_array(d.tri_p, shape=(n * 9,)).reshape(n, 3, 3)
+    for k in range(n):
+        s = np.float32(2.0) ** k
+        p[k] = [[s, 0, 0], [s * np.float32(1.001), 0, 0], [s, 0, s * np.float32(0.001)]]
+    ctx.set_build(rt.RT_BUILD_CLUSTER)
+    try:
+        sid = ctx.upload(scene)
+    finally:
+        ctx.set_build(rt.RT_BUILD_RADIX)
+    nodes, _ = ctx.bvh(sid)
+    ctx.release_scene(sid)
+    assert _tree_depth(nodes, n) <= 63
+
+
 def test_cancel_stops_a_render_and_the_next_render_is_whole(ctx):
     """rt_cancel lands on the device flag while the render runs; the render reports
     RT_ERR_CANCELLED and the next render is complete and unaffected."""
