@@ -281,13 +281,21 @@ __device__ void closest_hit(const DevScene &S, V3 O, V3 D, int excl, bool inside
                 bool h[4];
                 int c[4] = {Q.ref.x, Q.ref.y, Q.ref.z, Q.ref.w};
                 slab4(ri, Q, self_inside ? before.t : best.t, t, h);
+                // leaves at once (ties resolve by object order, not by visit order), one code copy
+                unsigned leaves = 0;
 #pragma unroll
-                for (int k = 0; k < 4; ++k)   // leaves at once (ties resolve by object order, not by visit order)
+                for (int k = 0; k < 4; ++k)
                     if (h[k] && c[k] < 0) {
                         h[k] = false;
-                        if ((unsigned)~c[k] < (unsigned)S.n_leaves) test_leaf(~c[k]);
-                        else wc.err |= 1;
+                        leaves |= 1u << k;
                     }
+                while (leaves) {
+                    const int k = __ffs(leaves) - 1;
+                    leaves &= leaves - 1u;
+                    const int ck = k == 0 ? c[0] : k == 1 ? c[1] : k == 2 ? c[2] : c[3];
+                    if ((unsigned)~ck < (unsigned)S.n_leaves) test_leaf(~ck);
+                    else wc.err |= 1;
+                }
                 const float cull = self_inside ? before.t : best.t;   // the leaves may have lowered it
                 int n_in = 0;
 #pragma unroll
@@ -379,21 +387,28 @@ __device__ __forceinline__ int any_hit_step(const float4 *__restrict__ quads, co
     const int c[4] = {Q.ref.x, Q.ref.y, Q.ref.z, Q.ref.w};
     slab4(ri, Q, dis, t, h);
     int next = -1;
+    unsigned leaves = 0;
 #pragma unroll
     for (int k = 0; k < 4; ++k) {   // any blocker ends the ray, so no ordering is needed
         if (!h[k]) continue;
-        if (c[k] < 0) {
-            if ((unsigned)~c[k] >= (unsigned)n_leaves) {
-                wc.err |= 1;
-                return 0;
-            }
-            if (leaf_blocks<COUNT>(tri, ~c[k], O, D, dis, excl, wc)) return 1;
-        } else if (next < 0)
+        if (c[k] < 0)
+            leaves |= 1u << k;
+        else if (next < 0)
             next = c[k];
         else if (sp < STACK)
             stack[sp++] = c[k];
         else
             wc.err |= 4;
+    }
+    while (leaves) {   // one code copy of the leaf test
+        const int k = __ffs(leaves) - 1;
+        leaves &= leaves - 1u;
+        const int ck = k == 0 ? c[0] : k == 1 ? c[1] : k == 2 ? c[2] : c[3];
+        if ((unsigned)~ck >= (unsigned)n_leaves) {
+            wc.err |= 1;
+            return 0;
+        }
+        if (leaf_blocks<COUNT>(tri, ~ck, O, D, dis, excl, wc)) return 1;
     }
     if (next >= 0) {
         node = next;
