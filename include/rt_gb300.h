@@ -197,7 +197,7 @@ int rt_ctx_release_cached(rt_ctx *ctx);
 /* ---- scenes: upload + device LBVH build (replaces RTPrepare, Model.cpp:402-480) ------ */
 int rt_scene_upload(rt_ctx *ctx, const rt_scene_desc *desc, int32_t *scene_id);
 int rt_scene_update_camera(rt_ctx *ctx, int32_t scene_id, const rt_camera *cam);
-int rt_scene_rebuild(rt_ctx *ctx, int32_t scene_id);      /* re-run the LBVH build */
+int rt_scene_rebuild(rt_ctx *ctx, int32_t scene_id);      /* re-run the hierarchy build (the context's build mode) */
 int rt_scene_release(rt_ctx *ctx, int32_t scene_id);
 int rt_scene_device_bytes(rt_ctx *ctx, int32_t scene_id, int64_t *bytes);
 /* last LBVH build time in ms (device time, CUDA events) */
