@@ -521,21 +521,33 @@ __global__ void k_ploc_merge(int m, int m4, int L, const int *nn, const int *id,
                              int *oid, float4 *olo, float4 *ohi, unsigned *valid, unsigned *pos, int *counts, float4 *nodes,
                              int *parent)
 {
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m4; i += gridDim.x * blockDim.x) {
+    // whole warps iterate together (the bound is rounded up to a warp), so a warp's merges take
+    // their node numbers with one atomic (a counter every merge hit at once serialised)
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    const long long top = ((long long)m4 + 31) & ~31ll;
+    const int lane = threadIdx.x & 31;
+    for (long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x; g - lane < top; g += stride) {
+        const int i = (int)g;
+        const int j = i < m ? nn[i] : -1;
+        const bool mutual = i < m && j >= 0 && nn[j] == i;
+        const bool merge = mutual && i < j;
+        const unsigned b = __ballot_sync(0xffffffffu, merge);
+        int base = 0;
+        if (lane == 0 && b) base = atomicAdd(&counts[0], __popc(b));
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (i >= m4) continue;
         if (i >= m) {
             pos[i] = 0;
             continue;
         }
-        const int j = nn[i];
-        const bool mutual = j >= 0 && nn[j] == i;
         if (mutual && i > j) {   // merged into j
             valid[i] = pos[i] = 0;
             continue;
         }
-        if (mutual) {
-            const int x = L - 2 - atomicAdd(&counts[0], 1);
-            const float4 a = lo[i], b = lo[j], c = hi[i], d = hi[j];
-            const float4 l = make_float4(fminf(a.x, b.x), fminf(a.y, b.y), fminf(a.z, b.z), __int_as_float(id[i]));
+        if (merge) {
+            const int x = L - 2 - (base + __popc(b & ((1u << lane) - 1u)));
+            const float4 a = lo[i], bl = lo[j], c = hi[i], d = hi[j];
+            const float4 l = make_float4(fminf(a.x, bl.x), fminf(a.y, bl.y), fminf(a.z, bl.z), __int_as_float(id[i]));
             const float4 h = make_float4(fmaxf(c.x, d.x), fmaxf(c.y, d.y), fmaxf(c.z, d.z), __int_as_float(id[j]));
             nodes[2ll * x] = l;
             nodes[2ll * x + 1] = h;
