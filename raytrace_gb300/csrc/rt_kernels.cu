@@ -372,7 +372,7 @@ __device__ V3 mode_material(const DevScene &S, const DevMaterial &M, V3 P, V3 N,
 // 640 resident threads per SM (up to 96 registers, no spills): shading is latency-bound on its
 // dependent loads, and 64-register builds spilled the records it writes
 template <bool DYN>
-__global__ void __launch_bounds__(128, 5) k_shade(Wavefront wf, int sel, int wslot, int tile)
+__global__ void __launch_bounds__(128, 5) k_shade(Wavefront wf, int sel, int wslot)
 {
     if (cancelled(wf.cancel)) return;
     Counters *C = wf.C;
@@ -388,7 +388,6 @@ __global__ void __launch_bounds__(128, 5) k_shade(Wavefront wf, int sel, int wsl
     __shared__ int s_cnt[2][8][2];
     __shared__ int s_base[2];
     int step = 0;
-    (void)tile;
     for_each_block_step<DYN>(n, &C->work[wslot], [&](int j, bool active) {
         // what the hit emits is decided first and written after the block has reserved queue
         // slots, so only the inputs of the records stay live across the reservation
@@ -885,10 +884,10 @@ void launch_shade(const Wavefront &wf, int sel, int level, const Tuning &t, cuda
     ts.block = 128;
     if (t.dynamic) {
         auto k = k_shade<true>;
-        k<<<grid_for(ts, (const void *)k), 128, 0, s>>>(wf, sel, wslot, t.tile);
+        k<<<grid_for(ts, (const void *)k), 128, 0, s>>>(wf, sel, wslot);
     } else {
         auto k = k_shade<false>;
-        k<<<grid_for(ts, (const void *)k), 128, 0, s>>>(wf, sel, wslot, t.tile);
+        k<<<grid_for(ts, (const void *)k), 128, 0, s>>>(wf, sel, wslot);
     }
 }
 
