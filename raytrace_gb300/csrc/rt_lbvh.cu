@@ -478,8 +478,9 @@ __device__ __forceinline__ float union_half_area(float4 alo, float4 ahi, float4 
     return dx * dy + dy * dz + dz * dx;
 }
 
-__global__ void k_ploc_init(int L, const float4 *nodes, int *id, float4 *lo, float4 *hi)
+__global__ void k_ploc_init(int L, const float4 *nodes, int *id, float4 *lo, float4 *hi, int *counts)
 {
+    if (blockIdx.x == 0 && threadIdx.x == 0) counts[1] = L;   // round 0's cluster count
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < L; k += gridDim.x * blockDim.x) {
         const long long x = (long long)(L - 1) + k;
         id[k] = (int)x;
@@ -488,9 +489,11 @@ __global__ void k_ploc_init(int L, const float4 *nodes, int *id, float4 *lo, flo
     }
 }
 
-__global__ void __launch_bounds__(kPlocThreads) k_ploc_nn(int m, const unsigned *box, const float4 *lo, const float4 *hi,
-                                                          int *nn)
+// m_in: this round's cluster count (device); the grid covers an upper bound of it
+__global__ void __launch_bounds__(kPlocThreads) k_ploc_nn(const int *m_in, const unsigned *box, const float4 *lo,
+                                                          const float4 *hi, int *nn)
 {
+    const int m = *m_in;
     float emax = 0.0f;
     for (int k = 0; k < 3; ++k) emax = fmaxf(emax, ord2f(box[3 + k]) - ord2f(box[k]));
     const float inv = emax > 0.0f && emax < INFINITY ? 1.0f / emax : 1.0f;
@@ -517,12 +520,14 @@ __global__ void __launch_bounds__(kPlocThreads) k_ploc_nn(int m, const unsigned 
 }
 
 // merge mutual pairs into `out` (uncompacted, the pair in its lower slot); pos[i] = survives
-__global__ void k_ploc_merge(int m, int m4, int L, const int *nn, const int *id, const float4 *lo, const float4 *hi,
+__global__ void k_ploc_merge(const int *m_in, int m4, int L, const int *nn, const int *id, const float4 *lo, const float4 *hi,
                              int *oid, float4 *olo, float4 *ohi, unsigned *valid, unsigned *pos, int *counts, float4 *nodes,
                              int *parent)
 {
     // whole warps iterate together (the bound is rounded up to a warp), so a warp's merges take
-    // their node numbers with one atomic (a counter every merge hit at once serialised)
+    // their node numbers with one atomic (a counter every merge hit at once serialised). m4 is
+    // a bound of this round's count rounded up to 4: the scan reads zeros beyond the count.
+    const int m = *m_in;
     const long long stride = (long long)gridDim.x * blockDim.x;
     const long long top = ((long long)m4 + 31) & ~31ll;
     const int lane = threadIdx.x & 31;
@@ -565,9 +570,10 @@ __global__ void k_ploc_merge(int m, int m4, int L, const int *nn, const int *id,
     }
 }
 
-__global__ void k_ploc_compact(int m, const unsigned *valid, const unsigned *pos, const int *id, const float4 *lo,
-                               const float4 *hi, int *oid, float4 *olo, float4 *ohi, int *counts)
+__global__ void k_ploc_compact(const int *m_in, const unsigned *valid, const unsigned *pos, const int *id,
+                               const float4 *lo, const float4 *hi, int *oid, float4 *olo, float4 *ohi, int *m_out)
 {
+    const int m = *m_in;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) {
         if (valid[i]) {
             const unsigned p = pos[i];
@@ -575,11 +581,11 @@ __global__ void k_ploc_compact(int m, const unsigned *valid, const unsigned *pos
             olo[p] = lo[i];
             ohi[p] = hi[i];
         }
-        if (i == m - 1) counts[1] = (int)(pos[i] + valid[i]);
+        if (i == m - 1) *m_out = (int)(pos[i] + valid[i]);
     }
 }
 
-// the deepest leaf of a clustered tree (root = node 0), into counts[2]; a walk longer than 4096
+// the deepest leaf of a clustered tree (root = node 0), into counts[3]; a walk longer than 4096
 // steps (no tree built here is) counts as 4096
 __global__ void k_ploc_depth(int L, const int *parent, int *counts)
 {
@@ -589,7 +595,7 @@ __global__ void k_ploc_depth(int L, const int *parent, int *counts)
             x = parent[x];
             ++d;
         }
-        atomicMax(&counts[2], d);
+        atomicMax(&counts[3], d);
     }
 }
 
@@ -758,37 +764,51 @@ cudaError_t lbvh_build(const LbvhInput &in, const LbvhOutput &out, void *scratch
     k_gather<<<grid_of(n, 256), 256, 0, s>>>(in, out, sc.idx[0], sc.box);
     if ((e = step("gather")) != cudaSuccess) return e;
     if (n > 1 && in.cluster_count) {
-        // clustering build: one round trip per round for the survivor count
-        k_ploc_init<<<grid_of(n, 256), 256, 0, s>>>(n, out.nodes, sc.cl_id[0], sc.cl_lo[0], sc.cl_hi[0]);
-        cudaMemsetAsync(sc.counts, 0, 12, s);
-        int m = n;
-        bool stuck = false;   // a round without a merge (distances that do not order, e.g. NaN)
-        for (int round = 0; m > 1 && !stuck; ++round) {
-            const int m4 = (m + 3) & ~3;
-            k_ploc_nn<<<(m + kPlocThreads - 1) / kPlocThreads, kPlocThreads, 0, s>>>(m, sc.box, sc.cl_lo[0], sc.cl_hi[0],
-                                                                                   sc.nn);
-            k_ploc_merge<<<grid_of(m4, 256), 256, 0, s>>>(m, m4, n, sc.nn, sc.cl_id[0], sc.cl_lo[0], sc.cl_hi[0], sc.cl_id[1],
-                                                          sc.cl_lo[1], sc.cl_hi[1], sc.valid, sc.pos, sc.counts, out.nodes,
-                                                          sc.parent);
-            const int chunks = scan_chunks(m4);
-            k_scan_reduce<<<chunks, kScanThreads, 0, s>>>(sc.pos, m4, sc.pos_part);
-            k_scan_top<<<1, kScanThreads, 0, s>>>(sc.pos_part, chunks);
-            k_scan_down<<<chunks, kScanThreads, 0, s>>>(sc.pos, m4, sc.pos_part);
-            k_ploc_compact<<<grid_of(m, 256), 256, 0, s>>>(m, sc.valid, sc.pos, sc.cl_id[1], sc.cl_lo[1], sc.cl_hi[1],
-                                                           sc.cl_id[0], sc.cl_lo[0], sc.cl_hi[0], sc.counts);
+        // clustering build. The cluster count stays on the device (round r reads slot 1 + r % 2
+        // and writes the other); kernels are sized by the last count the host read, which bounds
+        // it. The host reads the count after every round while clusters are many (those rounds
+        // are long) and after every 8 rounds when they are few (a round trip each would cost
+        // more than the rounds).
+        cudaMemsetAsync(sc.counts, 0, 16, s);
+        k_ploc_init<<<grid_of(n, 256), 256, 0, s>>>(n, out.nodes, sc.cl_id[0], sc.cl_lo[0], sc.cl_hi[0], sc.counts);
+        int mh = n, r = 0;
+        bool stuck = false;   // rounds without a merge (distances that do not order, e.g. NaN)
+        while (true) {
+            const int rounds = mh > 65536 ? 1 : 8;
+            for (int q = 0; q < rounds; ++q, ++r) {
+                const int *m_in = sc.counts + 1 + (r & 1);
+                int *m_out = sc.counts + 1 + ((r + 1) & 1);
+                const int m4 = (mh + 3) & ~3;
+                k_ploc_nn<<<(mh + kPlocThreads - 1) / kPlocThreads, kPlocThreads, 0, s>>>(m_in, sc.box, sc.cl_lo[0],
+                                                                                        sc.cl_hi[0], sc.nn);
+                k_ploc_merge<<<grid_of(m4, 256), 256, 0, s>>>(m_in, m4, n, sc.nn, sc.cl_id[0], sc.cl_lo[0], sc.cl_hi[0],
+                                                              sc.cl_id[1], sc.cl_lo[1], sc.cl_hi[1], sc.valid, sc.pos,
+                                                              sc.counts, out.nodes, sc.parent);
+                const int chunks = scan_chunks(m4);
+                k_scan_reduce<<<chunks, kScanThreads, 0, s>>>(sc.pos, m4, sc.pos_part);
+                k_scan_top<<<1, kScanThreads, 0, s>>>(sc.pos_part, chunks);
+                k_scan_down<<<chunks, kScanThreads, 0, s>>>(sc.pos, m4, sc.pos_part);
+                k_ploc_compact<<<grid_of(mh, 256), 256, 0, s>>>(m_in, sc.valid, sc.pos, sc.cl_id[1], sc.cl_lo[1],
+                                                               sc.cl_hi[1], sc.cl_id[0], sc.cl_lo[0], sc.cl_hi[0], m_out);
+            }
             if ((e = step("clustering")) != cudaSuccess) return e;
-            if ((e = cudaMemcpyAsync(in.cluster_count, sc.counts + 1, sizeof(int), cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+            if ((e = cudaMemcpyAsync(in.cluster_count, sc.counts + 1 + (r & 1), sizeof(int), cudaMemcpyDeviceToHost, s)) !=
+                    cudaSuccess ||
                 (e = cudaStreamSynchronize(s)) != cudaSuccess)
                 return e;
-            const int m2 = *in.cluster_count;
-            if (m2 >= m || m2 < 1) stuck = true;
-            else m = m2;
+            const int m = *in.cluster_count;
+            if (m <= 1) break;
+            if (m >= mh) {   // every round with two or more clusters merges its closest pair
+                stuck = true;
+                break;
+            }
+            mh = m;
         }
         // traversal keeps 96 stack entries, enough for trees of depth 63: a deeper clustered tree
         // (or one the rounds could not finish) is replaced by the radix tree, which never is
         if (!stuck) k_ploc_depth<<<grid_of(n, 256), 256, 0, s>>>(n, sc.parent, sc.counts);
         if ((e = step("clustering depth")) != cudaSuccess) return e;
-        if ((e = cudaMemcpyAsync(in.cluster_count, sc.counts + 2, sizeof(int), cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+        if ((e = cudaMemcpyAsync(in.cluster_count, sc.counts + 3, sizeof(int), cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
             (e = cudaStreamSynchronize(s)) != cudaSuccess)
             return e;
         if (!stuck && *in.cluster_count <= 63) {
