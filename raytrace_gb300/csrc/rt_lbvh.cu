@@ -480,7 +480,7 @@ __device__ __forceinline__ float union_half_area(float4 alo, float4 ahi, float4 
 
 __global__ void k_ploc_init(int L, const float4 *nodes, int *id, float4 *lo, float4 *hi, int *counts)
 {
-    if (blockIdx.x == 0 && threadIdx.x == 0) counts[1] = L;   // round 0's cluster count
+    if (blockIdx.x == 0 && threadIdx.x == 0) counts[1] = L;   // cluster count before the first merge pass
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < L; k += gridDim.x * blockDim.x) {
         const long long x = (long long)(L - 1) + k;
         id[k] = (int)x;
