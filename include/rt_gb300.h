@@ -281,8 +281,8 @@ typedef struct rt_server_config {
     int32_t max_level;           /* recursion depth of every request */
     int32_t spp;                 /* samples per pixel of every request (>= 1) */
     int32_t plain;               /* 1: one request at a time through rt_render (comparison path) */
-    int64_t queue_rays;          /* ray-queue entries of one wave, 232 B each (0 = 2^26, halved
-                                    until the queues take at most a quarter of the budget) */
+    int64_t queue_rays;          /* ray-queue entries of one wave, 292 B each (0 = 2^27, halved
+                                    until the queues take at most a third of the budget) */
     int64_t max_pixels;          /* largest width*height of a request (0 = 1920*1080) */
     int32_t keep_images;         /* 1: keep finished images in host memory until rt_server_result */
     int32_t stages;              /* waves the host may enqueue ahead of the device (0 = 2) */

@@ -200,8 +200,8 @@ int wave_enqueue(rt_ctx *ctx, WaveRunner &R, const std::vector<WaveJob *> &jobs,
 // ---- batch ---------------------------------------------------------------------------------------------------
 
 namespace {
-// ray-queue entries of one batch wave by default: 2^26 entries of kWsBytesPerEntry (232 B),
-// 15.6 GB. Fewer, larger waves pay each bounce's tail (the longest
+// ray-queue entries of one batch wave by default: 2^26 entries of kWsBytesPerEntry (292 B),
+// 19.6 GB. Fewer, larger waves pay each bounce's tail (the longest
 // ray of the pass) fewer times.
 constexpr long long kBatchQueue = 1ll << 26;
 } // namespace

@@ -607,9 +607,9 @@ static int server_init(rt_server *srv)
     rt_ctx *ctx = srv->ctx;
     rt_server_config &c = srv->cfg;
     if (c.max_inflight <= 0) c.max_inflight = 64;
-    if (c.queue_rays <= 0) {   // 2^26 entries, halved until the wave queues take at most a quarter of the budget
-        c.queue_rays = 1ll << 26;
-        while (c.queue_rays > (1ll << 16) && kWsBytesPerEntry * c.queue_rays > c.hbm_budget_bytes / 4) c.queue_rays >>= 1;
+    if (c.queue_rays <= 0) {   // 2^27 entries, halved until the wave queues take at most a third of the budget
+        c.queue_rays = 1ll << 27;
+        while (c.queue_rays > (1ll << 16) && kWsBytesPerEntry * c.queue_rays > c.hbm_budget_bytes / 3) c.queue_rays >>= 1;
     }
     if (c.max_pixels <= 0) c.max_pixels = 1920ll * 1080;
     if (c.stages <= 0) c.stages = 2;
