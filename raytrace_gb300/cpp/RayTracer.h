@@ -35,7 +35,10 @@ private:
 public:
     unsigned int texID = 0;
     uint8_t *output;
-    volatile bool isFinish = true;
+    // the reference declares `volatile bool`; an atomic keeps every use of it (`if
+    // (!rt.isFinish)`, polling loops, assignment) and orders the render thread's writes of
+    // `output`, `useTime` and the status before the flag, which volatile does not on Arm
+    std::atomic<bool> isFinish{true};
     volatile double useTime = 0.0;
     uint8_t maxLevel = 1;
     int width = 0, height = 0;
