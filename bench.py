@@ -44,8 +44,11 @@ W, H, SPP, LEVEL, SEED = 1920, 1080, 4, 4, 2
 METRIC = "Mrays/s at 1080p (config 2: 1920x1080, 4 spp, depth 4)"
 WORKLOAD = ("config2: 1920x1080 full frame, 4 spp Philox jitter (seed 2), depth 4, 1024^2-vertex fBm terrain "
             "(2,093,058 tris) + 64 spheres (16 refractive), 4 point lights")
-CPU_SAMPLE_TILES = 4          # tiles of the reference's 30x16-tile region per CPU-baseline sample
-REF_STEP_TILES = 2            # tiles per step of the --impl reference arm
+# CPU samples take tiles of the reference's 30x16-tile region stratified by tile row: the
+# frame's cost sits in the terrain rows (a sky tile costs a thousandth of a terrain tile), so
+# a uniform draw of a few tiles can land on sky only and overstate the rate many times over
+CPU_SAMPLE_TILES = 16         # tiles per CPU-baseline sample: one per tile row
+REF_STEP_TILES = 4            # tiles per step of the --impl reference arm: one per band of 4 rows
 
 
 def dist_env():
@@ -126,10 +129,21 @@ def profiled_traffic() -> float | None:
 
 
 def cpu_tiles(n: int, seed: int) -> list[int]:
+    """n seeded tiles, tile k from the k-th of n equal bands of tile rows (random row in the band,
+    random column): every part of the frame, sky and terrain, in proportion."""
     import numpy as np
 
     bw, bh = W // 64, H // 64
-    return sorted(np.random.default_rng(seed).choice(bw * bh, size=n, replace=False).tolist())
+    rng = np.random.default_rng(seed)
+    tiles = set()
+    for k in range(n):
+        lo, hi = (k * bh) // n, max((k * bh) // n + 1, ((k + 1) * bh) // n)
+        while True:
+            t = int(rng.integers(lo, hi)) * bw + int(rng.integers(bw))
+            if t not in tiles:
+                tiles.add(t)
+                break
+    return sorted(tiles)
 
 
 def cpu_sample(scene, n_tiles: int, seed: int, threads: int) -> dict:
@@ -158,7 +172,8 @@ def run_reference(args) -> None:
         rays += s["rays"]
         secs += s["seconds"]
     v = rays / secs / 1e6
-    sample = (f"{REF_STEP_TILES} seeded 64x64 tiles per step (of 480 in the reference's 1920x1024 region), 4 spp, "
+    sample = (f"{REF_STEP_TILES} seeded 64x64 tiles per step, one from each band of {16 // REF_STEP_TILES} tile rows "
+              f"(of 480 in the reference's 1920x1024 region), 4 spp, "
               f"depth 4; CPU oracle restating the reference algorithm (octant lists, brute-force leaves)")
     print(json.dumps({
         "metric": METRIC, "value": round(v, 4), "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
@@ -440,7 +455,8 @@ def run_gpu(args) -> None:
         s = cpu_sample(scene, CPU_SAMPLE_TILES, 0, os.cpu_count() or 1)
         out["cpu_baseline"] = {
             "value": round(s["mrays"], 4), "unit": "Mrays/s", "cores": os.cpu_count() or 1, "kind": "port",
-            "sample": f"{CPU_SAMPLE_TILES} seeded 64x64 tiles {s['tiles']} of the 1920x1024 reference region, 4 spp, "
+            "sample": f"{CPU_SAMPLE_TILES} seeded 64x64 tiles {s['tiles']}, one per tile row of the 1920x1024 "
+                      f"reference region, 4 spp, "
                       f"depth 4: {s['rays']} rays in {s['seconds']:.2f} s; CPU oracle restating the reference "
                       f"algorithm (octant lists, brute-force leaves)"}
     print(json.dumps(out), flush=True)
