@@ -1,7 +1,7 @@
 // scene_api.cpp — runs the shared Scene API sequence (tests/cpp/scene_api_sequence.inc) on the
 // reference's own Scene / Light / Camera classes, compiled from the reference sources by
 // oracle/ref/Makefile into oracle/_ref/rt_ref_scene_api. TEST INFRASTRUCTURE ONLY: its output
-// is the golden trace tests/golden/scene_api_ref.txt (tests/golden/make_scene_api_golden.py).
+// is the golden trace tests/golden/scene_api/trace_ref.txt (tests/golden/make_scene_api_golden.py).
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>

@@ -5,23 +5,34 @@ limit of 8 and past it, every object kind, light component and luminance changes
 changes by preset and by colour, moves that translate objects, rotate the plane and ball-plane
 frames and move lights, visibility switches, camera moves, deletes) and dumps the return value
 of every call and the resulting lights, objects, materials and camera with each float as its
-bit pattern. tests/golden/scene_api_ref.txt is that trace from the reference's own classes
+bit pattern. tests/golden/scene_api/trace_ref.txt is that trace from the reference's own classes
 (tests/golden/make_scene_api_golden.py, Scene.cpp:83-301, 3DElement.cpp:340-635); here the
 same sequence is compiled against the drop-in classes with the library's host flags and must
 print the same trace. Where the reference-compiled program is present on this machine it is
 run as well.
+
+tests/cpp/scene_render_sequence.inc builds a scene through the same shared API (plane, moved
+spheres with the reflective and refractive presets, a hidden sphere, a cube, a rotated ball
+plane, the textured OBJ model of tests/golden/obj, moved point and parallel lights, a moved and
+pitched camera). tests/golden/scene_api/render_ref.npz is the reference's RayTracer::start
+image of it; the drop-in builds the same scene, flattens it as its RayTracer::start does
+(flatten_scene), and the CPU oracle's render of that description must give the same bytes on
+every pixel the oracle does not mark ambiguous.
 """
 import importlib.util
 import os
 import shutil
 import subprocess
 
+import numpy as np
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-GOLDEN = os.path.join(ROOT, "tests", "golden", "scene_api_ref.txt")
+GOLDEN = os.path.join(ROOT, "tests", "golden", "scene_api", "trace_ref.txt")
 REF_EXE = os.path.join(ROOT, "oracle", "_ref", "rt_ref_scene_api")
 DROPIN_SOURCES = ["3DElement.cpp", "Basic3DObject.cpp", "Model.cpp", "Scene.cpp"]
+RENDER_GOLDEN = os.path.join(ROOT, "tests", "golden", "scene_api", "render_ref.npz")
+OBJ_DIR = os.path.join(ROOT, "tests", "golden", "obj")
 
 
 def _host_flags() -> list[str]:
@@ -68,3 +79,23 @@ def test_reference_program_still_prints_the_golden_trace():
     live = subprocess.run([REF_EXE], check=True, capture_output=True, text=True).stdout
     with open(GOLDEN) as f:
         assert live == f.read()
+
+
+def test_dropin_scene_renders_like_reference(tmp_path):
+    import raytrace_gb300 as rt
+    from oracle import port
+
+    if shutil.which("g++") is None:
+        pytest.skip("g++ not available")
+    lib_dir = os.path.dirname(rt.LIB_PATH)
+    exe, scn = str(tmp_path / "scene_render_flatten"), str(tmp_path / "scene.rtsc")
+    subprocess.run(["g++", *_host_flags(), os.path.join(ROOT, "tests", "cpp", "scene_render_flatten.cpp"), "-o", exe,
+                    f"-L{lib_dir}", "-lrt_gb300", f"-Wl,-rpath,{lib_dir}", "-pthread"], check=True)
+    subprocess.run([exe, scn], check=True, capture_output=True, cwd=OBJ_DIR)   # textures relative to the cwd
+    ref = np.load(RENDER_GOLDEN)["rgb8"]
+    h, w = ref.shape[:2]
+    got = port.render(rt.SceneHost.load(scn), w, h, 1, 3, 0, ref_tiles=True, check=True)
+    amb = got["ambiguous"]
+    differ = np.any(got["rgb8"] != ref, axis=2)
+    assert not (differ & ~amb).any(), f"{int((differ & ~amb).sum())} pixels differ ({int(amb.sum())} ambiguous)"
+    assert amb.sum() <= 8
