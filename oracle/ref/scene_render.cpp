@@ -6,6 +6,7 @@
 // tests/golden/scene_api/render_ref.npz (tests/golden/make_scene_api_golden.py).
 #include <chrono>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <thread>
 #include <vector>
@@ -18,12 +19,13 @@
 int main(int argc, char **argv)
 {
     if (argc < 2) return 2;
+    const int mode = argc > 2 ? (int)std::strtol(argv[2], nullptr, 0) : MY_MODEL_RAYTRACE;
     Scene scene;
     build_render_scene(scene);
     RayTracer rt(scene);
     rt.maxLevel = kRenderLevel;
     const unsigned hc = std::thread::hardware_concurrency();
-    rt.start(MY_MODEL_RAYTRACE, (int8_t)(hc == 0 ? 1 : hc > 32 ? 32 : hc));
+    rt.start((uint8_t)mode, (int8_t)(hc == 0 ? 1 : hc > 32 ? 32 : hc));
     while (!rt.isFinish) std::this_thread::sleep_for(std::chrono::milliseconds(1));
     const int W = rt.width, H = rt.height;
     std::vector<uint8_t> img((size_t)W * H * 3);
@@ -33,7 +35,7 @@ int main(int argc, char **argv)
     if (!f) return 1;
     std::fwrite(img.data(), 1, img.size(), f);
     std::fclose(f);
-    std::printf("{\"width\": %d, \"height\": %d, \"objects\": %d, \"lights\": %d}\n", W, H, (int)scene.Objects.size(),
-                (int)scene.Lights.size());
+    std::printf("{\"width\": %d, \"height\": %d, \"mode\": %d, \"objects\": %d, \"lights\": %d}\n", W, H, mode,
+                (int)scene.Objects.size(), (int)scene.Lights.size());
     return 0;
 }

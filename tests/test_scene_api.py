@@ -14,8 +14,8 @@ run as well.
 tests/cpp/scene_render_sequence.inc builds a scene through the same shared API (plane, moved
 spheres with the reflective and refractive presets, a hidden sphere, a cube, a rotated ball
 plane, the textured OBJ model of tests/golden/obj, moved point and parallel lights, a moved and
-pitched camera). tests/golden/scene_api/render_ref.npz is the reference's RayTracer::start
-image of it; the drop-in builds the same scene, flattens it as its RayTracer::start does
+pitched camera). tests/golden/scene_api/render_ref.npz holds the reference's RayTracer::start
+images of it in every mode; the drop-in builds the same scene, flattens it as its RayTracer::start does
 (flatten_scene), and the CPU oracle's render of that description must give the same bytes on
 every pixel the oracle does not mark ambiguous.
 """
@@ -81,20 +81,29 @@ def test_reference_program_still_prints_the_golden_trace():
         assert live == f.read()
 
 
-def test_dropin_scene_renders_like_reference(tmp_path):
+@pytest.fixture(scope="module")
+def dropin_render_scene(tmp_path_factory):
     import raytrace_gb300 as rt
-    from oracle import port
 
     if shutil.which("g++") is None:
         pytest.skip("g++ not available")
+    d = tmp_path_factory.mktemp("scene_render")
     lib_dir = os.path.dirname(rt.LIB_PATH)
-    exe, scn = str(tmp_path / "scene_render_flatten"), str(tmp_path / "scene.rtsc")
+    exe, scn = str(d / "scene_render_flatten"), str(d / "scene.rtsc")
     subprocess.run(["g++", *_host_flags(), os.path.join(ROOT, "tests", "cpp", "scene_render_flatten.cpp"), "-o", exe,
                     f"-L{lib_dir}", "-lrt_gb300", f"-Wl,-rpath,{lib_dir}", "-pthread"], check=True)
     subprocess.run([exe, scn], check=True, capture_output=True, cwd=OBJ_DIR)   # textures relative to the cwd
-    ref = np.load(RENDER_GOLDEN)["rgb8"]
+    return rt.SceneHost.load(scn)
+
+
+# ray tracing, then the check, depth, normal, texture, material, shadow, reflect and refract tests
+@pytest.mark.parametrize("mode", [0x80, 1, 2, 3, 4, 5, 6, 7, 8])
+def test_dropin_scene_renders_like_reference(dropin_render_scene, mode):
+    from oracle import port
+
+    ref = np.load(RENDER_GOLDEN)[f"rgb8_{mode}"]
     h, w = ref.shape[:2]
-    got = port.render(rt.SceneHost.load(scn), w, h, 1, 3, 0, ref_tiles=True, check=True)
+    got = port.render(dropin_render_scene, w, h, 1, 3, 0, ref_tiles=True, check=True, mode=mode)
     amb = got["ambiguous"]
     differ = np.any(got["rgb8"] != ref, axis=2)
     assert not (differ & ~amb).any(), f"{int((differ & ~amb).sum())} pixels differ ({int(amb.sum())} ambiguous)"
