@@ -20,8 +20,10 @@ int main(int argc, char **argv)
 {
     if (argc < 2) return 2;
     const int mode = argc > 2 ? (int)std::strtol(argv[2], nullptr, 0) : MY_MODEL_RAYTRACE;
+    const int variant = argc > 3 ? std::atoi(argv[3]) : 0;
+    if (variant < 0 || variant >= kRenderVariants) return 2;
     Scene scene;
-    build_render_scene(scene);
+    build_render_scene(scene, variant);
     RayTracer rt(scene);
     rt.maxLevel = kRenderLevel;
     const unsigned hc = std::thread::hardware_concurrency();
@@ -35,7 +37,7 @@ int main(int argc, char **argv)
     if (!f) return 1;
     std::fwrite(img.data(), 1, img.size(), f);
     std::fclose(f);
-    std::printf("{\"width\": %d, \"height\": %d, \"mode\": %d, \"objects\": %d, \"lights\": %d}\n", W, H, mode,
+    std::printf("{\"width\": %d, \"height\": %d, \"mode\": %d, \"variant\": %d, \"objects\": %d, \"lights\": %d}\n", W, H, mode, variant,
                 (int)scene.Objects.size(), (int)scene.Lights.size());
     return 0;
 }

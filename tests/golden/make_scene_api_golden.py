@@ -6,8 +6,8 @@ tests/cpp/scene_api_sequence.inc) and stores what it prints: the return value of
 of a fixed sequence of scene edits and the state after it, every float as its bit pattern.
 Then builds oracle/_ref/rt_ref_scene_render, which builds the scene of
 tests/cpp/scene_render_sequence.inc through the reference's API and renders it with the
-reference's RayTracer::start in every mode (ray tracing and the eight MY_MODEL_* test modes),
-and stores those uint8 images (rows in the output's order).
+reference's RayTracer::start in every mode (ray tracing and the eight MY_MODEL_* test modes)
+for each of its scene variants, and stores those uint8 images (rows in the output's order).
 
     python tests/golden/make_scene_api_golden.py     # needs the reference sources (x86 host)
 """
@@ -25,6 +25,7 @@ RENDER_OUT = os.path.join(HERE, "scene_api", "render_ref.npz")
 # RayTracer::start's modes (RayTracer.h:9-18): ray tracing, then check, depth, normal, texture,
 # material, shadow, reflect and refract tests
 MODES = [0x80, 1, 2, 3, 4, 5, 6, 7, 8]
+VARIANTS = 4   # the scenes of tests/cpp/scene_render_sequence.inc
 
 
 def main() -> None:
@@ -42,14 +43,15 @@ def main() -> None:
     subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle", "ref"), RENDER_EXE], check=True)
     images, infos = {}, []
     with tempfile.TemporaryDirectory() as d:
-        for mode in MODES:
-            img_p = os.path.join(d, f"ref_{mode}.rgb8")
-            info = json.loads(subprocess.run([RENDER_EXE, img_p, str(mode)], check=True, capture_output=True,
-                                             text=True, cwd=os.path.join(HERE, "obj")).stdout)
-            images[f"rgb8_{mode}"] = np.fromfile(img_p, np.uint8).reshape(info["height"], info["width"], 3)
-            infos.append(info)
+        for variant in range(VARIANTS):
+            for mode in MODES:
+                img_p = os.path.join(d, f"ref_{variant}_{mode}.rgb8")
+                info = json.loads(subprocess.run([RENDER_EXE, img_p, str(mode), str(variant)], check=True,
+                                                 capture_output=True, text=True, cwd=os.path.join(HERE, "obj")).stdout)
+                images[f"rgb8_v{variant}_{mode}"] = np.fromfile(img_p, np.uint8).reshape(info["height"], info["width"], 3)
+                infos.append(info)
     np.savez_compressed(RENDER_OUT, meta=np.array(json.dumps(infos)), **images)
-    print(f"{RENDER_OUT}: {len(images)} modes, {infos[0]['width']}x{infos[0]['height']}")
+    print(f"{RENDER_OUT}: {len(images)} images ({VARIANTS} scenes x {len(MODES)} modes)")
 
 
 if __name__ == "__main__":
