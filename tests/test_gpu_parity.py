@@ -27,12 +27,6 @@ def gpu_render(ctx, scene, w, h, spp, lvl, seed, ref_tiles=True, mode=rt.RT_MODE
     return out, st
 
 
-def compare(out, ref, amb, region):
-    o, r, a = (x[region] for x in (out, ref, amb))
-    id_bad = ((o["obj"] != r["obj"]) | (o["prim"] != r["prim"])) if False else None
-    return id_bad
-
-
 def check_parity(out, ref, amb, h, w, max_rgb8_lsb=1):
     rh, rw = (h // 64) * 64, (w // 64) * 64
     sl = (slice(0, rh), slice(0, rw))
@@ -363,3 +357,42 @@ def test_out_of_range_triangle_material_is_rejected(ctx):
     sid = ctx.upload(scene)   # a valid scene still uploads
     ctx.release_scene(sid)
 
+
+
+# the scenes of tests/cpp/scene_render_sequence.inc: built through the Scene API the drop-in
+# shares with the reference, flattened as the drop-in's RayTracer::start does
+API_SCENES = ["rich", "empty", "lights_off_camera_inside_sphere", "ragged_200x136"]
+
+
+@pytest.fixture(scope="module")
+def api_scenes(tmp_path_factory):
+    lib_dir = os.path.dirname(rt.LIB_PATH)
+    d = tmp_path_factory.mktemp("api_scenes")
+    exe = str(d / "scene_render_flatten")
+    subprocess.run(["g++", "-O2", "-std=c++17", "-ffp-contract=off",
+                    os.path.join(ROOT, "tests", "cpp", "scene_render_flatten.cpp"), "-o", exe, f"-L{lib_dir}",
+                    "-lrt_gb300", f"-Wl,-rpath,{lib_dir}", "-pthread"], check=True)
+    out = []
+    for v in range(len(API_SCENES)):
+        p = str(d / f"s{v}.rtsc")
+        subprocess.run([exe, p, str(v)], check=True, capture_output=True, cwd=os.path.join(ROOT, "tests", "golden", "obj"))
+        out.append(rt.SceneHost.load(p))
+    return out
+
+
+@pytest.mark.parametrize("mode", [rt.RT_MODE_RAYTRACE, 1, 2, 3, 4, 5, 6, 7, 8])
+@pytest.mark.parametrize("variant", range(len(API_SCENES)), ids=API_SCENES)
+def test_api_built_scenes_match_oracle_and_reference(ctx, api_scenes, variant, mode):
+    """Scenes built through the shared Scene API (including an empty scene, every light off with
+    the camera inside a sphere, and partial tiles), in every RayTracer::start mode: the GPU
+    matches the CPU oracle (ids, distances, colour within the tolerance) and the reference's
+    own start() image (tests/golden/scene_api/render_ref.npz) within one uint8 step."""
+    scene = api_scenes[variant]
+    ref_img = np.load(os.path.join(ROOT, "tests", "golden", "scene_api", "render_ref.npz"))[f"rgb8_v{variant}_{mode}"]
+    h, w = ref_img.shape[:2]
+    out, _ = gpu_render(ctx, scene, w, h, 1, 3, 0, mode=mode)
+    ref = port.render(scene, w, h, 1, 3, 0, ref_tiles=True, check=True, mode=mode)
+    check_parity(out, ref, ref["ambiguous"], h, w)
+    th, tw = (h // 64) * 64, (w // 64) * 64
+    lsb = np.abs(out["rgb8"][:th, :tw].astype(int) - ref_img[:th, :tw].astype(int)).max(axis=2)
+    assert lsb[~ref["ambiguous"][:th, :tw]].max() <= 1
