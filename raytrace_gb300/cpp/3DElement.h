@@ -168,7 +168,14 @@ public:
 };
 
 // Base of every scene object. The renderer never calls a virtual per pixel: RayTracer::start
-// flattens Scene::Objects into device tables (raytrace_gb300/cpp/Flatten.cpp). There is no
+// flattens Scene::Objects into device tables (raytrace_gb300/cpp/Flatten.cpp). intersect() is
+// the reference's per-ray test (3DElement.h:201) for host-side tools such as picking or a
+// visibility query: it returns `hr` unchanged, or a closer hit with the reference's distance,
+// position, normal, texture coordinate, material and identity token (`obj`: the object, a
+// ball-plane sphere as this + 1..16, a model triangle as the address of its Triangle); a ray
+// whose `hr.obj` is an object's token skips it (a sphere then takes its inside branch when the
+// ray is inside), and a hit below `min` ends a model's search at once (the shadow rays' any-hit).
+// Call RTPrepare() after moving or editing an object and before intersect(). There is no
 // OpenGL on the target machines, so GLPrepare/GLDraw are no-ops kept for source compatibility.
 class DrawObject
 {
@@ -185,6 +192,7 @@ public:
     void GLDraw() {}
     virtual void GLPrepare() {}
     virtual void RTPrepare() {}
+    virtual HitRes intersect(const Ray &ray, const HitRes &hr, const float min = 0) = 0;
 };
 
 class Light

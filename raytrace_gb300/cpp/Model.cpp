@@ -5,6 +5,8 @@
 // rewritten to "<stem>.bmp", and the whole mesh is rescaled so its largest extent is 8.
 #include "Model.h"
 
+#include "Basic3DObject.h"
+
 #include <algorithm>
 #include <cstdio>
 #include <cstdlib>
@@ -57,6 +59,65 @@ void Model::RTPrepare()
         bboxs.push_back(borders[i] + position);
         bboxs.push_back(borders[i + 1] + position);
     }
+}
+
+// Moller-Trumbore as the reference's TriangleTest (Model.cpp:720-744): edges e1 = p1 - p0,
+// e2 = p2 - p0 and the corner p0 + position (RTPrepare's clTri, Model.cpp:425), no determinant
+// check; the distance when t > 1e-5 with the barycentrics in `coord` = (1-u-v, u, v), else 1e20
+static float triangle_test(const Ray &ray, const Triangle &tri, const Vertex &pos, Vertex &coord)
+{
+    const Vertex e1 = tri.points[1] - tri.points[0], e2 = tri.points[2] - tri.points[0];
+    const Vertex p0 = tri.points[0] + pos;
+    const Vertex pv = ray.direction * e2;
+    const Vertex t2r = ray.origin - p0;
+    const float f = 1.0f / (e1 & pv);
+    const float u = (t2r & pv) * f;
+    if (u < 0.0f || u > 1.0f) return 1e20f;
+    const Vertex qv = t2r * e1;
+    const float v = (ray.direction & qv) * f, w = 1 - u - v;
+    if (v < 0.0f || w < 0.0f) return 1e20f;
+    const float t = (e2 & qv) * f;
+    if (!(t > 1e-5f)) return 1e20f;
+    coord = Vertex(w, u, v);
+    return t;
+}
+
+HitRes Model::intersect(const Ray &ray, const HitRes &hr, const float min)
+{
+    // The reference bins each part's triangles into octant lists around the part centre and
+    // tests the lists of the octants the ray enters (Model.cpp:748-811); here every triangle of
+    // a part whose box the ray enters is tested, in part order. Both find the nearest triangle
+    // (strict <, the first found wins a tie) and stop at the first one closer than `min`.
+    float exit;
+    if (!(BorderTest(ray, BorderMin, BorderMax, &exit) < hr.distance)) return hr;
+    float best = hr.distance;
+    const Triangle *hit = nullptr;
+    size_t hit_part = 0;
+    Vertex coord;
+    for (size_t a = 0; a < parts.size() && 2 * a + 1 < bboxs.size() && !(hit && best < min); ++a) {
+        if (!(BorderTest(ray, bboxs[2 * a], bboxs[2 * a + 1], &exit) < hr.distance)) continue;
+        for (const Triangle &t : parts[a]) {
+            if (hr.obj == (intptr_t)&t) continue;   // the triangle the ray starts on
+            Vertex c;
+            const float d = triangle_test(ray, t, position, c);
+            if (d < best) {
+                best = d, hit = &t, hit_part = a, coord = c;
+                if (d < min) break;
+            }
+        }
+    }
+    if (!hit) return hr;
+    HitRes h(best);
+    h.position = ray.origin + ray.direction * best;
+    h.normal = hit->norms[0] * coord.x + hit->norms[1] * coord.y + hit->norms[2] * coord.z;
+    h.tcoord = hit->tcoords[0] * coord.x + hit->tcoords[1] * coord.y + hit->tcoords[2] * coord.z;
+    const int m = part_mtl[hit_part];
+    h.mtl = &mtls[(size_t)m];
+    h.rfr = h.mtl->rfr;
+    const int tx = mtl_tex[(size_t)m];
+    if (tx >= 0) h.tex = &texs[(size_t)tx];
+    h.obj = (intptr_t)hit;
+    return h;
 }
 
 void Model::setMesh(const std::vector<Triangle> &tris, const Material &m)

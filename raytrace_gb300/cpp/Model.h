@@ -1,7 +1,8 @@
 // Model.h — triangle-mesh object of the drop-in API (the reference's Model.h:6-50).
 // Parts, per-part materials and textures are kept as in the reference. RTPrepare's octant
 // lists (Model.cpp:402-480 of the reference) are replaced by the device LBVH built in
-// rt_scene_upload, so this class only holds the mesh.
+// rt_scene_upload; on the host, RTPrepare places the part boxes and intersect() tests a ray
+// against the triangles of every part whose box it enters.
 #pragma once
 #include "3DElement.h"
 
@@ -34,6 +35,7 @@ public:
     void zRotate();
     void SetMtl(const Material &mtl) override;
     void RTPrepare() override;
+    HitRes intersect(const Ray &ray, const HitRes &hr, const float min = 0) override;
     // inject a procedural mesh as a single part with one material (no rescale)
     void setMesh(const std::vector<Triangle> &tris, const Material &mtl);
     const Vertex &getVerMin() const { return VerMin; }
