@@ -908,6 +908,9 @@ struct Params {
     int32_t n_tiles;
     int32_t block;          // work-unit edge inside a tile for the thread pool (64 = whole tile)
     int32_t mode;           // RT_MODE_* (0 = RT_MODE_RAYTRACE)
+    const uint8_t *check_mask;   // with check: only pixels whose byte is non-zero are checked (NULL = all)
+    double *tile_seconds;        // per entry of the tile list: thread-seconds spent on it (NULL = not kept)
+    int64_t *tile_rays;          // per entry of the tile list: rays traced for it (NULL = not kept)
 };
 
 template <class T>
@@ -937,6 +940,9 @@ int render(const rt_scene_desc *d, const Params &p, T *rgb, uint8_t *rgb8, int32
     const int per_tile = (64 / blk) * (64 / blk);
     std::atomic<int64_t> next(0);
     std::vector<Counts> per((size_t)std::max(1, p.threads));
+    // per tile-list entry: thread time and rays of its work units, summed over threads
+    std::vector<std::atomic<int64_t>> tile_ns(tiles.size()), tile_rays(tiles.size());
+    for (size_t i = 0; i < tiles.size(); ++i) tile_ns[i] = 0, tile_rays[i] = 0;
     auto worker = [&](int tid) {
         Tls tls;
         tls.check = p.check;
@@ -946,7 +952,10 @@ int render(const rt_scene_desc *d, const Params &p, T *rgb, uint8_t *rgb8, int32
         while (true) {
             const int64_t k = next.fetch_add(1);
             if (k >= (int64_t)tiles.size() * per_tile) break;
-            const int tile = tiles[(size_t)(k / per_tile)], sub = (int)(k % per_tile);
+            const size_t entry = (size_t)(k / per_tile);
+            const int tile = tiles[entry], sub = (int)(k % per_tile);
+            const auto unit_t0 = std::chrono::steady_clock::now();
+            const int64_t unit_rays0 = tls.counts.primary + tls.counts.secondary + tls.counts.shadow;
             const int bx = tile % bw, by = tile / bw;
             const int r0 = by * 64 + (sub / (64 / blk)) * blk, c0 = bx * 64 + (sub % (64 / blk)) * blk;
             for (int row = r0; row < std::min(ylim, r0 + blk); ++row)
@@ -954,6 +963,7 @@ int render(const rt_scene_desc *d, const Params &p, T *rgb, uint8_t *rgb8, int32
                     const int xcur = col - W / 2, ycur = row - H / 2;
                     const size_t pix = (size_t)row * W + col;
                     tls.ambiguous = 0;
+                    tls.check = p.check && (!p.check_mask || p.check_mask[pix]);
                     T acc[3] = {0, 0, 0};
                     for (int s = 0; s < p.spp; ++s) {
                         T a, b;
@@ -1002,6 +1012,9 @@ int render(const rt_scene_desc *d, const Params &p, T *rgb, uint8_t *rgb8, int32
                     }
                     if (amb) amb[pix] = (uint8_t)tls.ambiguous;
                 }
+            tile_ns[entry] += std::chrono::duration_cast<std::chrono::nanoseconds>(std::chrono::steady_clock::now() - unit_t0)
+                                  .count();
+            tile_rays[entry] += tls.counts.primary + tls.counts.secondary + tls.counts.shadow - unit_rays0;
         }
         per[(size_t)tid] = tls.counts;
     };
@@ -1012,6 +1025,10 @@ int render(const rt_scene_desc *d, const Params &p, T *rgb, uint8_t *rgb8, int32
     worker(0);
     for (auto &t : th) t.join();
     if (seconds) *seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    for (size_t i = 0; i < tiles.size(); ++i) {
+        if (p.tile_seconds) p.tile_seconds[i] = 1e-9 * (double)tile_ns[i].load();
+        if (p.tile_rays) p.tile_rays[i] = tile_rays[i].load();
+    }
     if (counts) {
         Counts c;
         for (auto &x : per) c.primary += x.primary, c.secondary += x.secondary, c.shadow += x.shadow;
@@ -1041,6 +1058,9 @@ typedef struct orc_params {
     int32_t n_tiles;
     int32_t block;
     int32_t mode;
+    const uint8_t *check_mask;   // W*H bytes: with check, only the non-zero pixels are checked (NULL = all)
+    double *tile_seconds;        // n_tiles entries (all tiles when `tiles` is NULL): thread-seconds per tile
+    int64_t *tile_rays;          // the same entries: rays traced per tile
 } orc_params;
 
 int orc_render_f32(const rt_scene_desc *d, const orc_params *p, float *rgb, uint8_t *rgb8, int32_t *obj, int32_t *prim,
@@ -1048,7 +1068,7 @@ int orc_render_f32(const rt_scene_desc *d, const orc_params *p, float *rgb, uint
 {
     if (!d || !p) return -1;
     Params q{p->width, p->height, p->spp, p->max_level, p->ref_tiles, p->threads, p->check, p->seed, p->tiles, p->n_tiles,
-             p->block, p->mode};
+             p->block, p->mode, p->check_mask, p->tile_seconds, p->tile_rays};
     return render<float>(d, q, rgb, rgb8, obj, prim, t, amb, counts, seconds);
 }
 
@@ -1057,7 +1077,7 @@ int orc_render_f64(const rt_scene_desc *d, const orc_params *p, double *rgb, int
 {
     if (!d || !p) return -1;
     Params q{p->width, p->height, p->spp, p->max_level, p->ref_tiles, p->threads, 0, p->seed, p->tiles, p->n_tiles,
-             p->block, p->mode};
+             p->block, p->mode, nullptr, p->tile_seconds, p->tile_rays};
     return render<double>(d, q, rgb, nullptr, obj, prim, t, nullptr, counts, seconds);
 }
 
