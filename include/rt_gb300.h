@@ -225,8 +225,13 @@ int rt_frame_device_ptrs(rt_ctx *ctx, int32_t frame_id, void **rgb, void **rgb8)
 int rt_render(rt_ctx *ctx, int32_t scene_id, int32_t frame_id, const rt_render_desc *rd);
 /* wait for the last render of the context; fills stats if not NULL */
 int rt_render_wait(rt_ctx *ctx, rt_render_stats *stats);
-/* cooperative cancel of the running render (RayTracer::stop, RayTracer.cpp:698-701) */
+/* cooperative cancel of the running render (RayTracer::stop, RayTracer.cpp:698-701). Callable
+ * from any thread. A render is cancelled by every rt_cancel made after it began (rt_render,
+ * rt_batch_render, rt_render_host) or after the mark it was given (rt_render_host_since);
+ * earlier calls do not affect it. */
 int rt_cancel(rt_ctx *ctx);
+/* the context's cancel mark: the number of rt_cancel calls made so far (thread-safe) */
+uint64_t rt_cancel_mark(rt_ctx *ctx);
 /* 1 if the last render finished, 0 if still running (RayTracer::isFinish) */
 int rt_poll(rt_ctx *ctx);
 
@@ -237,21 +242,38 @@ int rt_poll(rt_ctx *ctx);
  */
 int rt_render_host(rt_ctx *ctx, const rt_scene_desc *desc, const rt_render_desc *rd,
                    uint8_t *out_rgb8, float *out_rgb, rt_render_stats *stats);
+/*
+ * rt_render_host for a render started on another thread: it is cancelled (RT_ERR_CANCELLED) by
+ * any rt_cancel made after `cancel_mark` was taken with rt_cancel_mark, including one made
+ * before this call began. The reference's start() sets isRun before its threads run, so a stop()
+ * right after start() ends that render (RayTracer.cpp:614-617, 698-701); a caller taking the mark
+ * in its start() gets the same. rt_render_host(...) is this call with the mark taken at entry.
+ */
+int rt_render_host_since(rt_ctx *ctx, uint64_t cancel_mark, const rt_scene_desc *desc,
+                         const rt_render_desc *rd, uint8_t *out_rgb8, float *out_rgb,
+                         rt_render_stats *stats);
 
 /* ---- batched multi-scene rendering (persistent wavefront kernel + CUDA graph) ------------ */
 typedef struct rt_batch_tuning {
     int32_t block;               /* threads per block of the traversal kernels (0 = default) */
-    int32_t tile;                /* rays taken per work-counter fetch (0 = default) */
-    int32_t stack;               /* traversal stack entries: 0 or 96 (fixed; 96 holds any path) */
+    int32_t tile;                /* rays taken per work-counter fetch (0 = default; at most 4096) */
+    int32_t stack;               /* traversal stack entries per thread kept in shared memory: 0, 8 or
+                                    16; the rest of the 96 entries that bound any path stay in local
+                                    memory (0 = all of them) */
     int32_t use_graph;           /* capture the per-bounce launch sequence as a CUDA graph */
-    int32_t min_blocks;          /* 0, 6, 8, 10 or 12: resident 128-thread blocks per SM the register
-                                    budget of the traversal kernels must allow (0 = compiler's) */
+    int32_t min_blocks;          /* 0, 6 or 8: resident 128-thread blocks per SM the register budget
+                                    of the traversal kernels must allow (0 = compiler's) */
     int32_t dynamic;             /* 0 or 1: pull ray tiles from a counter; 2: static grid stride */
     int64_t wave_rays;           /* batch: ray-queue entries of one wave (0 = 2^26) */
+    int32_t shadow_chunk;        /* shadow rays light-major within chunks of this many hits, a
+                                    multiple of 32 (0 = all of a bounce's hits in one chunk) */
+    int32_t reserved;            /* 0 */
 } rt_batch_tuning;
 
 /* kernel tuning of the plain per-scene path (rt_render); NULL restores the defaults */
 int rt_ctx_set_tuning(rt_ctx *ctx, const rt_batch_tuning *tuning);
+/* the plain path's current tuning (the defaults unless rt_ctx_set_tuning changed them) */
+int rt_ctx_get_tuning(const rt_ctx *ctx, rt_batch_tuning *out);
 
 /* render n (scene, frame, desc) jobs as one wavefront; returns after enqueueing */
 int rt_batch_render(rt_ctx *ctx, int32_t n, const int32_t *scene_ids, const int32_t *frame_ids,
@@ -260,7 +282,8 @@ int rt_batch_render(rt_ctx *ctx, int32_t n, const int32_t *scene_ids, const int3
 int rt_batch_render_plain(rt_ctx *ctx, int32_t n, const int32_t *scene_ids,
                           const int32_t *frame_ids, const rt_render_desc *rds);
 /* pick block size, register cap and ray tile (or the static stride) for these jobs by timing
- * candidates; the stack depth is fixed at the bound of the tree. Writes the choice. */
+ * candidates, then the short-stack depth in shared memory, the shadow chunk and the wave size.
+ * Writes the choice. */
 int rt_batch_autotune(rt_ctx *ctx, int32_t n, const int32_t *scene_ids, const int32_t *frame_ids,
                       const rt_render_desc *rds, rt_batch_tuning *out);
 
@@ -318,6 +341,13 @@ typedef struct rt_serve_stats {
     double mean_wave_requests;   /* requests sharing a wave, averaged over waves */
     int64_t admitted_busy;       /* requests admitted while other requests were in flight */
     int64_t pixels;              /* pixels of the completed frames */
+    double wave_ms_mean, wave_ms_p50, wave_ms_p99;   /* device time of one wave, table copies to
+                                                        counters back (CUDA events) */
+    double device_busy_s;        /* sum of the waves' device times: the compute stream's busy time */
+    double host_step_s;          /* host time inside rt_server_step: admission, staging, enqueue,
+                                    retirement (for the plain mode: the renders themselves) */
+    double host_wait_s;          /* of it, blocked on the device (a full staging ring, a frame copy) */
+    int64_t steps;
 } rt_serve_stats;
 
 int    rt_server_create(rt_ctx *ctx, const rt_server_config *cfg, rt_server **out);
@@ -370,12 +400,26 @@ int rt_morton_sort(rt_ctx *ctx, const float *tri_p, int64_t n_tris, uint32_t *co
  * owns; the working memory is one fixed static device array sized for RT_NOALLOC_MAX_TRIS
  * triangles (about 7.5 MB, held by every GPU that loads the library). Larger inputs return
  * RT_ERR_TOO_LARGE. Runs on cuda_stream (NULL = default stream) and returns after enqueueing.
- * The first call on a device sets up the array's address; make it before any stream capture.
- * Calls that overlap on the GPU share the array and race. No counterpart in the reference.
+ * The first call on a device loads the array there; make it before any stream capture. An
+ * error already pending from the caller's own CUDA work is left pending and the call returns
+ * RT_ERR_CUDA without enqueueing anything. Calls that overlap on the GPU share the array and
+ * race. No counterpart in the reference.
  */
 #define RT_NOALLOC_MAX_TRIS (1 << 18)
 int rt_morton_sort_noalloc(const float *d_tri_p, int64_t n_tris, uint32_t *d_codes, uint32_t *d_perm,
                            void *cuda_stream);
+/* Test hooks for the device-side limits (a corrupt tree, an overflowing queue), no counterpart
+ * in the reference. rt_scene_test_set_node_refs overwrites the four child references of 4-wide
+ * node `node` (0..L-2) of a scene's hierarchy: >= 0 an internal node 0..L-2, < 0 leaf ~k with
+ * k < L. Only references inside the tree are accepted, so a traversal of the changed tree reads
+ * no memory outside it; a cycle among valid nodes makes the traversal's visit limit (2^22 node
+ * visits per ray) and stack bound fire, and the render reports RT_ERR_CUDA ("corrupt LBVH")
+ * instead of looping. rt_ctx_test_queue_entries makes the first attempt of each later rt_render
+ * size its ray queues for `entries` rays (0 = twice the frame's samples, the default); a
+ * context whose workspace is already larger keeps the larger queues. A render that overflows
+ * its queues is retried with queues twice as large (rt_render_stats.overflow_retries). */
+int rt_scene_test_set_node_refs(rt_ctx *ctx, int32_t scene_id, int32_t node, const int32_t *refs);
+int rt_ctx_test_queue_entries(rt_ctx *ctx, int64_t entries);
 /* download the LBVH of a scene with L leaves (triangles and spheres): nodes float[(2L-1)*8]
    (min xyz, left | max xyz, right; leaf k is node L-1+k) and perm[L], the leaf order: the
    reported id of a triangle leaf, 0x80000000 | primitive index of a sphere leaf */

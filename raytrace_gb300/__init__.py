@@ -90,10 +90,11 @@ class RenderStats(C.Structure):
 
 class BatchTuning(C.Structure):
     _fields_ = [("block", C.c_int32), ("tile", C.c_int32), ("stack", C.c_int32), ("use_graph", C.c_int32),
-                ("min_blocks", C.c_int32), ("dynamic", C.c_int32), ("wave_rays", C.c_int64)]
+                ("min_blocks", C.c_int32), ("dynamic", C.c_int32), ("wave_rays", C.c_int64),
+                ("shadow_chunk", C.c_int32), ("reserved", C.c_int32)]
 
     def as_dict(self) -> dict:
-        return {k: getattr(self, k) for k, _ in self._fields_}
+        return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
 
 
 class ServerConfig(C.Structure):
@@ -121,7 +122,10 @@ class ServeStats(C.Structure):
                 ("evictions", C.c_int64), ("rebuilds", C.c_int64), ("p50_ms", C.c_double), ("p99_ms", C.c_double),
                 ("mean_ms", C.c_double), ("max_ms", C.c_double), ("mrays_per_s", C.c_double),
                 ("wall_s", C.c_double), ("rays", C.c_int64), ("peak_bytes", C.c_int64), ("waves", C.c_int64),
-                ("mean_wave_requests", C.c_double), ("admitted_busy", C.c_int64), ("pixels", C.c_int64)]
+                ("mean_wave_requests", C.c_double), ("admitted_busy", C.c_int64), ("pixels", C.c_int64),
+                ("wave_ms_mean", C.c_double), ("wave_ms_p50", C.c_double), ("wave_ms_p99", C.c_double),
+                ("device_busy_s", C.c_double), ("host_step_s", C.c_double), ("host_wait_s", C.c_double),
+                ("steps", C.c_int64)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -152,7 +156,11 @@ _SIGS = {
     "rt_cancel": (C.c_int, [P]),
     "rt_poll": (C.c_int, [P]),
     "rt_render_host": (C.c_int, [P, C.POINTER(SceneDesc), C.POINTER(RenderDesc), P, P, C.POINTER(RenderStats)]),
+    "rt_cancel_mark": (C.c_uint64, [P]),
+    "rt_render_host_since": (C.c_int, [P, C.c_uint64, C.POINTER(SceneDesc), C.POINTER(RenderDesc), P, P,
+                                       C.POINTER(RenderStats)]),
     "rt_ctx_set_tuning": (C.c_int, [P, C.POINTER(BatchTuning)]),
+    "rt_ctx_get_tuning": (C.c_int, [P, C.POINTER(BatchTuning)]),
     "rt_batch_render": (C.c_int, [P, C.c_int32, P, P, P, C.POINTER(BatchTuning)]),
     "rt_batch_render_plain": (C.c_int, [P, C.c_int32, P, P, P]),
     "rt_batch_autotune": (C.c_int, [P, C.c_int32, P, P, P, C.POINTER(BatchTuning)]),
@@ -175,6 +183,8 @@ _SIGS = {
     "rt_morton_sort": (C.c_int, [P, P, C.c_int64, P, P]),
     "rt_morton_sort_noalloc": (C.c_int, [P, C.c_int64, P, P, P]),
     "rt_scene_bvh_download": (C.c_int, [P, C.c_int32, P, P, C.POINTER(C.c_int64)]),
+    "rt_scene_test_set_node_refs": (C.c_int, [P, C.c_int32, C.c_int32, C.POINTER(C.c_int32)]),
+    "rt_ctx_test_queue_entries": (C.c_int, [P, C.c_int64]),
     "rt_scenegen": (C.c_int, [C.c_int32, C.c_int32, C.POINTER(P)]),
     "rt_scenegen_small": (C.c_int, [C.c_uint64, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.POINTER(P)]),
     "rt_scenegen_extras": (C.c_int, [C.c_uint64, C.c_int32, C.c_int32, C.POINTER(P)]),
@@ -440,6 +450,12 @@ class Context:
         arr = (RenderDesc * n)(*rds)
         t = BatchTuning()
         self._ck(lib.rt_batch_autotune(self._h, n, _ptr(s), _ptr(f), C.cast(arr, P), C.byref(t)), "rt_batch_autotune")
+        return t
+
+    def tuning(self) -> BatchTuning:
+        """The plain path's current tuning."""
+        t = BatchTuning()
+        self._ck(lib.rt_ctx_get_tuning(self._h, C.byref(t)), "rt_ctx_get_tuning")
         return t
 
     def set_tuning(self, tuning: BatchTuning | None) -> None:

@@ -14,7 +14,7 @@ import sys
 
 import numpy as np
 
-from . import RT_FLAG_PROFILE, RT_FLAG_REF_TILES, Context, SceneHost
+from . import RT_FLAG_PROFILE, RT_FLAG_REF_TILES, BatchTuning, Context, SceneHost
 
 
 def write_ppm(path: str, rgb8: np.ndarray) -> None:
@@ -41,6 +41,8 @@ def main(argv: list[str] | None = None) -> int:
     ap.add_argument("--level", type=int, default=-1)
     ap.add_argument("--repeat", type=int, default=1)
     ap.add_argument("--ref-tiles", action="store_true", help="only the reference's 64x64-tile region")
+    ap.add_argument("--stack", type=int, default=-1, help="traversal stack entries in shared memory: 0, 8, 16")
+    ap.add_argument("--chunk", type=int, default=-1, help="shadow rays light-major in chunks of this many hits")
     ap.add_argument("--out", default="")
     ap.add_argument("--pfm", default="")
     a = ap.parse_args(argv)
@@ -53,6 +55,13 @@ def main(argv: list[str] | None = None) -> int:
     spp = a.spp or spp
     lvl = lvl if a.level < 0 else a.level
     with Context(0) as ctx:
+        if a.stack >= 0 or a.chunk >= 0:
+            t = ctx.tuning()
+            if a.stack >= 0:
+                t.stack = a.stack
+            if a.chunk >= 0:
+                t.shadow_chunk = a.chunk
+            ctx.set_tuning(t)
         sid = ctx.upload(scene)
         fid = ctx.frame(w, h)
         flags = RT_FLAG_PROFILE | (RT_FLAG_REF_TILES if a.ref_tiles else 0)

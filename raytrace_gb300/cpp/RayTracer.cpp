@@ -53,14 +53,18 @@ void RayTracer::start(const uint8_t type, const int8_t)
     // the scene is read now, so the caller may edit it once start() has returned
     flatten_scene(*scene, flat);
     const uint8_t level = maxLevel;
-    worker = std::thread([this, mode, level] {
+    // the cancel mark is taken here, before the render thread runs: a stop() from now on ends
+    // this render even while the thread is still uploading the scene (the reference sets isRun
+    // in start(), RayTracer.cpp:617)
+    const uint64_t mark = rt_cancel_mark(ctx);
+    worker = std::thread([this, mode, level, mark] {
         const int W = width, H = height;
         std::vector<uint8_t> img((size_t)W * H * 3);
         rt_render_desc rd{};
         rd.width = W, rd.height = H, rd.spp = 1, rd.max_level = level, rd.mode = mode;
         rd.flags = RT_FLAG_REF_TILES;
         const auto t0 = std::chrono::steady_clock::now();
-        int rc = rt_render_host(ctx, &flat.desc, &rd, img.data(), nullptr, nullptr);
+        int rc = rt_render_host_since(ctx, mark, &flat.desc, &rd, img.data(), nullptr, nullptr);
         const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
         if (rc == RT_OK) {
             const int bw = W / 64, bh = H / 64;

@@ -22,6 +22,7 @@ WaveRunner::~WaveRunner()
             cudaEventSynchronize(st.done);
             cudaEventDestroy(st.done);
         }
+        if (st.start) cudaEventDestroy(st.start);
         if (st.jobs) cudaFreeHost(st.jobs);
     }
     if (ftab_copied) {
@@ -44,9 +45,16 @@ size_t wave_runner_bytes(const WaveRunner &R) { return R.ws.mem.bytes + R.ftab_d
 static int stage_harvest(rt_ctx *ctx, WaveRunner &R, WaveStage &st, bool wait)
 {
     if (!st.busy) return RT_OK;
-    cudaError_t e = wait ? cudaEventSynchronize(st.done) : cudaEventQuery(st.done);
+    cudaError_t e = cudaEventQuery(st.done);
+    if (e == cudaErrorNotReady && wait) {
+        const auto t0 = std::chrono::steady_clock::now();
+        e = cudaEventSynchronize(st.done);
+        R.wait_s += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    }
     if (e == cudaErrorNotReady) return RT_OK;
     if (e != cudaSuccess) return ctx_fail(ctx, RT_ERR_CUDA, "wave: %s", cudaGetErrorString(e));
+    float ms = 0.0f;
+    if (cudaEventElapsedTime(&ms, st.start, st.done) == cudaSuccess) R.wave_ms.push_back(ms);
     const Counters &C = *st.counters;
     R.rays_primary += C.rays_primary;
     R.rays_secondary += C.rays_secondary;
@@ -82,6 +90,7 @@ int wave_runner_init(rt_ctx *ctx, WaveRunner &R, long long qcap, int jobcap, int
     for (WaveStage &st : R.stages) {
         if (st.jobs) cudaFreeHost(st.jobs);
         if (st.done) cudaEventDestroy(st.done);
+        if (st.start) cudaEventDestroy(st.start);
     }
     R.stages.assign((size_t)n_stages, WaveStage());
     R.next = 0;
@@ -98,14 +107,14 @@ int wave_runner_init(rt_ctx *ctx, WaveRunner &R, long long qcap, int jobcap, int
         st.scalars = (long long *)(b + o_sc);
         st.counters = (Counters *)(b + o_ctr);
         CK(ctx, cudaEventCreate(&st.done));
+        CK(ctx, cudaEventCreate(&st.start));
     }
     return RT_OK;
 }
 
 static int wave_graph(rt_ctx *ctx, WaveRunner &R, int max_level, const Tuning &t, cudaGraphExec_t &exec)
 {
-    const long long key = ((long long)max_level << 40) ^ ((long long)t.block << 24) ^ ((long long)t.tile << 8) ^
-                          (long long)t.stack ^ ((long long)t.dynamic << 50) ^ ((long long)t.min_blocks << 52);
+    const long long key = tuning_key(max_level, t);
     auto it = R.graphs.find(key);
     if (it != R.graphs.end()) {
         exec = it->second->exec;
@@ -174,6 +183,7 @@ int wave_enqueue(rt_ctx *ctx, WaveRunner &R, const std::vector<WaveJob *> &jobs,
     st.n_jobs = n;
     st.samples = samples;
     Workspace &ws = R.ws;
+    CK(ctx, cudaEventRecord(st.start, s));
     CK(ctx, cudaMemcpyAsync(ws.scenes, st.scenes, sizeof(DevScene) * n_scenes, cudaMemcpyHostToDevice, s));
     CK(ctx, cudaMemcpyAsync(ws.jobs, st.jobs, sizeof(DevJob) * n, cudaMemcpyHostToDevice, s));
     CK(ctx, cudaMemcpyAsync(ws.job_end, st.end, 8 * (size_t)n, cudaMemcpyHostToDevice, s));
@@ -243,10 +253,12 @@ static int batch_core(rt_ctx *ctx, int32_t n, const int32_t *scene_ids, const in
     KernelProfiler *P = profile ? &ctx->prof : nullptr;
     cudaStream_t s = ctx->stream;
     R.ws.wf.cancel = ctx->cancel_dev;
-    rc = cancel_arm(ctx);
+    rc = cancel_arm(ctx, ctx->cancel_count.load());
     if (rc) return rc;
     R.rays_primary = R.rays_secondary = R.rays_shadow = 0;
     R.overflow = R.error = 0;
+    R.wave_ms.clear();
+    R.wait_s = 0.0;
     // the frame table; its pinned host copy is rewritten once the previous copy out of it ran
     if (!R.ftab_copied) CK(ctx, cudaEventCreateWithFlags(&R.ftab_copied, cudaEventDisableTiming));
     CK(ctx, cudaEventSynchronize(R.ftab_copied));
@@ -290,6 +302,7 @@ static int batch_core(rt_ctx *ctx, int32_t n, const int32_t *scene_ids, const in
     C.rays_primary = R.rays_primary, C.rays_secondary = R.rays_secondary, C.rays_shadow = R.rays_shadow;
     C.overflow = R.overflow, C.error = R.error;
     ctx->pending.active = false;
+    if (cancel_requested(ctx)) return ctx_fail(ctx, RT_ERR_CANCELLED, "batch cancelled");
     if (R.overflow) return ctx_fail(ctx, RT_ERR_OVERFLOW, "batch ray queue overflow");
     if (R.error) return ctx_fail(ctx, RT_ERR_CUDA, "traversal stopped on a corrupt LBVH (flags 0x%x)", R.error);
     return RT_OK;
@@ -336,30 +349,51 @@ extern "C" int rt_batch_autotune(rt_ctx *ctx, int32_t n, const int32_t *scene_id
                                  const rt_render_desc *rds, rt_batch_tuning *out)
 {
     if (!ctx || !out) return RT_ERR_INVALID;
-    // (threads per block, register cap as resident blocks per SM) x rays per tile fetch
-    // tile 0 stands for the static grid stride; the stack depth is fixed (kStack)
+    // Coordinate search, each candidate timed as the best of three batches after a warm one
+    // (which captures its graph): (threads per block, register cap as resident blocks per SM) x
+    // rays per tile fetch (0 = the static grid stride), then the traversal stack entries kept in
+    // shared memory, then the shadow work chunk, then the wave size. The caller picks the jobs:
+    // tuning on a sample of the workload and measuring on the rest keeps the choice honest.
     const int shapes[][2] = {{128, 8}, {128, 6}, {64, 8}, {256, 0}};
     const int tiles[] = {0, 32, 64, 128, 256};
-    // then the wave size (ray-queue entries per wave) for the best shape
-    const long long waves[] = {1ll << 25, 1ll << 27};
+    const int stacks[] = {0, 8, 16};
+    const int chunks[] = {0, 2048, 8192, 32768};
+    const long long waves[] = {1ll << 25, 1ll << 27};   // the default is 2^26
     double best = 1e30;
-    rt_batch_tuning best_t{128, 32, 0, 1, 8, 1, 0};
+    rt_batch_tuning best_t{128, 32, 0, 1, 8, 1, 0, 0, 0};
     auto trial = [&](const rt_batch_tuning &t) {
         int rc = rt_batch_render(ctx, n, scene_ids, frame_ids, rds, &t);   // warm (captures the graph)
         if (rc) return rc;
-        auto t0 = std::chrono::steady_clock::now();
-        rc = rt_batch_render(ctx, n, scene_ids, frame_ids, rds, &t);
-        if (rc) return rc;
-        cudaStreamSynchronize(ctx->stream);
-        double dt = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        double dt = 1e30;
+        for (int rep = 0; rep < 3; ++rep) {
+            auto t0 = std::chrono::steady_clock::now();
+            rc = rt_batch_render(ctx, n, scene_ids, frame_ids, rds, &t);
+            if (rc) return rc;
+            cudaStreamSynchronize(ctx->stream);
+            dt = std::min(dt, std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count());
+        }
         if (dt < best) best = dt, best_t = t;
         return RT_OK;
     };
     for (const auto &sh : shapes)
         for (int tl : tiles) {
-            int rc = trial(rt_batch_tuning{sh[0], tl ? tl : 32, 0, 1, sh[1], tl ? 1 : 2, 0});
+            int rc = trial(rt_batch_tuning{sh[0], tl ? tl : 32, 0, 1, sh[1], tl ? 1 : 2, 0, 0, 0});
             if (rc) return rc;
         }
+    for (int ss : stacks) {
+        if (ss == best_t.stack) continue;
+        rt_batch_tuning t = best_t;
+        t.stack = ss;
+        int rc = trial(t);
+        if (rc) return rc;
+    }
+    for (int ch : chunks) {
+        if (ch == best_t.shadow_chunk) continue;
+        rt_batch_tuning t = best_t;
+        t.shadow_chunk = ch;
+        int rc = trial(t);
+        if (rc) return rc;
+    }
     for (long long w : waves) {
         rt_batch_tuning t = best_t;
         t.wave_rays = w;

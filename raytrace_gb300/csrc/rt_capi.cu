@@ -115,10 +115,15 @@ void spare_take(rt_ctx *ctx, DevBuf &dst, size_t need)
 // ---- version / context -------------------------------------------------------------------------------
 // Cancel: rt_cancel writes 1 into a device word from page-locked memory on a side stream, which
 // runs beside the render; each render clears it on the same stream first and its kernels wait
-// for the clear. Kernels then read device memory, not host memory over the bus.
-int cancel_arm(rt_ctx *ctx)
+// for the clear. Kernels then read device memory, not host memory over the bus. Both writes are
+// made under the context's cancel mutex, and a render whose mark a cancel has already passed
+// does not clear the flag: the side stream then holds every cancel's write after the clear
+// that could hide it.
+int cancel_arm(rt_ctx *ctx, unsigned long long mark)
 {
-    ctx->cancel_host = 0;
+    std::lock_guard<std::mutex> lock(ctx->cancel_mu);
+    ctx->cancel_base = mark;
+    if (ctx->cancel_count.load() != mark) return ctx_fail(ctx, RT_ERR_CANCELLED, "render cancelled");
     CK(ctx, cudaMemcpyAsync(ctx->cancel_dev, ctx->cancel_vals, sizeof(int), cudaMemcpyHostToDevice, ctx->side));
     CK(ctx, cudaEventRecord(ctx->ev_armed, ctx->side));
     CK(ctx, cudaStreamWaitEvent(ctx->stream, ctx->ev_armed, 0));
@@ -902,9 +907,7 @@ static int plain_graph(rt_ctx *ctx, int max_level, const Tuning &t, cudaGraphExe
         ctx->plain_graphs.clear();
         ctx->plain_graph_gen = ws.gen;
     }
-    const long long key = ((long long)max_level << 40) ^ ((long long)t.block << 24) ^ ((long long)t.tile << 8) ^
-                          (long long)t.stack ^ ((long long)t.dynamic << 50) ^ ((long long)t.min_blocks << 52) ^
-                          ((long long)t.count << 58);
+    const long long key = tuning_key(max_level, t);
     auto it = ctx->plain_graphs.find(key);
     if (it != ctx->plain_graphs.end()) {
         exec = it->second->exec;
@@ -928,19 +931,20 @@ static int plain_graph(rt_ctx *ctx, int max_level, const Tuning &t, cudaGraphExe
     return RT_OK;
 }
 
-static int render_once(rt_ctx *ctx, SceneDev &sc, FrameDev &f, const rt_render_desc *rd, long long qcap)
+static int render_once(rt_ctx *ctx, SceneDev &sc, FrameDev &f, const rt_render_desc *rd, long long qcap,
+                       unsigned long long cancel_mark)
 {
     DevJob J;
     long long samples = 0;
     int rc = make_job(ctx, sc, f, rd, 0, J, samples);
     if (rc) return rc;
-    if (qcap <= 0) qcap = std::max<long long>(2 * samples, 4096);
+    if (qcap <= 0) qcap = ctx->test_queue > 0 ? ctx->test_queue : std::max<long long>(2 * samples, 4096);
     rc = ws_ensure(ctx, ctx->ws, qcap, 1);
     if (rc) return rc;
     Workspace &ws = ctx->ws;
     cudaStream_t s = ctx->stream;
     ws.wf.cancel = ctx->cancel_dev;
-    rc = cancel_arm(ctx);
+    rc = cancel_arm(ctx, cancel_mark);
     if (rc) return rc;
     // the job tables (job, its sample end, the wave scalars, the scene header) go up in one copy
     // from page-locked memory laid out as in the workspace
@@ -985,7 +989,9 @@ static int render_once(rt_ctx *ctx, SceneDev &sc, FrameDev &f, const rt_render_d
     return RT_OK;
 }
 
-extern "C" int rt_render(rt_ctx *ctx, int32_t scene_id, int32_t frame_id, const rt_render_desc *rd)
+// rt_render, cancelled by any rt_cancel counted after `cancel_mark`
+static int render_since(rt_ctx *ctx, unsigned long long cancel_mark, int32_t scene_id, int32_t frame_id,
+                        const rt_render_desc *rd)
 {
     if (!ctx) return RT_ERR_INVALID;
     auto si = ctx->scenes.find(scene_id);
@@ -994,9 +1000,15 @@ extern "C" int rt_render(rt_ctx *ctx, int32_t scene_id, int32_t frame_id, const 
     if (fi == ctx->frames.end()) return ctx_fail(ctx, RT_ERR_NOT_FOUND, "unknown frame %d", frame_id);
     CK(ctx, cudaSetDevice(ctx->device));
     ctx->pending = Pending{scene_id, frame_id, rd ? *rd : rt_render_desc{}, true, 0};
-    int rc = render_once(ctx, *si->second, *fi->second, rd, 0);
+    int rc = render_once(ctx, *si->second, *fi->second, rd, 0, cancel_mark);
     if (rc) ctx->pending.active = false;
     return rc;
+}
+
+extern "C" int rt_render(rt_ctx *ctx, int32_t scene_id, int32_t frame_id, const rt_render_desc *rd)
+{
+    if (!ctx) return RT_ERR_INVALID;
+    return render_since(ctx, ctx->cancel_count.load(), scene_id, frame_id, rd);
 }
 
 extern "C" int rt_render_wait(rt_ctx *ctx, rt_render_stats *stats)
@@ -1009,13 +1021,15 @@ extern "C" int rt_render_wait(rt_ctx *ctx, rt_render_stats *stats)
         auto si = ctx->scenes.find(ctx->pending.scene);
         auto fi = ctx->frames.find(ctx->pending.frame);
         if (si == ctx->scenes.end() || fi == ctx->frames.end()) return ctx_fail(ctx, RT_ERR_NOT_FOUND, "render target released");
-        int rc = render_once(ctx, *si->second, *fi->second, &ctx->pending.rd, ctx->ws.qcap * 2);
-        if (rc) return rc;
+        int rc = render_once(ctx, *si->second, *fi->second, &ctx->pending.rd, ctx->ws.qcap * 2, ctx->cancel_base);
+        if (rc) {
+            ctx->pending.active = false;
+            return rc;
+        }
         CK(ctx, cudaEventSynchronize(ctx->ev_stop));
     }
     ctx->pending.retries = retries;
-    const bool was_cancelled = ctx->cancel_host != 0;
-    ctx->cancel_host = 0;
+    const bool was_cancelled = cancel_requested(ctx);
     if (stats) {
         const Counters &C = *ctx->counters_host;
         stats->rays_primary = (int64_t)C.rays_primary;
@@ -1047,16 +1061,36 @@ int tuning_from(rt_ctx *ctx, const rt_batch_tuning *in, Tuning &t)
     if (!in) return RT_OK;
     if (in->block) t.block = in->block;
     if (in->tile) t.tile = in->tile;
-    if (in->stack) t.stack = in->stack;
+    t.stack = in->stack;
     t.min_blocks = in->min_blocks;
+    t.shadow_chunk = in->shadow_chunk;
     if (in->dynamic < 0 || in->dynamic > 2) return ctx_fail(ctx, RT_ERR_INVALID, "dynamic %d: use 0, 1 or 2", in->dynamic);
     t.dynamic = in->dynamic != 2;
-    if (t.block % 32 || t.block < 32 || t.block > 256 || t.tile % 32 || t.tile <= 0)
+    if (t.block % 32 || t.block < 32 || t.block > 256 || t.tile % 32 || t.tile <= 0 || t.tile > 4096)
         return ctx_fail(ctx, RT_ERR_INVALID, "tuning block %d / tile %d not supported", t.block, t.tile);
-    if (t.min_blocks != 0 && t.min_blocks != 6 && t.min_blocks != 8 && t.min_blocks != 10 && t.min_blocks != 12)
-        return ctx_fail(ctx, RT_ERR_INVALID, "min_blocks %d: use 0, 6, 8, 10 or 12", t.min_blocks);
+    if (t.min_blocks != 0 && t.min_blocks != 6 && t.min_blocks != 8)
+        return ctx_fail(ctx, RT_ERR_INVALID, "min_blocks %d: use 0, 6 or 8", t.min_blocks);
     if (t.min_blocks && t.block > 128) return ctx_fail(ctx, RT_ERR_INVALID, "min_blocks needs blocks of at most 128 threads");
-    if (t.stack != kStack) return ctx_fail(ctx, RT_ERR_INVALID, "stack %d: the traversal uses %d entries", t.stack, kStack);
+    if (t.stack != 0 && t.stack != 8 && t.stack != 16)
+        return ctx_fail(ctx, RT_ERR_INVALID, "stack %d: use 0, 8 or 16 shared-memory entries", t.stack);
+    if (t.shadow_chunk < 0 || t.shadow_chunk % 32 || t.shadow_chunk > (1 << 27))
+        return ctx_fail(ctx, RT_ERR_INVALID, "shadow_chunk %d: a multiple of 32 in [0, 2^27]", t.shadow_chunk);
+    return RT_OK;
+}
+
+// key of a captured level loop: every tuning value a launch in it depends on
+long long tuning_key(int max_level, const Tuning &t)
+{
+    return (long long)max_level | (long long)(t.block / 32) << 3 | (long long)(t.tile / 32) << 7 |
+           (long long)t.stack << 15 | (long long)t.dynamic << 20 | (long long)t.min_blocks << 21 |
+           (long long)t.count << 25 | (long long)(t.shadow_chunk / 32) << 26;
+}
+
+extern "C" int rt_ctx_get_tuning(const rt_ctx *ctx, rt_batch_tuning *out)
+{
+    if (!ctx || !out) return RT_ERR_INVALID;
+    const Tuning &t = ctx->plain_tuning;
+    *out = rt_batch_tuning{t.block, t.tile, t.stack, 1, t.min_blocks, t.dynamic ? 1 : 2, 0, t.shadow_chunk, 0};
     return RT_OK;
 }
 
@@ -1075,10 +1109,21 @@ extern "C" int rt_ctx_set_tuning(rt_ctx *ctx, const rt_batch_tuning *tuning)
 extern "C" int rt_cancel(rt_ctx *ctx)
 {
     if (!ctx) return RT_ERR_INVALID;
-    ctx->cancel_host = 1;
-    CK(ctx, cudaMemcpyAsync(ctx->cancel_dev, ctx->cancel_vals + 1, sizeof(int), cudaMemcpyHostToDevice, ctx->side));
+    // callable from any thread: the write goes on the context's device, the caller's current
+    // device is left as it was
+    int prev = -1;
+    if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+    std::lock_guard<std::mutex> lock(ctx->cancel_mu);
+    ctx->cancel_count.fetch_add(1);
+    cudaError_t e = cudaSetDevice(ctx->device);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(ctx->cancel_dev, ctx->cancel_vals + 1, sizeof(int), cudaMemcpyHostToDevice, ctx->side);
+    if (prev >= 0 && prev != ctx->device) cudaSetDevice(prev);
+    if (e != cudaSuccess) return ctx_fail(ctx, RT_ERR_CUDA, "rt_cancel: %s", cudaGetErrorString(e));
     return RT_OK;
 }
+
+extern "C" uint64_t rt_cancel_mark(rt_ctx *ctx) { return ctx ? (uint64_t)ctx->cancel_count.load() : 0; }
 
 extern "C" int rt_poll(rt_ctx *ctx)
 {
@@ -1089,22 +1134,36 @@ extern "C" int rt_poll(rt_ctx *ctx)
     return 1;
 }
 
-extern "C" int rt_render_host(rt_ctx *ctx, const rt_scene_desc *desc, const rt_render_desc *rd, uint8_t *out_rgb8,
-                              float *out_rgb, rt_render_stats *stats)
+extern "C" int rt_render_host_since(rt_ctx *ctx, uint64_t cancel_mark, const rt_scene_desc *desc,
+                                    const rt_render_desc *rd, uint8_t *out_rgb8, float *out_rgb, rt_render_stats *stats)
 {
     if (!ctx || !desc || !rd) return RT_ERR_INVALID;
+    // a cancel that came before or between the stages ends the call there; one that comes
+    // while the kernels run stops them through the device flag
+    auto cancelled = [&] {
+        if (ctx->cancel_count.load() == cancel_mark) return false;
+        ctx_fail(ctx, RT_ERR_CANCELLED, "render cancelled");
+        return true;
+    };
+    if (cancelled()) return RT_ERR_CANCELLED;
     int32_t sid = -1, fid = -1;
     int rc = rt_scene_upload(ctx, desc, &sid);
     if (rc) return rc;
     const rt_camera &cam = rd->camera ? *rd->camera : desc->camera;
     const int W = rd->width > 0 ? rd->width : cam.width, H = rd->height > 0 ? rd->height : cam.height;
-    rc = rt_frame_create(ctx, W, H, &fid);
-    if (!rc) rc = rt_render(ctx, sid, fid, rd);
+    rc = cancelled() ? RT_ERR_CANCELLED : rt_frame_create(ctx, W, H, &fid);
+    if (!rc) rc = render_since(ctx, cancel_mark, sid, fid, rd);
     if (!rc) rc = rt_render_wait(ctx, stats);
     if (!rc) rc = rt_frame_download(ctx, fid, out_rgb, out_rgb8, nullptr, nullptr, nullptr);
     if (fid >= 0) rt_frame_release(ctx, fid);
     rt_scene_release(ctx, sid);
     return rc;
+}
+
+extern "C" int rt_render_host(rt_ctx *ctx, const rt_scene_desc *desc, const rt_render_desc *rd, uint8_t *out_rgb8,
+                              float *out_rgb, rt_render_stats *stats)
+{
+    return rt_render_host_since(ctx, rt_cancel_mark(ctx), desc, rd, out_rgb8, out_rgb, stats);
 }
 
 // ---- LBVH test hooks ------------------------------------------------------------------------------------------
@@ -1157,6 +1216,33 @@ extern "C" int rt_scene_bvh_download(rt_ctx *ctx, int32_t id, float *nodes, uint
         }
     }
     CK(ctx, cudaStreamSynchronize(s));
+    return RT_OK;
+}
+
+// ---- test hooks: a corrupt hierarchy, a queue too small for the frame -------------------------------------
+extern "C" int rt_scene_test_set_node_refs(rt_ctx *ctx, int32_t scene_id, int32_t node, const int32_t *refs)
+{
+    if (!ctx || !refs) return RT_ERR_INVALID;
+    auto it = ctx->scenes.find(scene_id);
+    if (it == ctx->scenes.end()) return ctx_fail(ctx, RT_ERR_NOT_FOUND, "unknown scene %d", scene_id);
+    SceneDev &sc = *it->second;
+    const int L = sc.n_leaves;
+    if (L < 2 || node < 0 || node > L - 2) return ctx_fail(ctx, RT_ERR_INVALID, "node %d outside 0..%d", node, L - 2);
+    for (int k = 0; k < 4; ++k) {   // only existing nodes and leaves: the changed tree reads nothing outside itself
+        const int c = refs[k];
+        if (c >= 0 ? c > L - 2 : ~c >= L) return ctx_fail(ctx, RT_ERR_INVALID, "reference %d outside the tree", c);
+    }
+    CK(ctx, cudaSetDevice(ctx->device));
+    float4 *slot = const_cast<float4 *>(sc.hdr.quads) + 8ll * node + 6;   // the record's child references
+    CK(ctx, cudaMemcpyAsync(slot, refs, 4 * sizeof(int32_t), cudaMemcpyHostToDevice, ctx->stream));
+    CK(ctx, cudaStreamSynchronize(ctx->stream));
+    return RT_OK;
+}
+
+extern "C" int rt_ctx_test_queue_entries(rt_ctx *ctx, int64_t entries)
+{
+    if (!ctx || entries < 0 || entries > (1ll << 27)) return RT_ERR_INVALID;
+    ctx->test_queue = entries;
     return RT_OK;
 }
 

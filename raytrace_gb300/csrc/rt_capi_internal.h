@@ -2,8 +2,10 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <map>
 #include <memory>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -153,6 +155,7 @@ struct WaveStage {
     rtg::DevScene *scenes = nullptr;
     long long *scalars = nullptr;
     rtg::Counters *counters = nullptr;
+    cudaEvent_t start = nullptr;         // recorded before the wave's table copies
     cudaEvent_t done = nullptr;
     bool busy = false;
     int n_jobs = 0;
@@ -173,6 +176,8 @@ struct WaveRunner {
     unsigned long long rays_primary = 0, rays_secondary = 0, rays_shadow = 0;
     int overflow = 0, error = 0;
     long long waves = 0, wave_jobs = 0;
+    std::vector<float> wave_ms;          // device time of each harvested wave (start to done)
+    double wait_s = 0.0;                 // host time blocked on waves (a full staging ring, a drain)
     // frame table of a batch (pinned host copy, device copy): prepared and resolved in one
     // launch each
     rtg::FrameJob *ftab_host = nullptr;
@@ -210,7 +215,13 @@ struct rt_ctx {
     int next_scene = 0, next_frame = 0;
     Workspace ws;
     DevBuf lbvh_scratch;
-    volatile int cancel_host = 0;        // rt_cancel was called since the render started
+    // Cancel: rt_cancel counts its calls; a render (or rt_render_host_since call) is cancelled
+    // once the count passes the mark it began from. The mutex orders rt_cancel's write of the
+    // device flag against the clear a new render makes, so no cancel made after a render's mark
+    // is wiped out by that render's clear.
+    std::mutex cancel_mu;
+    std::atomic<unsigned long long> cancel_count{0};   // rt_cancel calls so far
+    unsigned long long cancel_base = 0;  // mark of the current render
     int *cancel_dev = nullptr;           // device copy the kernels read (written on `side`)
     int *cancel_vals = nullptr;          // page-locked {0, 1}: sources of those writes
     cudaStream_t side = nullptr;         // cancel writes, ordered apart from the render stream
@@ -232,14 +243,19 @@ struct rt_ctx {
     cudaEvent_t ev_upload = nullptr;     // the last upload's staging copy
     cudaStream_t upload_side = nullptr;  // copies of the triangle shading data, beside the build
     int build_mode = RT_BUILD_RADIX;     // hierarchy of the next builds (rt_ctx_set_build)
+    long long test_queue = 0;            // rt_ctx_test_queue_entries: first-attempt queue size (0 = default)
     cudaEvent_t ev_upload_go = nullptr;  // the render stream's work before an upload
     cudaEvent_t ev_shading = nullptr;    // the shading data of the last upload has arrived
     int *build_flag = nullptr;           // page-locked: the LBVH build's material check
 };
 
 int ctx_fail(rt_ctx *ctx, int code, const char *fmt, ...);
-// clear the cancel flag for a render about to be enqueued on the context stream
-int cancel_arm(rt_ctx *ctx);
+// begin a render cancelled by any rt_cancel counted after `mark`: clear the device flag for the
+// kernels about to be enqueued on the context stream, or return RT_ERR_CANCELLED (flag left set)
+// when such a cancel has already come
+int cancel_arm(rt_ctx *ctx, unsigned long long mark);
+// a cancel has come since the current render's mark
+inline bool cancel_requested(const rt_ctx *ctx) { return ctx->cancel_count.load() != ctx->cancel_base; }
 // released scene / frame buffers the context keeps for reuse: their bytes, and freeing them
 size_t spare_bytes(const rt_ctx *ctx);
 void spare_trim(rt_ctx *ctx);
@@ -259,6 +275,8 @@ int make_job(rt_ctx *ctx, const SceneDev &sc, FrameDev &f, const rt_render_desc 
 // the preparation / resolve record of a frame rendered by job J (w x h pixels)
 rtg::FrameJob frame_job(const rtg::FrameBufs &fb, int w, int h, const rtg::DevJob &J);
 int tuning_from(rt_ctx *ctx, const rt_batch_tuning *in, rtg::Tuning &t);
+// key of a captured level loop (max_level and every tuning value its launches depend on)
+long long tuning_key(int max_level, const rtg::Tuning &t);
 // (extend, shade, shadow) per level, the first extend making the primary rays; `prof` (may be
 // NULL) brackets every launch
 void enqueue_levels(rt_ctx *ctx, Workspace &ws, int max_level, const rtg::Tuning &t, cudaStream_t s,

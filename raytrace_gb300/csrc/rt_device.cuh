@@ -19,6 +19,10 @@ constexpr float kEps6 = 9.99999997e-07f;     // float nearest below 1e-6
 constexpr float kMiss = 1e20f;               // HitRes() distance
 constexpr int kTriFlag = 0x40000000;         // primitive key bit for triangles
 constexpr int kMaxLights = 8;                // Scene::AddLight limit
+// Traversal stack entries. A Karras node's common prefix grows by at least one bit per level
+// over 30 Morton bits plus the index bits that break ties, so a path has at most 63 binary
+// levels, i.e. 32 four-wide nodes, each pushing at most 3 entries.
+constexpr int kStack = 96;
 
 // ray type codes (MY_RAY_*)
 constexpr int kRayBase = 1, kRayShadow = 2, kRayReflect = 3, kRayRefract = 4;

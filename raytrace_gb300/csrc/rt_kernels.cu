@@ -1,4 +1,5 @@
-// rt_kernels.cu — wavefront kernels of the GB300 renderer.
+// rt_kernels.cu — wavefront kernels of the GB300 renderer: shading, frame preparation and
+// resolve, and the launch helpers (extend and shadow are in rt_extend.cu and rt_shadow.cu).
 //
 // One level of the reference's RTfrac recursion (RayTracer.cpp:450-596) is one pass:
 //   extend  closest hit of every ray in the queue                 (:458-465)
@@ -18,266 +19,9 @@
 #include <map>
 #include <mutex>
 
-#include "rt_fixed.cuh"
-#include "rt_kernels.cuh"
-#include "rt_trace.cuh"
+#include "rt_wave.cuh"
 
 namespace rtg {
-
-constexpr unsigned kFull = 0xffffffffu;
-
-__device__ __forceinline__ void acc_add(long long *acc, int pix, V3 c)
-{
-    unsigned long long *a = reinterpret_cast<unsigned long long *>(acc + 3ll * pix);
-    if (c.x != 0.0f && c.x == c.x) atomicAdd(a + 0, (unsigned long long)float_to_fix32(c.x));
-    if (c.y != 0.0f && c.y == c.y) atomicAdd(a + 1, (unsigned long long)float_to_fix32(c.y));
-    if (c.z != 0.0f && c.z == c.z) atomicAdd(a + 2, (unsigned long long)float_to_fix32(c.z));
-}
-
-// Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11)
-__device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint2 k)
-{
-    const unsigned M0 = 0xD2511F53u, M1 = 0xCD9E8D57u, W0 = 0x9E3779B9u, W1 = 0xBB67AE85u;
-#pragma unroll
-    for (int r = 0; r < 10; ++r) {
-        unsigned hi0 = __umulhi(M0, c.x), lo0 = M0 * c.x;
-        unsigned hi1 = __umulhi(M1, c.z), lo1 = M1 * c.z;
-        c = make_uint4(hi1 ^ c.y ^ k.x, lo1, hi0 ^ c.w ^ k.y, lo0);
-        k.x += W0;
-        k.y += W1;
-    }
-    return c;
-}
-
-// Warp-uniform loops over the rays [0, n).
-//
-// for_each_ray: each warp first takes its own 32 rays (no atomics: a launch with at most
-// 32 x warps rays touches no counter), then the rest by grid stride (DYN false) or in `tile`-ray
-// tiles pulled from a counter (DYN true) — fine-grained, for traversal, whose cost per ray
-// varies by orders of magnitude.
-template <bool DYN, class F>
-__device__ __forceinline__ void for_each_ray(int n, int *work, int tile, F &&body)
-{
-    const int lane = threadIdx.x & 31;
-    const int nw = gridDim.x * (blockDim.x >> 5);
-    const int w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-    const int first = min(n, nw * 32);   // the static prefix
-    if (w * 32 < first) body(w * 32 + lane, w * 32 + lane < first);
-    if (first >= n) return;
-    if (!DYN) {
-        for (long long base = (long long)first + (long long)w * 32; base < n; base += (long long)nw * 32)
-            body((int)(base + lane), base + lane < n);
-    } else {
-        while (true) {
-            int start = 0;
-            if (lane == 0) start = atomicAdd(work, tile);
-            start = first + __shfl_sync(kFull, start, 0);
-            if (start >= n) break;
-            const int end = min(start + tile, n);
-            for (int base = start; base < end; base += 32)
-                body(base + lane, base + lane < end);
-        }
-    }
-}
-
-// Block-uniform loop over [0, n) in steps of blockDim.x items, one per thread: every thread of a
-// block runs the body the same number of times, so the body may synchronise the block. Chunks
-// come from a counter, a share of what is left (DYN), or by grid stride.
-template <bool DYN, class F>
-__device__ __forceinline__ void for_each_block_step(int n, int *work, F &&body)
-{
-    __shared__ int s_start;
-    const int B = blockDim.x;
-    if (!DYN) {
-        for (long long base = (long long)blockIdx.x * B; base < n; base += (long long)gridDim.x * B)
-            body((int)base + (int)threadIdx.x, base + threadIdx.x < n);
-        return;
-    }
-    int chunk = max(B, ((n / (2 * (int)gridDim.x)) + B - 1) / B * B);
-    while (true) {
-        if (threadIdx.x == 0) s_start = atomicAdd(work, chunk);
-        __syncthreads();
-        const int start = s_start;
-        __syncthreads();   // s_start is written again by the next round
-        if (start >= n) break;
-        const int end = min(start + chunk, n);
-        for (int base = start; base < end; base += B) body(base + (int)threadIdx.x, base + (int)threadIdx.x < end);
-        chunk = max(B, (((n - end) / (2 * (int)gridDim.x)) + B - 1) / B * B);
-    }
-}
-
-__device__ __forceinline__ bool cancelled(const volatile int *cancel) { return cancel && *cancel; }
-
-// ---- ray generation (parallelRT, RayTracer.cpp:13-27) -------------------------------------
-// Primary rays are made inside the first extend pass, in registers: a ray queue entry is
-// written only for a ray that hits something, which is what shading reads.
-
-// the job that holds global sample gs. Lane 0 searches for the first sample of the warp's 32
-// (base), the lanes walk on from there: 32 consecutive samples span few jobs. All lanes call.
-__device__ __forceinline__ int job_of(const Wavefront &wf, long long gs, long long base, bool active)
-{
-    int j = 0;
-    if ((threadIdx.x & 31) == 0) {
-        int lo = 0, hi = (int)*wf.n_jobs - 1;
-        while (lo < hi) {
-            const int mid = (lo + hi) >> 1;
-            if (wf.job_sample_end[mid] > base) hi = mid;
-            else lo = mid + 1;
-        }
-        j = lo;
-    }
-    j = __shfl_sync(kFull, j, 0);
-    // ends: the last job's end is the number of samples of all jobs, above any active gs
-    if (active)
-        while (wf.job_sample_end[j] <= gs) ++j;
-    return j;
-}
-
-struct PrimaryRay {
-    V3 o, d;
-    int pixel, row, col;
-    int sample;   // sample index within the pixel
-};
-
-// camera ray of the job's sample `local` (pixel-major: local = pixel * spp + sample)
-__device__ __forceinline__ PrimaryRay primary_ray(const DevJob &J, long long local)
-{
-    PrimaryRay r;
-    long long p;
-    int s;
-    if (J.spp == 1) {
-        p = local;
-        s = 0;
-    } else if (local < (1ll << 32)) {   // 32-bit division where it suffices
-        const unsigned q = (unsigned)local / (unsigned)J.spp;
-        p = q;
-        s = (int)((unsigned)local - q * (unsigned)J.spp);
-    } else {
-        p = local / J.spp;
-        s = (int)(local - p * J.spp);
-    }
-    // p < 2^28: frames are at most 16384 x 16384
-    const unsigned row = (unsigned)p / (unsigned)J.xlim, col = (unsigned)p - row * (unsigned)J.xlim;
-    const int xcur = (int)col - J.width / 2, ycur = (int)row - J.height / 2;
-    float a, b;
-    DSplit d = split_double_bits((unsigned long long)__double_as_longlong(J.dp));
-    if (J.axis) {   // one sample per pixel: the offsets of the frame's table
-        a = J.axis[col];
-        b = J.axis[J.width + row];
-    } else if (J.spp > 1) {   // sub-pixel jitter in [0,1) from a per-pixel Philox stream
-        const unsigned pix = row * (unsigned)J.width + col;
-        const uint4 x = philox4x32_10(make_uint4(pix, 0u, (unsigned)s, 0u),
-                                      make_uint2((unsigned)J.seed, (unsigned)(J.seed >> 32)));
-        // (float)(((double)xcur + (x >> 8) * 2^-24) * dp): the sum is exact in 38 bits, so it
-        // is the integer xcur * 2^24 + (x >> 8) times dp * 2^-24
-        d.e -= 24;
-        a = dmul_to_float((long long)xcur * 16777216ll + (long long)(x.x >> 8), d);
-        b = dmul_to_float((long long)ycur * 16777216ll + (long long)(x.y >> 8), d);
-    } else {   // (float)((double)xcur * dp)
-        a = dmul_to_float(xcur, d);
-        b = dmul_to_float(ycur, d);
-    }
-    const V3 n = mk(J.cam_n[0], J.cam_n[1], J.cam_n[2]);
-    const V3 u = mk(J.cam_u[0], J.cam_u[1], J.cam_u[2]);
-    const V3 v = mk(J.cam_v[0], J.cam_v[1], J.cam_v[2]);
-    r.d = normalise(vadd(vadd(n, vscale(u, a)), vscale(v, b)));
-    r.o = mk(J.cam_pos[0], J.cam_pos[1], J.cam_pos[2]);
-    r.pixel = (int)(row * (unsigned)J.width + col);
-    r.row = (int)row, r.col = (int)col;
-    r.sample = s;
-    return r;
-}
-
-// ---- extend: closest hit -------------------------------------------------------------------
-// MINB > 0 caps registers so MINB blocks of 128 threads fit on an SM. GEN: the first pass of a
-// wave, which makes its primary rays instead of reading a queue.
-template <int STACK, bool DYN, bool COUNT, int MINB, bool GEN>
-__global__ void __launch_bounds__(MINB ? 128 : 256, MINB ? MINB : 1) k_extend(Wavefront wf, int sel, int wslot, int tile)
-{
-    Counters *C = wf.C;
-    const RayQueue q = wf.q[sel];
-    const long long total = GEN ? *wf.total_samples : 0, first = GEN ? *wf.sample_offset : 0;
-    if (blockIdx.x == 0 && threadIdx.x == 0) {   // the next queue fills in shade
-        C->q_count[sel ^ 1] = 0;
-        // the rays of this queue are the children the last shading spawned (counted once here,
-        // not by an atomic per warp on one address)
-        if (!GEN) C->rays_secondary += (unsigned long long)C->q_count[sel];
-        if (GEN) {
-            C->q_count[sel] = (int)min(total, (long long)q.capacity);
-            C->rays_primary = (unsigned long long)total;
-            if (total > q.capacity) atomicExch(&C->overflow, 1);
-        }
-    }
-    if (cancelled(wf.cancel)) return;
-    const int n = GEN ? (int)min(total, (long long)q.capacity) : min(C->q_count[sel], q.capacity);
-    WorkCount wc{0, 0, 0, 0};
-    const int level = wslot / 3;
-    const int lane = threadIdx.x & 31;
-    const unsigned lt = (1u << lane) - 1u;
-    const HitQueue hq = wf.hq;
-    for_each_ray<DYN>(n, &C->work[wslot], tile, [&](int i, bool active) {
-        Best best;
-        best.key = -1;
-        int newobj = -1, job = 0, pixel = 0, plane = 0;
-        V3 o, d;
-        if constexpr (GEN) {
-            job = job_of(wf, first + i, first + (i - lane), active);
-            if (active) {
-                const DevJob &J = wf.jobs[job];
-                const PrimaryRay pr = primary_ray(J, first + i - J.sample_base);
-                if (J.mode == kModeCheck && ((pr.row >> 6) & 1) == ((pr.col >> 6) & 1))
-                    acc_add(J.acc, pr.pixel, mk(1.0f, 1.0f, 1.0f));   // RTcheck: white 64x64 tiles
-                plane = pr.sample == 0 && J.plane_obj != nullptr;
-                pixel = pr.pixel;
-                o = pr.o, d = pr.d;
-                closest_hit<STACK, COUNT>(wf.scenes[J.scene], o, d, -1, false, best, newobj, wc);
-            }
-        } else if (active) {
-            const float4 o4 = q.o[i], d4 = q.d[i];
-            const int4 m4 = q.m[i];
-            closest_hit<STACK, COUNT>(wf.scenes[wf.jobs[m4.w].scene], mk(o4), mk(d4), m4.x, ray_inside(m4.y) != 0, best,
-                                      newobj, wc);
-        }
-        // the hits go to the hit queue densely (one atomic per warp): shading reads them with
-        // coalesced loads, and misses cost it nothing
-        const bool is_hit = best.key >= 0;
-        const unsigned hb = __ballot_sync(kFull, is_hit);
-        if (hb) {
-            int base = 0;
-            if (lane == 0) base = atomicAdd(&C->h_count[level], __popc(hb));
-            base = __shfl_sync(kFull, base, 0);
-            if (is_hit) {
-                const int h = base + __popc(hb & lt);   // below the queue capacity: one per ray
-                hq.h[h] = make_float4(best.t, best.u, best.v, __int_as_float(best.key));
-                hq.nob[h] = newobj;
-                if constexpr (GEN) {
-                    hq.o[h] = make_float4(o.x, o.y, o.z, 1.0f);
-                    hq.d[h] = make_float4(d.x, d.y, d.z, 1.0f);
-                    hq.w[h] = make_float4(1.0f, 1.0f, 1.0f, __int_as_float(pixel));
-                    hq.m[h] = make_int4(-1, ray_flags(0, kRayBase, 0, plane), -1, job);
-                } else {   // the ray record again (its lines were read at the start of this tile)
-                    hq.o[h] = q.o[i];
-                    hq.d[h] = q.d[i];
-                    hq.w[h] = q.w[i];
-                    hq.m[h] = q.m[i];
-                }
-            }
-        }
-    });
-    if (wc.err) atomicOr(&C->error, wc.err);
-    if (COUNT) {
-        for (int off = 16; off > 0; off >>= 1) {
-            wc.nodes += __shfl_down_sync(kFull, wc.nodes, off);
-            wc.tris += __shfl_down_sync(kFull, wc.tris, off);
-            wc.spheres += __shfl_down_sync(kFull, wc.spheres, off);
-        }
-        if ((threadIdx.x & 31) == 0) {
-            atomicAdd(&C->nodes, (unsigned long long)wc.nodes);
-            atomicAdd(&C->tris, (unsigned long long)wc.tris);
-            atomicAdd(&C->spheres, (unsigned long long)wc.spheres);
-        }
-    }
-}
 
 // texture colour: nearest texel, wrapped, BGR bytes (Color(Texture*,Coord2D), 3DElement.cpp:430-450)
 __device__ V3 tex_color(const DevScene &S, int tex, float u, float v)
@@ -293,33 +37,6 @@ __device__ V3 tex_color(const DevScene &S, int tex, float u, float v)
     off = off > last ? last : (off < 0 ? 0 : off);
     const uint8_t *t = S.texels + T.offset + off;
     return mk(__fdiv_rn((float)t[2], 255.0f), __fdiv_rn((float)t[1], 255.0f), __fdiv_rn((float)t[0], 255.0f));
-}
-
-// light terms of one light at P (RayTracer.cpp:482-503)
-struct LightTerm {
-    V3 p2l;
-    float dis, lum;
-    bool point;
-};
-__device__ __forceinline__ LightTerm light_term(const DevLight &L, V3 P)
-{
-    LightTerm r;
-    if (L.type == 2) {   // MY_LIGHT_POINT
-        V3 p2l_v = vsub(mk(L.pos[0], L.pos[1], L.pos[2]), P);
-        float d2 = dot3(p2l_v, p2l_v);
-        float step = __fadd_rn(L.att[0], __fmul_rn(L.att[2], d2));
-        r.dis = __fsqrt_rn(d2);
-        step = __fadd_rn(step, __fmul_rn(L.att[1], r.dis));
-        r.lum = __fdiv_rn(1.0f, step);
-        r.p2l = normalise(p2l_v);
-        r.point = true;
-    } else {
-        r.dis = 1e10f;
-        r.lum = 1.0f;
-        r.p2l = normalise(mk(L.pos[0], L.pos[1], L.pos[2]));
-        r.point = false;
-    }
-    return r;
 }
 
 // ---- first-hit test modes (RayTracer.cpp:81-220) -----------------------------------------
@@ -613,67 +330,6 @@ __global__ void __launch_bounds__(128, 5) k_shade(Wavefront wf, int sel, int wsl
     });
 }
 
-// ---- shadow: per-light any-hit + direct light ---------------------------------------------------
-template <int STACK, bool DYN, bool COUNT, int MINB>
-__global__ void __launch_bounds__(MINB ? 128 : 256, MINB ? MINB : 1) k_shadow(Wavefront wf, int wslot, int tile)
-{
-    if (cancelled(wf.cancel)) return;
-    Counters *C = wf.C;
-    const ShadowQueue sq = wf.sq;
-    // slot i holds the shadow record of hit i of this bounce, or is empty (job -1)
-    const int n = min(C->h_count[wslot / 3], sq.capacity);
-    const int nl = (int)*wf.max_lights;
-    WorkCount wc{0, 0, 0, 0};
-    unsigned long long rays = 0;
-    // one thread per (hit, light), light-major: neighbouring threads aim at the same light
-    // from neighbouring hit points, so their traversals stay coherent
-    for_each_ray<DYN>(n * nl, &C->work[wslot], tile, [&](int w, bool active) {
-        if (!active) return;
-        const int l = w / n, i = w - l * n;
-        const int job = __float_as_int(sq.wc[i].w);
-        if (job < 0) return;
-        const DevScene &S = wf.scenes[wf.jobs[job].scene];
-        if (l >= S.n_lights) return;
-        const DevLight &L = S.lights[l];
-        if (!L.on) return;
-        ++rays;
-        const V3 P = mk(sq.p[i]);
-        const LightTerm lt = light_term(L, P);
-        if (any_hit<STACK, COUNT>(S, P, lt.p2l, lt.dis, __float_as_int(sq.v[i].w), wc)) return;
-        // the light is visible: the rest of the hit record comes back from L1/L2 here rather
-        // than sitting in registers across the traversal
-        const DevJob &J = wf.jobs[job];
-        const float4 p4 = sq.p[i], v4 = sq.v[i], n4 = sq.n[i], wc4 = sq.wc[i], ws4 = sq.ws[i];
-        const V3 D = mk(v4);
-        const DevMaterial &M = S.mtl[__float_as_int(n4.w)];
-        const V3 N = mk(n4), Wc = mk(wc4), Ws = mk(ws4);
-        V3 ld = mk(L.dif[0], L.dif[1], L.dif[2]), ls = mk(L.spec[0], L.spec[1], L.spec[2]);
-        if (lt.point) ld = vscale(ld, lt.lum), ls = vscale(ls, lt.lum);
-        V3 sum = mk(0.0f, 0.0f, 0.0f);
-        float nn = dot3(N, lt.p2l);
-        if (nn > 0) sum = vmul(Wc, vscale(vmul(mk(M.kd[0], M.kd[1], M.kd[2]), ld), nn));
-        const V3 h = normalise(vsub(lt.p2l, D));
-        nn = dot3(N, h);
-        if (nn > 0) sum = vadd(sum, vmul(Ws, vscale(vmul(mk(M.ks[0], M.ks[1], M.ks[2]), ls), powf(nn, M.shininess))));
-        acc_add(J.acc, __float_as_int(p4.w), sum);
-    });
-    if (wc.err) atomicOr(&C->error, wc.err);
-    for (int off = 16; off > 0; off >>= 1) rays += __shfl_down_sync(kFull, rays, off);
-    if ((threadIdx.x & 31) == 0 && rays) atomicAdd(&C->rays_shadow, rays);
-    if (COUNT) {
-        for (int off = 16; off > 0; off >>= 1) {
-            wc.nodes += __shfl_down_sync(kFull, wc.nodes, off);
-            wc.tris += __shfl_down_sync(kFull, wc.tris, off);
-            wc.spheres += __shfl_down_sync(kFull, wc.spheres, off);
-        }
-        if ((threadIdx.x & 31) == 0) {
-            atomicAdd(&C->s_nodes, (unsigned long long)wc.nodes);
-            atomicAdd(&C->s_tris, (unsigned long long)wc.tris);
-            atomicAdd(&C->s_spheres, (unsigned long long)wc.spheres);
-        }
-    }
-}
-
 // ---- resolve: fixed point -> float rgb and Color::put bytes ---------------------------------------
 __device__ __forceinline__ uint8_t put_channel(float c)
 {
@@ -820,61 +476,33 @@ int sm_count()
     return n;
 }
 
-// resident blocks per SM of a kernel at a block size, queried once (the query costs host time
-// on every launch otherwise, which small renders feel as idle gaps between kernels)
-static int grid_for(const Tuning &t, const void *kernel)
+// resident blocks per SM of a kernel at a block size and dynamic shared memory, queried once (the
+// query costs host time on every launch otherwise, which small renders feel as idle gaps between
+// kernels)
+int grid_for(const Tuning &t, const void *kernel, size_t smem)
 {
     if (t.grid > 0) return t.grid;
     static std::mutex mu;
-    static std::map<std::pair<const void *, int>, int> cache;
+    static std::map<std::pair<const void *, long long>, int> cache;
     std::lock_guard<std::mutex> lock(mu);
-    auto key = std::make_pair(kernel, t.block);
+    auto key = std::make_pair(kernel, (long long)t.block << 32 | (long long)smem);
     auto it = cache.find(key);
     if (it == cache.end()) {
         int per_sm = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, t.block, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, t.block, smem);
         it = cache.emplace(key, per_sm > 0 ? per_sm : 1).first;
     }
     return sm_count() * it->second;
 }
 
-template <bool DYN, bool CNT, bool GEN>
-static void extend_launch(const Wavefront &wf, int sel, int wslot, const Tuning &t, cudaStream_t s)
-{
-#define RT_EXT(MB)                                                                                                \
-    {                                                                                                             \
-        auto k = k_extend<kStack, DYN, CNT, MB, GEN>;                                                             \
-        k<<<grid_for(t, (const void *)k), t.block, 0, s>>>(wf, sel, wslot, t.tile);                              \
-    }
-    if constexpr (CNT) RT_EXT(8)
-    else if (t.min_blocks == 8) RT_EXT(8) else if (t.min_blocks == 6) RT_EXT(6) else if (t.min_blocks == 10) RT_EXT(10)
-    else if (t.min_blocks == 12) RT_EXT(12) else RT_EXT(0)
-#undef RT_EXT
-}
 
 // The counting pass (an untimed statistics pass) runs in one configuration: what it counts
 // does not depend on the launch shape.
-static Tuning count_tuning(const Tuning &t)
+Tuning count_tuning(const Tuning &t)
 {
     Tuning c = t;
     c.block = 128, c.dynamic = true, c.min_blocks = 8;
     return c;
-}
-
-void launch_extend(const Wavefront &wf, int sel, int level, bool gen, const Tuning &t, cudaStream_t s)
-{
-    const int wslot = 3 * level;
-    if (t.count) {
-        const Tuning c = count_tuning(t);
-        if (gen) extend_launch<true, true, true>(wf, sel, wslot, c, s);
-        else extend_launch<true, true, false>(wf, sel, wslot, c, s);
-    } else if (t.dynamic) {
-        if (gen) extend_launch<true, false, true>(wf, sel, wslot, t, s);
-        else extend_launch<true, false, false>(wf, sel, wslot, t, s);
-    } else {
-        if (gen) extend_launch<false, false, true>(wf, sel, wslot, t, s);
-        else extend_launch<false, false, false>(wf, sel, wslot, t, s);
-    }
 }
 
 void launch_shade(const Wavefront &wf, int sel, int level, const Tuning &t, cudaStream_t s)
@@ -889,28 +517,6 @@ void launch_shade(const Wavefront &wf, int sel, int level, const Tuning &t, cuda
         auto k = k_shade<false>;
         k<<<grid_for(ts, (const void *)k), 128, 0, s>>>(wf, sel, wslot);
     }
-}
-
-template <bool DYN, bool CNT>
-static void shadow_launch(const Wavefront &wf, int wslot, const Tuning &t, cudaStream_t s)
-{
-#define RT_SHD(MB)                                                                                                \
-    {                                                                                                             \
-        auto k = k_shadow<kStack, DYN, CNT, MB>;                                                                      \
-        k<<<grid_for(t, (const void *)k), t.block, 0, s>>>(wf, wslot, t.tile);                                   \
-    }
-    if constexpr (CNT) RT_SHD(8)
-    else if (t.min_blocks == 8) RT_SHD(8) else if (t.min_blocks == 6) RT_SHD(6) else if (t.min_blocks == 10) RT_SHD(10)
-    else if (t.min_blocks == 12) RT_SHD(12) else RT_SHD(0)
-#undef RT_SHD
-}
-
-void launch_shadow(const Wavefront &wf, int level, const Tuning &t, cudaStream_t s)
-{
-    const int wslot = 3 * level + 2;
-    if (t.count) shadow_launch<true, true>(wf, wslot, count_tuning(t), s);
-    else if (t.dynamic) shadow_launch<true, false>(wf, wslot, t, s);
-    else shadow_launch<false, false>(wf, wslot, t, s);
 }
 
 void launch_resolve(const FrameBufs &fb, int width, int height, int spp, cudaStream_t s)

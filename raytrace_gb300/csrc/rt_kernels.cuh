@@ -47,19 +47,16 @@ struct Wavefront {
     const volatile int *cancel;       // device cancel flag (NULL = not cancellable)
 };
 
-// Traversal stack entries. A Karras node's common prefix grows by at least one bit per level
-// over 30 Morton bits plus the index bits that break ties, so a path has at most 63 binary
-// levels, i.e. 32 four-wide nodes, each pushing at most 3 entries.
-constexpr int kStack = 96;
-
 struct Tuning {
     int block = 128;     // threads per block of the traversal kernels
     int tile = 32;       // rays per dynamic work fetch (multiple of 32)
-    int stack = kStack;  // traversal stack entries (fixed: see kStack)
+    int stack = 0;       // traversal stack entries kept in shared memory per thread: 0, 8 or 16
+                         // (the rest of the kStack entries in local memory)
     bool dynamic = true; // persistent grid pulling tiles from a global counter
     bool count = false;  // count BVH nodes / triangles / spheres
     int grid = 0;        // blocks (0 = derived from the SM count)
-    int min_blocks = 8;  // 0, 6, 8, 10 or 12: register cap of the traversal kernels (128-thread blocks)
+    int min_blocks = 8;  // 0, 6 or 8: register cap of the traversal kernels (128-thread blocks)
+    int shadow_chunk = 0;   // shadow work in light-major chunks of this many hits (0 = one chunk)
 };
 
 int sm_count();

@@ -673,8 +673,12 @@ cudaError_t morton_and_sort(const LbvhInput &in, const Scratch &sc, cudaStream_t
 {
     const int n = in.n + in.n_sph;
     const int tiles = (n + kTileKeys - 1) / kTileKeys;
-    cudaMemsetAsync(sc.box, 0xff, 12, s);
-    cudaMemsetAsync(sc.box + 3, 0, 12, s);
+    cudaError_t e = cudaMemsetAsync(sc.box, 0xff, 12, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(sc.box + 3, 0, 12, s);
+    if (e != cudaSuccess) {
+        g_build_step = "scene box";
+        return e;
+    }
     k_prep<<<grid_of(n, 256), 256, 0, s>>>(in, sc.centroid, sc.box);
     k_morton<<<grid_of(n, 256), 256, 0, s>>>(n, sc.centroid, sc.box, sc.codes[0], sc.idx[0]);
     {
@@ -837,7 +841,6 @@ cudaError_t lbvh_build(const LbvhInput &in, const LbvhOutput &out, void *scratch
 // for their scan, the scene box and a zero object position). Every GPU that loads the library
 // holds it until the process exits.
 #include <cstdio>
-#include <mutex>
 
 #include "../../include/rt_gb300.h"
 
@@ -851,10 +854,6 @@ constexpr size_t kNoAllocBytes = 256 + 256 + 16 * kNoAllocN + 4 * kNoAllocN + 4 
                                  1024 * kNoAllocTiles + 4 * kNoAllocChunks;
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 
-constexpr int kNoAllocMaxDevices = 64;
-void *g_noalloc_ptr[kNoAllocMaxDevices];
-std::mutex g_noalloc_mu;
-
 } // namespace
 } // namespace rtg
 
@@ -862,11 +861,12 @@ std::mutex g_noalloc_mu;
 // device memory is owned and budgeted by that application, or code on a latency-bound path
 // where cudaMalloc / cudaFree would block on the device. They pass device buffers they
 // already own; this entry point uses only the fixed array above (no cudaMalloc, cudaFree or
-// allocating library call). The first call on a device looks up the array's device address
-// for that device (cudaGetSymbolAddress, with the device current); make that first call
-// before any stream capture. All calls share the one array, which keeps the last call's
-// contents: calls that overlap on the GPU (two streams, two threads) race and corrupt each
-// other's results, so serialise them.
+// allocating library call). Every call looks up the array's device address on the current
+// device (cudaGetSymbolAddress): an address kept from an earlier call would dangle after a
+// cudaDeviceReset, which reloads the module. The first call on a device loads the module
+// there; make that first call before any stream capture. All calls share the one array,
+// which keeps the last call's contents: calls that overlap on the GPU (two streams, two
+// threads) race and corrupt each other's results, so serialise them.
 extern "C" int rt_morton_sort_noalloc(const float *d_tri_p, int64_t n_tris, uint32_t *d_codes, uint32_t *d_perm,
                                       void *cuda_stream)
 {
@@ -878,20 +878,13 @@ extern "C" int rt_morton_sort_noalloc(const float *d_tri_p, int64_t n_tris, uint
         return RT_ERR_TOO_LARGE;
     }
     if (n_tris == 0) return RT_OK;
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kNoAllocMaxDevices) return RT_ERR_CUDA;
+    // an error the caller's own CUDA work left pending is theirs: report it without clearing
+    // it, rather than taking it for a failure of the launches below
+    if (cudaPeekAtLastError() != cudaSuccess) return RT_ERR_CUDA;
     void *base = nullptr;
-    {
-        std::lock_guard<std::mutex> lk(g_noalloc_mu);
-        if (!g_noalloc_ptr[dev]) {
-            void *p = nullptr;
-            if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) {
-                cudaGetLastError();
-                return RT_ERR_CUDA;
-            }
-            g_noalloc_ptr[dev] = p;
-        }
-        base = g_noalloc_ptr[dev];
+    if (cudaGetSymbolAddress(&base, g_noalloc_scratch) != cudaSuccess || !base) {
+        cudaGetLastError();   // the failed lookup's own error
+        return RT_ERR_CUDA;
     }
     const int n = (int)n_tris;
     cudaStream_t s = (cudaStream_t)cuda_stream;

@@ -137,6 +137,8 @@ struct rt_server {
     double first_arrival = -1.0, last_done = 0.0;
     unsigned long long plain_rays = 0;
     long long waves0 = 0, wave_jobs0 = 0;
+    double host_step_s = 0.0, host_wait_s = 0.0;   // inside rt_server_step; blocked on frame copies
+    int64_t steps = 0;
     std::map<std::pair<int, int>, int> plain_frames;
     int64_t plain_frame_bytes = 0;
 
@@ -396,7 +398,12 @@ static int retire(rt_server *srv, bool wait_one)
     rt_ctx *ctx = srv->ctx;
     while (!srv->resolving.empty()) {
         Request *r = srv->resolving.front();
-        cudaError_t e = wait_one ? cudaEventSynchronize(r->done_ev) : cudaEventQuery(r->done_ev);
+        cudaError_t e = cudaEventQuery(r->done_ev);
+        if (e == cudaErrorNotReady && wait_one) {
+            const auto t0 = Clock::now();
+            e = cudaEventSynchronize(r->done_ev);
+            srv->host_wait_s += std::chrono::duration<double>(Clock::now() - t0).count();
+        }
         wait_one = false;
         if (e == cudaErrorNotReady) break;
         if (e != cudaSuccess) return srv_fail(srv, RT_ERR_CUDA, "frame copy: %s", cudaGetErrorString(e));
@@ -529,6 +536,10 @@ static void reset_stats(rt_server *srv)
     srv->waves0 = srv->runner.waves;
     srv->wave_jobs0 = srv->runner.wave_jobs;
     srv->peak_bytes = used_bytes(srv);
+    srv->runner.wave_ms.clear();
+    srv->runner.wait_s = 0.0;
+    srv->host_step_s = srv->host_wait_s = 0.0;
+    srv->steps = 0;
 }
 
 static double percentile(std::vector<double> v, double p)
@@ -565,6 +576,17 @@ static void fill_stats(const rt_server *srv, rt_serve_stats *st)
     st->mean_wave_requests = st->waves ? (double)(srv->runner.wave_jobs - srv->wave_jobs0) / (double)st->waves : 0.0;
     st->admitted_busy = srv->admitted_busy;
     st->pixels = srv->pixels;
+    const std::vector<float> &w = srv->runner.wave_ms;
+    std::vector<double> wd(w.begin(), w.end());
+    double busy = 0.0;
+    for (double x : wd) busy += x;
+    st->wave_ms_mean = wd.empty() ? 0.0 : busy / (double)wd.size();
+    st->wave_ms_p50 = percentile(wd, 0.50);
+    st->wave_ms_p99 = percentile(wd, 0.99);
+    st->device_busy_s = 1e-3 * busy;
+    st->host_step_s = srv->host_step_s;
+    st->host_wait_s = srv->host_wait_s + srv->runner.wait_s;
+    st->steps = srv->steps;
 }
 
 // orbit camera about the world origin (Camera::lookAt with up = +y, 3DElement.cpp:364)
@@ -789,7 +811,10 @@ int rt_server_submit(rt_server *srv, const rt_request *req, int64_t *request_id)
 int rt_server_step(rt_server *srv, int32_t *n_pending)
 {
     if (!srv) return RT_ERR_INVALID;
+    const auto t0 = Clock::now();
     int rc = srv->cfg.plain ? step_plain(srv) : step_batched(srv);
+    srv->host_step_s += std::chrono::duration<double>(Clock::now() - t0).count();
+    srv->steps++;
     if (n_pending) *n_pending = pending(srv);
     return rc;
 }

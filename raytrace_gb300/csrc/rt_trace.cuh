@@ -174,6 +174,55 @@ __device__ __forceinline__ void sort4(float t[4], int c[4])
 }
 constexpr float kInf = __builtin_huge_valf();
 
+// ---- traversal stack (kStack entries, rt_device.cuh) --------------------------------------
+
+// the launch's dynamic shared memory: the traversal kernels' short stacks
+extern __shared__ int rt_short_stack[];
+
+// A thread's traversal stack. With SS > 0 (a power of two) its top SS entries live in shared
+// memory, SS * blockDim.x ints given at launch, entry slot k of thread t at
+// [k * blockDim.x + t] so that a warp's accesses fall in 32 different banks; deeper entries go
+// to a local-memory array: a push beyond SS moves the entry SS below it out to local memory, a
+// pop brings it back. Most paths stay within SS entries and never touch local memory, which
+// also holds the node lines in L1. SS = 0 keeps the whole stack in local memory.
+template <int SS>
+struct TravStack {
+    int deep[kStack - SS];
+    int sp;
+    __device__ __forceinline__ TravStack() : sp(0) {}
+    __device__ __forceinline__ bool empty() const { return sp == 0; }
+    __device__ __forceinline__ int *slot(int e) const
+    {
+        return rt_short_stack + (e & (SS - 1)) * (int)blockDim.x + (int)threadIdx.x;
+    }
+    // false when all kStack entries are taken (the entry is dropped; the caller flags it)
+    __device__ __forceinline__ bool push(int v)
+    {
+        if (sp >= kStack) return false;
+        if constexpr (SS == 0) {
+            deep[sp] = v;
+        } else {
+            int *s = slot(sp);
+            if (sp >= SS) deep[sp - SS] = *s;
+            *s = v;
+        }
+        ++sp;
+        return true;
+    }
+    __device__ __forceinline__ int pop()
+    {
+        --sp;
+        if constexpr (SS == 0) {
+            return deep[sp];
+        } else {
+            int *s = slot(sp);
+            const int v = *s;
+            if (sp >= SS) *s = deep[sp - SS];
+            return v;
+        }
+    }
+};
+
 struct WorkCount {
     unsigned nodes, tris, spheres;
     int err;   // 1: a child index outside the node array, 2: visit limit reached
@@ -201,7 +250,7 @@ __device__ __forceinline__ Leaf load_leaf(const float4 *__restrict__ tri, int k)
 // ---- closest hit ---------------------------------------------------------------------------
 // excl: the ray's exclude key (-1 = none). inside: Ray::isInside != 0. Writes the winner to
 // `best` and the exclude key for the children to `newobj`.
-template <int STACK, bool COUNT>
+template <int SS, bool COUNT>
 __device__ void closest_hit(const DevScene &S, V3 O, V3 D, int excl, bool inside, Best &best, int &newobj, WorkCount &wc)
 {
     // "no hit" sits at 1e20 with order -1: a primitive must be strictly closer to replace it,
@@ -267,8 +316,7 @@ __device__ void closest_hit(const DevScene &S, V3 O, V3 D, int excl, bool inside
             const float4 *__restrict__ quads = S.quads;
             const RayInv ri = make_inv(O, D);
             const unsigned last = (unsigned)S.n_leaves - 2u;   // internal nodes 0..L-2
-            int stack[STACK];
-            int sp = 0;
+            TravStack<SS> stack;
             int node = 0;
             for (unsigned visits = 0;; ++visits) {
                 if (COUNT) wc.nodes++;
@@ -305,8 +353,8 @@ __device__ void closest_hit(const DevScene &S, V3 O, V3 D, int excl, bool inside
                     n_in += in;
                 }
                 if (n_in == 0) {
-                    if (sp == 0) break;
-                    node = stack[--sp];
+                    if (stack.empty()) break;
+                    node = stack.pop();
                     continue;
                 }
                 if (n_in == 1) {
@@ -315,10 +363,8 @@ __device__ void closest_hit(const DevScene &S, V3 O, V3 D, int excl, bool inside
                 }
                 sort4(t, c);   // nearest next, the others pushed farthest first
                 node = c[0];
-                for (int k = n_in - 1; k >= 1; --k) {
-                    if (sp < STACK) stack[sp++] = c[k];
-                    else wc.err |= 4;
-                }
+                for (int k = n_in - 1; k >= 1; --k)
+                    if (!stack.push(c[k])) wc.err |= 4;
             }
         }
     }
@@ -371,10 +417,10 @@ __device__ __forceinline__ int any_hit_begin(const DevScene &S, V3 O, V3 D, floa
 
 // one 4-wide node visit: 1 blocked, 0 not blocked (the stack ran empty), -1 continue at `node`
 // (the tree is given by its node and leaf arrays and leaf count, held in registers by the caller)
-template <int STACK, bool COUNT>
+template <int SS, bool COUNT>
 __device__ __forceinline__ int any_hit_step(const float4 *__restrict__ quads, const float4 *__restrict__ tri, int n_leaves,
-                                            V3 O, V3 D, const RayInv &ri, float dis, int excl, int &node, int &sp,
-                                            int *stack, unsigned &visits, WorkCount &wc)
+                                            V3 O, V3 D, const RayInv &ri, float dis, int excl, int &node,
+                                            TravStack<SS> &stack, unsigned &visits, WorkCount &wc)
 {
     if (COUNT) wc.nodes++;
     if ((unsigned)node > (unsigned)n_leaves - 2u || visits++ >= kMaxVisits) {
@@ -395,9 +441,7 @@ __device__ __forceinline__ int any_hit_step(const float4 *__restrict__ quads, co
             leaves |= 1u << k;
         else if (next < 0)
             next = c[k];
-        else if (sp < STACK)
-            stack[sp++] = c[k];
-        else
+        else if (!stack.push(c[k]))
             wc.err |= 4;
     }
     while (leaves) {   // one code copy of the leaf test
@@ -414,23 +458,22 @@ __device__ __forceinline__ int any_hit_step(const float4 *__restrict__ quads, co
         node = next;
         return -1;
     }
-    if (sp == 0) return 0;
-    node = stack[--sp];
+    if (stack.empty()) return 0;
+    node = stack.pop();
     return -1;
 }
 
 // true when some primitive other than `excl` is hit at a distance below `dis`
-template <int STACK, bool COUNT>
+template <int SS, bool COUNT>
 __device__ bool any_hit(const DevScene &S, V3 O, V3 D, float dis, int excl, WorkCount &wc)
 {
     int r = any_hit_begin<COUNT>(S, O, D, dis, excl, wc);
     if (r >= 0) return r == 1;
     const RayInv ri = make_inv(O, D);
-    int stack[STACK];
-    int node = 0, sp = 0;
+    TravStack<SS> stack;
+    int node = 0;
     unsigned visits = 0;
-    while ((r = any_hit_step<STACK, COUNT>(S.quads, S.tri, S.n_leaves, O, D, ri, dis, excl, node, sp, stack, visits,
-                                           wc)) < 0) {
+    while ((r = any_hit_step<SS, COUNT>(S.quads, S.tri, S.n_leaves, O, D, ri, dis, excl, node, stack, visits, wc)) < 0) {
     }
     return r == 1;
 }

@@ -3,7 +3,8 @@
 The reference arm times the CPU oracle on a bounded sample of the config-2 frame. Nearly all
 of that frame's CPU time sits in the terrain rows (a sky tile costs about a thousandth of a
 terrain tile), so the sample takes one tile from each band of tile rows; a uniform draw of a
-few tiles could land on sky only and overstate the rate many times over.
+few tiles could land on sky only and overstate the rate many times over. The GPU arm's
+CPU baseline takes two tiles from every tile row and reports a bootstrap interval.
 """
 import json
 import os
@@ -32,9 +33,25 @@ def test_tiles_are_one_per_band_of_rows(n):
         assert bench.cpu_tiles(n, seed) == tiles   # seeded
 
 
-def test_full_sample_covers_every_tile_row():
+def test_full_sample_takes_two_tiles_from_every_tile_row():
     rows = sorted(t // BW for t in bench.cpu_tiles(bench.CPU_SAMPLE_TILES, 0))
-    assert rows == list(range(BH))
+    assert rows == sorted(list(range(BH)) * 2)
+
+
+def test_bootstrap_interval_brackets_the_measured_rate():
+    """The CPU baseline's 95 % interval: tiles resampled within their row, scaled to the
+    measured wall-clock rate; it contains that rate and widens with the spread of tile costs."""
+    import numpy as np
+
+    rng = np.random.default_rng(0)
+    rows = np.repeat(np.arange(16), 2)
+    rays = rng.integers(10_000, 20_000, size=32)
+    even = rays / 1e5
+    lo, hi = bench.bootstrap_rate(rays, even, rows, 0.25)
+    assert lo == hi == 0.25   # every tile at the same rate: no spread
+    uneven = even * rng.uniform(0.2, 5.0, size=32)
+    lo, hi = bench.bootstrap_rate(rays, uneven, rows, 0.25)
+    assert lo < 0.25 < hi
 
 
 def test_reference_arm_prints_the_contract_line():
@@ -47,4 +64,5 @@ def test_reference_arm_prints_the_contract_line():
     assert d["higher_is_better"] is True and d["steps"] == 1 and d["warmup"] == 3
     assert d["value"] > 0 and d["cpu_baseline"]["value"] == d["value"]
     assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["cores"] >= 1
+    assert d["cpu_baseline"]["cpu_model"]
     assert d["e2e"] == {"value": d["value"], "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}

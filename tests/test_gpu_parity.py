@@ -168,6 +168,43 @@ def test_deterministic_and_order_independent(ctx):
     np.testing.assert_array_equal(a["rgb"].view(np.uint32), b["rgb"].view(np.uint32))
 
 
+TUNINGS = [(0, 0, 8), (8, 0, 8), (16, 0, 8), (8, 2048, 8), (16, 64, 6), (0, 32768, 0)]   # (stack, chunk, cap)
+
+
+@pytest.mark.parametrize("stack,chunk,cap", TUNINGS)
+def test_tuning_variants_give_the_same_image(ctx, stack, chunk, cap):
+    """Traversal stack entries in shared memory (0, 8, 16), shadow work in light-major chunks and
+    register caps change only how the work runs: every variant's frame is the default's bit for
+    bit, through the plain path and through the batch path, on a deep jittered frame with
+    refraction (long traversal stacks) and on a config-3 mesh."""
+    scene = rt.SceneHost.small(21, 14, 12, 96, 64, 2)
+    mesh = rt.SceneHost.config(3, 4)
+    want = [gpu_render(ctx, scene, 96, 64, 4, 4, 77, ref_tiles=False)[0],
+            gpu_render(ctx, mesh, 128, 96, 1, 3, 0, ref_tiles=False)[0]]
+    ctx.set_tuning(rt.BatchTuning(128 if cap else 256, 32, stack, 1, cap, 1, 0, chunk))
+    try:
+        got = [gpu_render(ctx, scene, 96, 64, 4, 4, 77, ref_tiles=False)[0],
+               gpu_render(ctx, mesh, 128, 96, 1, 3, 0, ref_tiles=False)[0]]
+    finally:
+        ctx.set_tuning(None)
+    for g, w in zip(got, want):
+        np.testing.assert_array_equal(g["rgb"].view(np.uint32), w["rgb"].view(np.uint32))
+        np.testing.assert_array_equal(g["obj"], w["obj"])
+    sids = [ctx.upload(scene), ctx.upload(mesh)]
+    fids = [ctx.frame(96, 64), ctx.frame(128, 96)]
+    rds = [ctx.render_desc(96, 64, 4, 4, flags=rt.RT_FLAG_HIT_PLANES, seed=77),
+           ctx.render_desc(128, 96, 1, 3, flags=rt.RT_FLAG_HIT_PLANES)]
+    try:
+        ctx.batch(sids, fids, rds, tuning=rt.BatchTuning(128 if cap else 256, 64, stack, 1, cap, 1, 0, chunk))
+        for f, (w, h), ref in zip(fids, [(96, 64), (128, 96)], want):
+            np.testing.assert_array_equal(ctx.download(f, w, h)["rgb"].view(np.uint32), ref["rgb"].view(np.uint32))
+    finally:
+        for f in fids:
+            ctx.release_frame(f)
+        for s in sids:
+            ctx.release_scene(s)
+
+
 def test_render_host_equals_device_path(ctx):
     scene = rt.SceneHost.small(31, 10, 6, 128, 96, 3)
     out, _ = gpu_render(ctx, scene, 128, 96, 1, 3, 0, ref_tiles=False)
@@ -329,6 +366,54 @@ def test_cancel_stops_a_render_and_the_next_render_is_whole(ctx):
     finally:
         ctx.release_frame(fid)
         ctx.release_scene(sid)
+
+
+def test_cancel_mark_orders_cancels_against_renders(ctx):
+    """A cancel made after the mark ends rt_render_host_since even though it came before the
+    call; a cancel made before a render began (rt_render, rt_render_host) does not end it."""
+    import ctypes
+
+    scene = rt.SceneHost.small(seed=9, n_spheres=6, ico_freq=8, width=96, height=64, refractive_every=3)
+    rd = ctx.render_desc(96, 64, 1, 3)
+    rgb8 = np.zeros((64, 96, 3), np.uint8)
+    st = rt.RenderStats()
+    mark = rt.lib.rt_cancel_mark(ctx.handle)
+    assert rt.lib.rt_cancel(ctx.handle) == 0
+    assert rt.lib.rt_cancel_mark(ctx.handle) == mark + 1
+    rc = rt.lib.rt_render_host_since(ctx.handle, mark, scene.desc_ptr(), ctypes.byref(rd),
+                                     rgb8.ctypes.data_as(ctypes.c_void_p), None, ctypes.byref(st))
+    assert rc == rt.RT_ERR_CANCELLED
+    assert not rgb8.any()
+    # the same cancel is older than these calls: both complete
+    _, got8, _ = ctx.render_host(scene, rd, 96, 64)
+    out, _ = gpu_render(ctx, scene, 96, 64, 1, 3, 0, ref_tiles=False)
+    np.testing.assert_array_equal(got8, out["rgb8"])
+    rc = rt.lib.rt_render_host_since(ctx.handle, rt.lib.rt_cancel_mark(ctx.handle), scene.desc_ptr(), ctypes.byref(rd),
+                                     rgb8.ctypes.data_as(ctypes.c_void_p), None, ctypes.byref(st))
+    assert rc == rt.RT_OK
+    np.testing.assert_array_equal(rgb8, out["rgb8"])
+
+
+def test_dropin_stop_right_after_start_cancels_that_render():
+    """RayTracer::stop() at once after start(): the render ends (RT_ERR_CANCELLED) sooner than a
+    whole render takes and leaves `output` as start() set it; a stop() made with nothing running
+    does not affect the next start()."""
+    import json
+
+    lib_dir = os.path.dirname(rt.LIB_PATH)
+    with tempfile.TemporaryDirectory() as d:
+        exe = os.path.join(d, "dropin_stop_test")
+        subprocess.run(["g++", "-O2", "-std=c++17", "-ffp-contract=off",
+                        os.path.join(ROOT, "tests", "cpp", "dropin_stop_test.cpp"), "-o", exe, f"-L{lib_dir}",
+                        "-lrt_gb300", f"-Wl,-rpath,{lib_dir}", "-pthread"], check=True)
+        r = subprocess.run([exe], check=True, capture_output=True, text=True, timeout=300)
+    res = json.loads(r.stdout.strip().splitlines()[-1])
+    print("dropin stop", res)
+    assert res["full_status"] == rt.RT_OK
+    assert res["stop_status"] == rt.RT_ERR_CANCELLED
+    assert res["untouched"] == 1
+    assert res["stop_s"] < res["full_s"]
+    assert res["after_status"] == rt.RT_OK and res["written"] == 1
 
 
 @pytest.mark.parametrize("mode", [rt.RT_MODE_DEPTH, rt.RT_MODE_NORMAL, rt.RT_MODE_TEXTURE, rt.RT_MODE_MATERIAL,

@@ -37,6 +37,36 @@ def test_noalloc_matches_allocating_sort_twice_in_a_row():
             np.testing.assert_array_equal(perm, ref_perm)
 
 
+def test_noalloc_at_capacity_matches_and_allocates_nothing():
+    """Exactly RT_NOALLOC_MAX_TRIS triangles (the fixed array's layout is tight there) against the
+    allocating sort; after a first call has loaded the array, a second call changes neither the
+    device's free memory nor torch's allocated bytes."""
+    torch = pytest.importorskip("torch")
+    n = rt.RT_NOALLOC_MAX_TRIS
+    tri = np.random.default_rng(99).uniform(-50, 50, size=(n, 9)).astype(np.float32)
+    d_tri = torch.from_numpy(tri).cuda()
+    d_codes = torch.empty(n, dtype=torch.int32, device="cuda")
+    d_perm = torch.empty(n, dtype=torch.int32, device="cuda")
+    stream = torch.cuda.current_stream().cuda_stream
+
+    def call():
+        d_codes.fill_(-1)
+        d_perm.fill_(-1)
+        rc = rt.lib.rt_morton_sort_noalloc(d_tri.data_ptr(), n, d_codes.data_ptr(), d_perm.data_ptr(), stream)
+        torch.cuda.synchronize()
+        return rc
+
+    assert call() == rt.RT_OK   # first call on the device: loads the library's array
+    free0, allocated0 = torch.cuda.mem_get_info()[0], torch.cuda.memory_allocated()
+    assert call() == rt.RT_OK
+    free1, allocated1 = torch.cuda.mem_get_info()[0], torch.cuda.memory_allocated()
+    assert (free1, allocated1) == (free0, allocated0)
+    with rt.Context(0) as ctx:
+        ref_codes, ref_perm = ctx.morton_sort(tri)
+    np.testing.assert_array_equal(d_codes.cpu().numpy().view(np.uint32), ref_codes)
+    np.testing.assert_array_equal(d_perm.cpu().numpy().view(np.uint32), ref_perm)
+
+
 def test_noalloc_rejects_inputs_beyond_capacity():
     torch = pytest.importorskip("torch")
     n = rt.RT_NOALLOC_MAX_TRIS + 1
