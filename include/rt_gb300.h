@@ -266,8 +266,10 @@ typedef struct rt_batch_tuning {
     int32_t dynamic;             /* 0 or 1: pull ray tiles from a counter; 2: static grid stride */
     int64_t wave_rays;           /* batch: ray-queue entries of one wave (0 = 2^26) */
     int32_t shadow_chunk;        /* shadow rays light-major within chunks of this many hits, a
-                                    multiple of 32 (0 = all of a bounce's hits in one chunk) */
-    int32_t reserved;            /* 0 */
+                                    multiple of 32 (0 = all of a bounce's hits in one chunk; the
+                                    default tuning uses 4096) */
+    int32_t pixel_tile;          /* primary rays traced in square pixel tiles of this edge, 0 (row by
+                                    row) or 2..64; the image does not depend on it */
 } rt_batch_tuning;
 
 /* kernel tuning of the plain per-scene path (rt_render); NULL restores the defaults */
@@ -282,7 +284,8 @@ int rt_batch_render(rt_ctx *ctx, int32_t n, const int32_t *scene_ids, const int3
 int rt_batch_render_plain(rt_ctx *ctx, int32_t n, const int32_t *scene_ids,
                           const int32_t *frame_ids, const rt_render_desc *rds);
 /* pick block size, register cap and ray tile (or the static stride) for these jobs by timing
- * candidates, then the short-stack depth in shared memory, the shadow chunk and the wave size.
+ * candidates, then the short-stack depth in shared memory, the pixel tile, the shadow chunk
+ * and the wave size.
  * Writes the choice. */
 int rt_batch_autotune(rt_ctx *ctx, int32_t n, const int32_t *scene_ids, const int32_t *frame_ids,
                       const rt_render_desc *rds, rt_batch_tuning *out);
@@ -353,6 +356,9 @@ typedef struct rt_serve_stats {
 int    rt_server_create(rt_ctx *ctx, const rt_server_config *cfg, rt_server **out);
 void   rt_server_destroy(rt_server *srv);
 const char *rt_server_last_error(const rt_server *srv);
+/* kernel tuning of the server's waves (NULL = the defaults; the plain mode sets the context's
+ * tuning, which its renders use); requests admitted from now on use it. Images do not depend on it. */
+int    rt_server_set_tuning(rt_server *srv, const rt_batch_tuning *tuning);
 /* register a scene (deep copy kept for rebuilds); it is uploaded now if the budget allows */
 int    rt_server_add_scene(rt_server *srv, const rt_scene_desc *desc, int32_t *scene);
 int    rt_server_submit(rt_server *srv, const rt_request *req, int64_t *request_id);

@@ -91,10 +91,10 @@ class RenderStats(C.Structure):
 class BatchTuning(C.Structure):
     _fields_ = [("block", C.c_int32), ("tile", C.c_int32), ("stack", C.c_int32), ("use_graph", C.c_int32),
                 ("min_blocks", C.c_int32), ("dynamic", C.c_int32), ("wave_rays", C.c_int64),
-                ("shadow_chunk", C.c_int32), ("reserved", C.c_int32)]
+                ("shadow_chunk", C.c_int32), ("pixel_tile", C.c_int32)]
 
     def as_dict(self) -> dict:
-        return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
+        return {k: getattr(self, k) for k, _ in self._fields_}
 
 
 class ServerConfig(C.Structure):
@@ -173,6 +173,7 @@ _SIGS = {
     "rt_orbit_camera": (C.c_int, [C.POINTER(Camera), C.c_double, C.c_double, C.c_int32, C.c_int32,
                                   C.POINTER(Camera)]),
     "rt_server_add_scene": (C.c_int, [P, C.POINTER(SceneDesc), C.POINTER(C.c_int32)]),
+    "rt_server_set_tuning": (C.c_int, [P, C.POINTER(BatchTuning)]),
     "rt_server_submit": (C.c_int, [P, C.POINTER(Request), C.POINTER(C.c_int64)]),
     "rt_server_step": (C.c_int, [P, C.POINTER(C.c_int32)]),
     "rt_server_drain": (C.c_int, [P]),
@@ -551,6 +552,10 @@ class Server:
     def _ck(self, rc: int, what: str) -> None:
         if rc:
             raise RTError(rc, f"{what}: {lib.rt_server_last_error(self._h).decode(errors='replace')}")
+
+    def set_tuning(self, tuning: BatchTuning | None) -> None:
+        self._ck(lib.rt_server_set_tuning(self._h, C.byref(tuning) if tuning is not None else None),
+                 "rt_server_set_tuning")
 
     def add_scene(self, scene: SceneHost) -> int:
         sid = C.c_int32()

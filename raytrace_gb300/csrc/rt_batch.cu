@@ -234,6 +234,7 @@ static int batch_core(rt_ctx *ctx, int32_t n, const int32_t *scene_ids, const in
         WaveJob &w = jobs[i];
         int rc = make_job(ctx, *si->second, *fi->second, &rds[i], 0, w.job, w.total);
         if (rc) return rc;
+        w.job.pixel_tile = t.pixel_tile;
         w.scene = si->second.get();
         w.weight = wave_weight(w.scene->branching, rds[i].max_level);
         frames[i] = fi->second.get();
@@ -352,15 +353,17 @@ extern "C" int rt_batch_autotune(rt_ctx *ctx, int32_t n, const int32_t *scene_id
     // Coordinate search, each candidate timed as the best of three batches after a warm one
     // (which captures its graph): (threads per block, register cap as resident blocks per SM) x
     // rays per tile fetch (0 = the static grid stride), then the traversal stack entries kept in
-    // shared memory, then the shadow work chunk, then the wave size. The caller picks the jobs:
+    // shared memory, then the primary rays' pixel tile, then the shadow work chunk, then the wave
+    // size. The caller picks the jobs:
     // tuning on a sample of the workload and measuring on the rest keeps the choice honest.
     const int shapes[][2] = {{128, 8}, {128, 6}, {64, 8}, {256, 0}};
     const int tiles[] = {0, 32, 64, 128, 256};
     const int stacks[] = {0, 8, 16};
-    const int chunks[] = {0, 2048, 8192, 32768};
+    const int chunks[] = {0, 1024, 4096, 16384};
+    const int pixel_tiles[] = {0, 8, 16, 32};
     const long long waves[] = {1ll << 25, 1ll << 27};   // the default is 2^26
     double best = 1e30;
-    rt_batch_tuning best_t{128, 32, 0, 1, 8, 1, 0, 0, 0};
+    rt_batch_tuning best_t{128, 32, 0, 1, 8, 1, 0, 4096, 0};
     auto trial = [&](const rt_batch_tuning &t) {
         int rc = rt_batch_render(ctx, n, scene_ids, frame_ids, rds, &t);   // warm (captures the graph)
         if (rc) return rc;
@@ -377,13 +380,20 @@ extern "C" int rt_batch_autotune(rt_ctx *ctx, int32_t n, const int32_t *scene_id
     };
     for (const auto &sh : shapes)
         for (int tl : tiles) {
-            int rc = trial(rt_batch_tuning{sh[0], tl ? tl : 32, 0, 1, sh[1], tl ? 1 : 2, 0, 0, 0});
+            int rc = trial(rt_batch_tuning{sh[0], tl ? tl : 32, 0, 1, sh[1], tl ? 1 : 2, 0, 4096, 0});
             if (rc) return rc;
         }
     for (int ss : stacks) {
         if (ss == best_t.stack) continue;
         rt_batch_tuning t = best_t;
         t.stack = ss;
+        int rc = trial(t);
+        if (rc) return rc;
+    }
+    for (int pt : pixel_tiles) {
+        if (pt == best_t.pixel_tile) continue;
+        rt_batch_tuning t = best_t;
+        t.pixel_tile = pt;
         int rc = trial(t);
         if (rc) return rc;
     }

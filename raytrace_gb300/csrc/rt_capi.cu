@@ -938,6 +938,7 @@ static int render_once(rt_ctx *ctx, SceneDev &sc, FrameDev &f, const rt_render_d
     long long samples = 0;
     int rc = make_job(ctx, sc, f, rd, 0, J, samples);
     if (rc) return rc;
+    J.pixel_tile = ctx->plain_tuning.pixel_tile;
     if (qcap <= 0) qcap = ctx->test_queue > 0 ? ctx->test_queue : std::max<long long>(2 * samples, 4096);
     rc = ws_ensure(ctx, ctx->ws, qcap, 1);
     if (rc) return rc;
@@ -1064,6 +1065,7 @@ int tuning_from(rt_ctx *ctx, const rt_batch_tuning *in, Tuning &t)
     t.stack = in->stack;
     t.min_blocks = in->min_blocks;
     t.shadow_chunk = in->shadow_chunk;
+    t.pixel_tile = in->pixel_tile;
     if (in->dynamic < 0 || in->dynamic > 2) return ctx_fail(ctx, RT_ERR_INVALID, "dynamic %d: use 0, 1 or 2", in->dynamic);
     t.dynamic = in->dynamic != 2;
     if (t.block % 32 || t.block < 32 || t.block > 256 || t.tile % 32 || t.tile <= 0 || t.tile > 4096)
@@ -1075,6 +1077,8 @@ int tuning_from(rt_ctx *ctx, const rt_batch_tuning *in, Tuning &t)
         return ctx_fail(ctx, RT_ERR_INVALID, "stack %d: use 0, 8 or 16 shared-memory entries", t.stack);
     if (t.shadow_chunk < 0 || t.shadow_chunk % 32 || t.shadow_chunk > (1 << 27))
         return ctx_fail(ctx, RT_ERR_INVALID, "shadow_chunk %d: a multiple of 32 in [0, 2^27]", t.shadow_chunk);
+    if (t.pixel_tile < 0 || t.pixel_tile == 1 || t.pixel_tile > 64)
+        return ctx_fail(ctx, RT_ERR_INVALID, "pixel_tile %d: 0 or 2..64", t.pixel_tile);
     return RT_OK;
 }
 
@@ -1083,14 +1087,14 @@ long long tuning_key(int max_level, const Tuning &t)
 {
     return (long long)max_level | (long long)(t.block / 32) << 3 | (long long)(t.tile / 32) << 7 |
            (long long)t.stack << 15 | (long long)t.dynamic << 20 | (long long)t.min_blocks << 21 |
-           (long long)t.count << 25 | (long long)(t.shadow_chunk / 32) << 26;
+           (long long)t.count << 25 | (long long)(t.shadow_chunk / 32) << 26 | (long long)t.pixel_tile << 48;
 }
 
 extern "C" int rt_ctx_get_tuning(const rt_ctx *ctx, rt_batch_tuning *out)
 {
     if (!ctx || !out) return RT_ERR_INVALID;
     const Tuning &t = ctx->plain_tuning;
-    *out = rt_batch_tuning{t.block, t.tile, t.stack, 1, t.min_blocks, t.dynamic ? 1 : 2, 0, t.shadow_chunk, 0};
+    *out = rt_batch_tuning{t.block, t.tile, t.stack, 1, t.min_blocks, t.dynamic ? 1 : 2, 0, t.shadow_chunk, t.pixel_tile};
     return RT_OK;
 }
 

@@ -134,7 +134,7 @@ struct DevJob {
     float znear, zfar;            // zfar already multiplied by sqrt(2) (RayTracer.cpp:15)
     unsigned long long seed;
     int slot;                     // serving slot (per-frame ray counter), -1 = none
-    int pad;
+    int pixel_tile;               // primary rays in pixel tiles of this edge, row-major tiles (0 = rows)
 };
 
 // ray queue, structure of arrays, 64 B per ray read as four 128-bit loads

@@ -52,6 +52,27 @@ struct PrimaryRay {
     int sample;   // sample index within the pixel
 };
 
+// The pixel of sequence number p over the xlim x ylim region: row by row (tile 0), or in tiles
+// of T x T pixels taken row by row, the pixels of a tile row by row; the last band of rows and
+// the last tile of each band may be narrower. A bijection either way: it only sets which rays a
+// warp and its neighbours trace together (hit points and shadow rays follow the primary order).
+__device__ __forceinline__ void pixel_of(unsigned p, unsigned xlim, unsigned ylim, unsigned T, unsigned &row,
+                                         unsigned &col)
+{
+    if (T == 0) {
+        row = p / xlim;
+        col = p - row * xlim;
+        return;
+    }
+    const unsigned band_px = xlim * T, band = p / band_px, r = p - band * band_px;
+    const unsigned hb = min(T, ylim - band * T);       // rows in this band
+    const unsigned t = r / (T * hb), q = r - t * (T * hb);
+    const unsigned wt = min(T, xlim - t * T);          // columns in this tile
+    const unsigned ri = q / wt;
+    row = band * T + ri;
+    col = t * T + (q - ri * wt);
+}
+
 // camera ray of the job's sample `local` (pixel-major: local = pixel * spp + sample)
 __device__ __forceinline__ PrimaryRay primary_ray(const DevJob &J, long long local)
 {
@@ -70,7 +91,8 @@ __device__ __forceinline__ PrimaryRay primary_ray(const DevJob &J, long long loc
         s = (int)(local - p * J.spp);
     }
     // p < 2^28: frames are at most 16384 x 16384
-    const unsigned row = (unsigned)p / (unsigned)J.xlim, col = (unsigned)p - row * (unsigned)J.xlim;
+    unsigned row, col;
+    pixel_of((unsigned)p, (unsigned)J.xlim, (unsigned)J.ylim, (unsigned)J.pixel_tile, row, col);
     const int xcur = (int)col - J.width / 2, ycur = (int)row - J.height / 2;
     float a, b;
     DSplit d = split_double_bits((unsigned long long)__double_as_longlong(J.dp));

@@ -56,7 +56,8 @@ struct Tuning {
     bool count = false;  // count BVH nodes / triangles / spheres
     int grid = 0;        // blocks (0 = derived from the SM count)
     int min_blocks = 8;  // 0, 6 or 8: register cap of the traversal kernels (128-thread blocks)
-    int shadow_chunk = 0;   // shadow work in light-major chunks of this many hits (0 = one chunk)
+    int shadow_chunk = 4096;   // shadow work in light-major chunks of this many hits (0 = one chunk)
+    int pixel_tile = 0;     // primary rays in square pixel tiles of this edge (0 = row by row)
 };
 
 int sm_count();

@@ -273,6 +273,7 @@ static int admit(rt_server *srv)
             reject(srv, r, rc);
             continue;
         }
+        r->wj.job.pixel_tile = srv->tuning.pixel_tile;
         r->wj.scene = &sd;
         r->wj.total = samples;
         r->wj.cursor = 0;
@@ -738,6 +739,20 @@ void rt_server_destroy(rt_server *srv)
 }
 
 const char *rt_server_last_error(const rt_server *srv) { return srv ? srv->ctx->err.c_str() : "no server"; }
+
+int rt_server_set_tuning(rt_server *srv, const rt_batch_tuning *tuning)
+{
+    if (!srv) return RT_ERR_INVALID;
+    Tuning t;
+    if (tuning) {
+        int rc = tuning_from(srv->ctx, tuning, t);
+        if (rc) return rc;
+    }
+    // the plain mode renders through rt_render, which takes the context's tuning
+    if (srv->cfg.plain) return rt_ctx_set_tuning(srv->ctx, tuning);
+    srv->tuning = t;
+    return RT_OK;
+}
 
 int rt_server_add_scene(rt_server *srv, const rt_scene_desc *desc, int32_t *scene)
 {

@@ -168,20 +168,23 @@ def test_deterministic_and_order_independent(ctx):
     np.testing.assert_array_equal(a["rgb"].view(np.uint32), b["rgb"].view(np.uint32))
 
 
-TUNINGS = [(0, 0, 8), (8, 0, 8), (16, 0, 8), (8, 2048, 8), (16, 64, 6), (0, 32768, 0)]   # (stack, chunk, cap)
+# (stack entries in shared memory, shadow chunk, register cap, pixel tile)
+TUNINGS = [(0, 0, 8, 0), (8, 0, 8, 0), (16, 0, 8, 16), (8, 2048, 8, 8), (16, 64, 6, 7), (0, 32768, 0, 32),
+           (0, 4096, 8, 64)]
 
 
-@pytest.mark.parametrize("stack,chunk,cap", TUNINGS)
-def test_tuning_variants_give_the_same_image(ctx, stack, chunk, cap):
-    """Traversal stack entries in shared memory (0, 8, 16), shadow work in light-major chunks and
-    register caps change only how the work runs: every variant's frame is the default's bit for
-    bit, through the plain path and through the batch path, on a deep jittered frame with
-    refraction (long traversal stacks) and on a config-3 mesh."""
+@pytest.mark.parametrize("stack,chunk,cap,ptile", TUNINGS)
+def test_tuning_variants_give_the_same_image(ctx, stack, chunk, cap, ptile):
+    """Traversal stack entries in shared memory (0, 8, 16), shadow work in light-major chunks,
+    register caps and the pixel tiles primary rays are traced in (frames whose sides are not
+    multiples of the tile included) change only how the work runs: every variant's frame is the
+    default's bit for bit, through the plain path and through the batch path, on a deep
+    jittered frame with refraction (long traversal stacks) and on a config-3 mesh."""
     scene = rt.SceneHost.small(21, 14, 12, 96, 64, 2)
     mesh = rt.SceneHost.config(3, 4)
     want = [gpu_render(ctx, scene, 96, 64, 4, 4, 77, ref_tiles=False)[0],
             gpu_render(ctx, mesh, 128, 96, 1, 3, 0, ref_tiles=False)[0]]
-    ctx.set_tuning(rt.BatchTuning(128 if cap else 256, 32, stack, 1, cap, 1, 0, chunk))
+    ctx.set_tuning(rt.BatchTuning(128 if cap else 256, 32, stack, 1, cap, 1, 0, chunk, ptile))
     try:
         got = [gpu_render(ctx, scene, 96, 64, 4, 4, 77, ref_tiles=False)[0],
                gpu_render(ctx, mesh, 128, 96, 1, 3, 0, ref_tiles=False)[0]]
@@ -195,9 +198,11 @@ def test_tuning_variants_give_the_same_image(ctx, stack, chunk, cap):
     rds = [ctx.render_desc(96, 64, 4, 4, flags=rt.RT_FLAG_HIT_PLANES, seed=77),
            ctx.render_desc(128, 96, 1, 3, flags=rt.RT_FLAG_HIT_PLANES)]
     try:
-        ctx.batch(sids, fids, rds, tuning=rt.BatchTuning(128 if cap else 256, 64, stack, 1, cap, 1, 0, chunk))
+        ctx.batch(sids, fids, rds, tuning=rt.BatchTuning(128 if cap else 256, 64, stack, 1, cap, 1, 0, chunk, ptile))
         for f, (w, h), ref in zip(fids, [(96, 64), (128, 96)], want):
-            np.testing.assert_array_equal(ctx.download(f, w, h)["rgb"].view(np.uint32), ref["rgb"].view(np.uint32))
+            got_b = ctx.download(f, w, h)
+            np.testing.assert_array_equal(got_b["rgb"].view(np.uint32), ref["rgb"].view(np.uint32))
+            np.testing.assert_array_equal(got_b["obj"], ref["obj"])
     finally:
         for f in fids:
             ctx.release_frame(f)
