@@ -53,6 +53,15 @@ CPU_SCENES = 8                # seeded scenes of configs 3 and 4 timed on the CP
 TUNE_SCENES = 32              # config-3 scenes the autotuner times; the other 224 measure its choice
 
 
+def json_default(o):
+    """numpy scalars and arrays in the JSON line (the CPU samples carry some)."""
+    if hasattr(o, "tolist"):
+        return o.tolist()
+    if hasattr(o, "item"):
+        return o.item()
+    raise TypeError(f"{type(o).__name__} is not JSON serialisable")
+
+
 def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -227,7 +236,7 @@ def cpu_scene_sample(scenes, tiles_per_scene: int, threads: int) -> dict:
         r = port.render(sc, w, h, 1, 3, 0, ref_tiles=True, threads=threads, check=False, tiles=tiles, block=8)
         n = int(r["counts"].sum())
         frame_s = r["seconds"] * (bw * bh) / len(tiles)
-        out.append({"scene": idx, "triangles": int(sc.desc.n_tris), "resolution": f"{w}x{h}", "tiles": tiles,
+        out.append({"scene": int(idx), "triangles": int(sc.desc.n_tris), "resolution": f"{w}x{h}", "tiles": tiles,
                     "rays": n, "seconds": round(r["seconds"], 4), "mrays_per_s": round(n / r["seconds"] / 1e6, 4),
                     "frame_s_estimate": round(frame_s, 3)})
         rays += n
@@ -601,7 +610,7 @@ def run_gpu(args) -> None:
                 out["batched"]["cpu_baseline"] = {**c3, "kind": "port", "cores": cores, "sample": note}
             if "served" in out:
                 out["served"]["cpu_baseline"] = {**c4, "kind": "port", "cores": cores, "sample": note}
-    print(json.dumps(out), flush=True)
+    print(json.dumps(out, default=json_default), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
 
