@@ -166,6 +166,12 @@ typedef struct rt_render_stats {
     int32_t overflow_retries;
     float   kernel_ms[RT_KERNEL_KINDS];       /* with RT_FLAG_PROFILE: device time per kernel kind */
     int32_t kernel_launches[RT_KERNEL_KINDS]; /* kernels launched per kind (always filled) */
+    float   kernel_idle[RT_KERNEL_KINDS];     /* with RT_FLAG_PROFILE, for extend, shade and shadow:
+                                                 the share of the launches' warp time (warps x span
+                                                 from the first warp's start to the last warp's end)
+                                                 spent before a warp's block started or after the
+                                                 warp ran out of work: the SM time a kernel that
+                                                 never drains between bounces could use */
 } rt_render_stats;
 
 typedef struct rt_ctx rt_ctx;
@@ -257,13 +263,14 @@ int rt_render_host_since(rt_ctx *ctx, uint64_t cancel_mark, const rt_scene_desc 
 typedef struct rt_batch_tuning {
     int32_t block;               /* threads per block of the traversal kernels (0 = default) */
     int32_t tile;                /* rays taken per work-counter fetch (0 = default; at most 4096) */
-    int32_t stack;               /* traversal stack entries per thread kept in shared memory: 0, 8 or
-                                    16; the rest of the 96 entries that bound any path stay in local
+    int32_t stack;               /* traversal stack entries per thread kept in shared memory: 0 or 8;
+                                    the rest of the 96 entries that bound any path stay in local
                                     memory (0 = all of them) */
     int32_t use_graph;           /* capture the per-bounce launch sequence as a CUDA graph */
     int32_t min_blocks;          /* 0, 6 or 8: resident 128-thread blocks per SM the register budget
                                     of the traversal kernels must allow (0 = compiler's) */
-    int32_t dynamic;             /* 0 or 1: pull ray tiles from a counter; 2: static grid stride */
+    int32_t dynamic;             /* 0 or 1: pull ray tiles from a counter; 2: static grid stride;
+                                    3: each SM first drains its own contiguous share of the rays */
     int64_t wave_rays;           /* batch: ray-queue entries of one wave (0 = 2^26) */
     int32_t shadow_chunk;        /* shadow rays light-major within chunks of this many hits, a
                                     multiple of 32 (0 = all of a bounce's hits in one chunk; the
@@ -284,8 +291,8 @@ int rt_batch_render(rt_ctx *ctx, int32_t n, const int32_t *scene_ids, const int3
 int rt_batch_render_plain(rt_ctx *ctx, int32_t n, const int32_t *scene_ids,
                           const int32_t *frame_ids, const rt_render_desc *rds);
 /* pick block size, register cap and ray tile (or the static stride) for these jobs by timing
- * candidates, then the short-stack depth in shared memory, the pixel tile, the shadow chunk
- * and the wave size.
+ * candidates, then per-SM shares of the rays, the short-stack depth in shared memory, the
+ * pixel tile, the shadow chunk and the wave size.
  * Writes the choice. */
 int rt_batch_autotune(rt_ctx *ctx, int32_t n, const int32_t *scene_ids, const int32_t *frame_ids,
                       const rt_render_desc *rds, rt_batch_tuning *out);

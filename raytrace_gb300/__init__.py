@@ -76,7 +76,7 @@ class RenderStats(C.Structure):
                 ("nodes_visited", C.c_int64), ("tris_tested", C.c_int64), ("spheres_tested", C.c_int64),
                 ("shadow_nodes_visited", C.c_int64), ("shadow_tris_tested", C.c_int64),
                 ("shadow_spheres_tested", C.c_int64), ("ms", C.c_float), ("overflow_retries", C.c_int32),
-                ("kernel_ms", C.c_float * 6), ("kernel_launches", C.c_int32 * 6)]
+                ("kernel_ms", C.c_float * 6), ("kernel_launches", C.c_int32 * 6), ("kernel_idle", C.c_float * 6)]
 
     def total_rays(self) -> int:
         return int(self.rays_primary + self.rays_secondary + self.rays_shadow)
@@ -85,6 +85,7 @@ class RenderStats(C.Structure):
         d = {k: getattr(self, k) for k, _ in self._fields_}
         d["kernel_ms"] = dict(zip(KERNEL_KINDS, list(self.kernel_ms)))
         d["kernel_launches"] = dict(zip(KERNEL_KINDS, list(self.kernel_launches)))
+        d["kernel_idle"] = dict(zip(KERNEL_KINDS, list(self.kernel_idle)))
         return d
 
 

@@ -41,7 +41,7 @@ def main(argv: list[str] | None = None) -> int:
     ap.add_argument("--level", type=int, default=-1)
     ap.add_argument("--repeat", type=int, default=1)
     ap.add_argument("--ref-tiles", action="store_true", help="only the reference's 64x64-tile region")
-    ap.add_argument("--stack", type=int, default=-1, help="traversal stack entries in shared memory: 0, 8, 16")
+    ap.add_argument("--stack", type=int, default=-1, help="traversal stack entries in shared memory: 0 or 8")
     ap.add_argument("--chunk", type=int, default=-1, help="shadow rays light-major in chunks of this many hits")
     ap.add_argument("--out", default="")
     ap.add_argument("--pfm", default="")

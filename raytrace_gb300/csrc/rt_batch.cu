@@ -124,7 +124,7 @@ static int wave_graph(rt_ctx *ctx, WaveRunner &R, int max_level, const Tuning &t
     CK(ctx, cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
     cudaGraph_t g;
     cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
-    cudaMemsetAsync(R.ws.wf.C, 0, sizeof(Counters), cap);
+    cudaMemsetAsync(R.ws.wf.C, 0, kCounterBlockBytes, cap);
     enqueue_levels(ctx, R.ws, max_level, t, cap, nullptr);
     cudaError_t e = cudaStreamEndCapture(cap, &g);
     cudaStreamDestroy(cap);
@@ -194,7 +194,7 @@ int wave_enqueue(rt_ctx *ctx, WaveRunner &R, const std::vector<WaveJob *> &jobs,
         if (rc) return rc;
         CK(ctx, cudaGraphLaunch(exec, s));
     } else {
-        CK(ctx, cudaMemsetAsync(ws.wf.C, 0, sizeof(Counters), s));
+        CK(ctx, cudaMemsetAsync(ws.wf.C, 0, kCounterBlockBytes, s));
         enqueue_levels(ctx, ws, max_level, t, s, prof);
     }
     CK(ctx, cudaMemcpyAsync(st.counters, ws.wf.C, sizeof(Counters), cudaMemcpyDeviceToHost, s));
@@ -258,6 +258,7 @@ static int batch_core(rt_ctx *ctx, int32_t n, const int32_t *scene_ids, const in
     if (rc) return rc;
     R.rays_primary = R.rays_secondary = R.rays_shadow = 0;
     R.overflow = R.error = 0;
+    ctx->stamped = false;   // warp stamps belong to profiled plain renders only
     R.wave_ms.clear();
     R.wait_s = 0.0;
     // the frame table; its pinned host copy is rewritten once the previous copy out of it ran
@@ -352,13 +353,13 @@ extern "C" int rt_batch_autotune(rt_ctx *ctx, int32_t n, const int32_t *scene_id
     if (!ctx || !out) return RT_ERR_INVALID;
     // Coordinate search, each candidate timed as the best of three batches after a warm one
     // (which captures its graph): (threads per block, register cap as resident blocks per SM) x
-    // rays per tile fetch (0 = the static grid stride), then the traversal stack entries kept in
-    // shared memory, then the primary rays' pixel tile, then the shadow work chunk, then the wave
-    // size. The caller picks the jobs:
-    // tuning on a sample of the workload and measuring on the rest keeps the choice honest.
+    // rays per tile fetch (0 = the static grid stride), then per-SM shares of the rays, then the
+    // traversal stack entries kept in shared memory, then the primary rays' pixel tile, then the
+    // shadow work chunk, then the wave size. The caller picks the jobs: tuning on a sample of the
+    // workload and measuring on the rest keeps the choice honest.
     const int shapes[][2] = {{128, 8}, {128, 6}, {64, 8}, {256, 0}};
     const int tiles[] = {0, 32, 64, 128, 256};
-    const int stacks[] = {0, 8, 16};
+    const int stacks[] = {0, 8};
     const int chunks[] = {0, 1024, 4096, 16384};
     const int pixel_tiles[] = {0, 8, 16, 32};
     const long long waves[] = {1ll << 25, 1ll << 27};   // the default is 2^26
@@ -383,6 +384,12 @@ extern "C" int rt_batch_autotune(rt_ctx *ctx, int32_t n, const int32_t *scene_id
             int rc = trial(rt_batch_tuning{sh[0], tl ? tl : 32, 0, 1, sh[1], tl ? 1 : 2, 0, 4096, 0});
             if (rc) return rc;
         }
+    if (best_t.dynamic == 1) {   // the tiles of each SM's own share of the rays first
+        rt_batch_tuning t = best_t;
+        t.dynamic = 3;
+        int rc = trial(t);
+        if (rc) return rc;
+    }
     for (int ss : stacks) {
         if (ss == best_t.stack) continue;
         rt_batch_tuning t = best_t;

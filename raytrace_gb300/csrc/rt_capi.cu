@@ -779,7 +779,7 @@ int ws_ensure(rt_ctx *ctx, Workspace &ws, long long qcap, int njobs)
     for (int j = 0; j < 5; ++j) os[j] = take(16 * q);
     size_t oh[5];
     for (int j = 0; j < 5; ++j) oh[j] = take(16 * q);
-    const size_t o_nob = take(4 * q), o_ctr = take(sizeof(Counters)),
+    const size_t o_nob = take(4 * q), o_ctr = take(kCounterBlockBytes),
                  o_jobs = take(sizeof(DevJob) * (size_t)njobs), o_end = take(8 * (size_t)njobs), o_tot = take(32),
                  o_scn = take(sizeof(DevScene) * (size_t)njobs);
     CK(ctx, ws.mem.ensure(off));
@@ -804,6 +804,7 @@ int ws_ensure(rt_ctx *ctx, Workspace &ws, long long qcap, int njobs)
     ws.wf.hq.h = (float4 *)(b + oh[4]);
     ws.wf.hq.nob = (int *)(b + o_nob);
     ws.wf.C = (Counters *)(b + o_ctr);
+    ws.wf.shares = (int *)(b + o_ctr + ((sizeof(Counters) + 255) / 256) * 256);
     ws.jobs = (DevJob *)(b + o_jobs);
     ws.job_end = (long long *)(b + o_end);
     ws.scalars = (long long *)(b + o_tot);
@@ -917,7 +918,7 @@ static int plain_graph(rt_ctx *ctx, int max_level, const Tuning &t, cudaGraphExe
     CK(ctx, cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
     cudaGraph_t g;
     cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
-    cudaMemsetAsync(ws.wf.C, 0, sizeof(Counters), cap);
+    cudaMemsetAsync(ws.wf.C, 0, kCounterBlockBytes, cap);
     enqueue_levels(ctx, ws, max_level, t, cap, nullptr);
     cudaError_t e = cudaStreamEndCapture(cap, &g);
     cudaStreamDestroy(cap);
@@ -970,9 +971,15 @@ static int render_once(rt_ctx *ctx, SceneDev &sc, FrameDev &f, const rt_render_d
     P.end(s);
     Tuning t = ctx->plain_tuning;
     t.count = (rd->flags & RT_FLAG_COUNT_WORK) != 0;
-    if (profile) {   // kernels one by one between events
-        CK(ctx, cudaMemsetAsync(ws.wf.C, 0, sizeof(Counters), s));
+    ctx->stamped = false;
+    if (profile) {   // kernels one by one between events, warps stamping their start and end
+        CK(ctx, cudaMemsetAsync(ws.wf.C, 0, kCounterBlockBytes, s));
+        CK(ctx, ctx->stamps.ensure(kStampBytes));
+        CK(ctx, cudaMemsetAsync(ctx->stamps.p, 0, kStampBytes, s));
+        ws.wf.stamps = (unsigned long long *)ctx->stamps.p;
         enqueue_levels(ctx, ws, rd->max_level, t, s, &P);
+        ws.wf.stamps = nullptr;   // launches copied their parameters; captured graphs never stamp
+        ctx->stamped = true;
     } else {
         cudaGraphExec_t exec = nullptr;
         rc = plain_graph(ctx, rd->max_level, t, exec);
@@ -1012,6 +1019,36 @@ extern "C" int rt_render(rt_ctx *ctx, int32_t scene_id, int32_t frame_id, const 
     return render_since(ctx, ctx->cancel_count.load(), scene_id, frame_id, rd);
 }
 
+// From the warp stamps of a profiled render: per kernel kind, the share of its launches' warp
+// time (warps x launch span) spent before a warp's block started or after the warp ran out of
+// work. A warp that never ran has no stamps and does not count.
+static int idle_shares(rt_ctx *ctx, float *idle)
+{
+    std::vector<unsigned long long> st(kStampBytes / sizeof(unsigned long long));
+    CK(ctx, cudaMemcpy(st.data(), ctx->stamps.p, kStampBytes, cudaMemcpyDeviceToHost));
+    double wasted[3] = {0, 0, 0}, total[3] = {0, 0, 0};
+    for (int slot = 0; slot < 15; ++slot) {
+        const unsigned long long *p = st.data() + 2ull * slot * kMaxStampWarps;
+        unsigned long long t0 = ~0ull, t1 = 0;
+        long long warps = 0;
+        for (int w = 0; w < kMaxStampWarps; ++w) {
+            if (!p[2 * w + 1]) continue;
+            t0 = std::min(t0, ~p[2 * w]);
+            t1 = std::max(t1, p[2 * w + 1]);
+            ++warps;
+        }
+        if (!warps || t1 <= t0) continue;
+        double w_idle = 0;
+        for (int w = 0; w < kMaxStampWarps; ++w)
+            if (p[2 * w + 1]) w_idle += (double)((~p[2 * w]) - t0) + (double)(t1 - p[2 * w + 1]);
+        wasted[slot % 3] += w_idle;
+        total[slot % 3] += (double)warps * (double)(t1 - t0);
+    }
+    const int kind[3] = {RT_KERNEL_EXTEND, RT_KERNEL_SHADE, RT_KERNEL_SHADOW};
+    for (int k = 0; k < 3; ++k) idle[kind[k]] = total[k] > 0 ? (float)(wasted[k] / total[k]) : 0.0f;
+    return RT_OK;
+}
+
 extern "C" int rt_render_wait(rt_ctx *ctx, rt_render_stats *stats)
 {
     if (!ctx) return RT_ERR_INVALID;
@@ -1047,7 +1084,11 @@ extern "C" int rt_render_wait(rt_ctx *ctx, rt_render_stats *stats)
         stats->ms = ms;
         stats->overflow_retries = retries;
         ctx->prof.collect(stats->kernel_ms);
-        for (int k = 0; k < RT_KERNEL_KINDS; ++k) stats->kernel_launches[k] = ctx->prof.launches[k];
+        for (int k = 0; k < RT_KERNEL_KINDS; ++k) stats->kernel_launches[k] = ctx->prof.launches[k], stats->kernel_idle[k] = 0;
+        if (ctx->stamped) {
+            int rc = idle_shares(ctx, stats->kernel_idle);
+            if (rc) return rc;
+        }
     }
     ctx->pending.active = false;
     if (was_cancelled) return ctx_fail(ctx, RT_ERR_CANCELLED, "render cancelled");
@@ -1066,15 +1107,16 @@ int tuning_from(rt_ctx *ctx, const rt_batch_tuning *in, Tuning &t)
     t.min_blocks = in->min_blocks;
     t.shadow_chunk = in->shadow_chunk;
     t.pixel_tile = in->pixel_tile;
-    if (in->dynamic < 0 || in->dynamic > 2) return ctx_fail(ctx, RT_ERR_INVALID, "dynamic %d: use 0, 1 or 2", in->dynamic);
+    if (in->dynamic < 0 || in->dynamic > 3) return ctx_fail(ctx, RT_ERR_INVALID, "dynamic %d: use 0..3", in->dynamic);
     t.dynamic = in->dynamic != 2;
+    t.shares = in->dynamic == 3;
     if (t.block % 32 || t.block < 32 || t.block > 256 || t.tile % 32 || t.tile <= 0 || t.tile > 4096)
         return ctx_fail(ctx, RT_ERR_INVALID, "tuning block %d / tile %d not supported", t.block, t.tile);
     if (t.min_blocks != 0 && t.min_blocks != 6 && t.min_blocks != 8)
         return ctx_fail(ctx, RT_ERR_INVALID, "min_blocks %d: use 0, 6 or 8", t.min_blocks);
     if (t.min_blocks && t.block > 128) return ctx_fail(ctx, RT_ERR_INVALID, "min_blocks needs blocks of at most 128 threads");
-    if (t.stack != 0 && t.stack != 8 && t.stack != 16)
-        return ctx_fail(ctx, RT_ERR_INVALID, "stack %d: use 0, 8 or 16 shared-memory entries", t.stack);
+    if (t.stack != 0 && t.stack != 8)
+        return ctx_fail(ctx, RT_ERR_INVALID, "stack %d: use 0 or 8 shared-memory entries", t.stack);
     if (t.shadow_chunk < 0 || t.shadow_chunk % 32 || t.shadow_chunk > (1 << 27))
         return ctx_fail(ctx, RT_ERR_INVALID, "shadow_chunk %d: a multiple of 32 in [0, 2^27]", t.shadow_chunk);
     if (t.pixel_tile < 0 || t.pixel_tile == 1 || t.pixel_tile > 64)
@@ -1087,14 +1129,16 @@ long long tuning_key(int max_level, const Tuning &t)
 {
     return (long long)max_level | (long long)(t.block / 32) << 3 | (long long)(t.tile / 32) << 7 |
            (long long)t.stack << 15 | (long long)t.dynamic << 20 | (long long)t.min_blocks << 21 |
-           (long long)t.count << 25 | (long long)(t.shadow_chunk / 32) << 26 | (long long)t.pixel_tile << 48;
+           (long long)t.count << 25 | (long long)(t.shadow_chunk / 32) << 26 | (long long)t.pixel_tile << 48 |
+           (long long)t.shares << 56;
 }
 
 extern "C" int rt_ctx_get_tuning(const rt_ctx *ctx, rt_batch_tuning *out)
 {
     if (!ctx || !out) return RT_ERR_INVALID;
     const Tuning &t = ctx->plain_tuning;
-    *out = rt_batch_tuning{t.block, t.tile, t.stack, 1, t.min_blocks, t.dynamic ? 1 : 2, 0, t.shadow_chunk, t.pixel_tile};
+    *out = rt_batch_tuning{t.block, t.tile, t.stack, 1, t.min_blocks, t.dynamic ? (t.shares ? 3 : 1) : 2, 0,
+                           t.shadow_chunk, t.pixel_tile};
     return RT_OK;
 }
 

@@ -215,6 +215,8 @@ struct rt_ctx {
     int next_scene = 0, next_frame = 0;
     Workspace ws;
     DevBuf lbvh_scratch;
+    DevBuf stamps;                       // warp time stamps of a profiled render (kStampBytes)
+    bool stamped = false;                // the last render wrote them
     // Cancel: rt_cancel counts its calls; a render (or rt_render_host_since call) is cancelled
     // once the count passes the mark it began from. The mutex orders rt_cancel's write of the
     // device flag against the clear a new render makes, so no cancel made after a render's mark

@@ -126,8 +126,9 @@ __device__ __forceinline__ PrimaryRay primary_ray(const DevJob &J, long long loc
 // ---- extend: closest hit -------------------------------------------------------------------
 // MINB > 0 caps registers so MINB blocks of 128 threads fit on an SM. GEN: the first pass of a
 // wave, which makes its primary rays instead of reading a queue. SS: traversal stack entries per
-// thread in shared memory (SS * blockDim.x ints of dynamic shared memory).
-template <int SS, bool DYN, bool COUNT, int MINB, bool GEN>
+// thread in shared memory (SS * blockDim.x ints of dynamic shared memory). MODE: how warps share
+// the rays (kWork*).
+template <int SS, int MODE, bool COUNT, int MINB, bool GEN>
 __global__ void __launch_bounds__(MINB ? 128 : 256, MINB ? MINB : 1) k_extend(Wavefront wf, int sel, int wslot, int tile)
 {
     Counters *C = wf.C;
@@ -145,13 +146,14 @@ __global__ void __launch_bounds__(MINB ? 128 : 256, MINB ? MINB : 1) k_extend(Wa
         }
     }
     if (cancelled(wf.cancel)) return;
+    stamp_start(wf.stamps, wslot);
     const int n = GEN ? (int)min(total, (long long)q.capacity) : min(C->q_count[sel], q.capacity);
     WorkCount wc{0, 0, 0, 0};
     const int level = wslot / 3;
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
     const HitQueue hq = wf.hq;
-    for_each_ray<DYN>(n, &C->work[wslot], tile, [&](int i, bool active) {
+    for_each_ray<MODE>(n, &C->work[wslot], wf.shares + wslot * kMaxShares, tile, [&](int i, bool active) {
         Best best;
         best.key = -1;
         int newobj = -1, job = 0, pixel = 0, plane = 0;
@@ -200,6 +202,7 @@ __global__ void __launch_bounds__(MINB ? 128 : 256, MINB ? MINB : 1) k_extend(Wa
             }
         }
     });
+    stamp_end(wf.stamps, wslot);
     if (wc.err) atomicOr(&C->error, wc.err);
     if (COUNT) {
         for (int off = 16; off > 0; off >>= 1) {
@@ -215,13 +218,13 @@ __global__ void __launch_bounds__(MINB ? 128 : 256, MINB ? MINB : 1) k_extend(Wa
     }
 }
 
-template <int SS, bool DYN, bool CNT, bool GEN>
+template <int SS, int MODE, bool CNT, bool GEN>
 static void extend_launch(const Wavefront &wf, int sel, int wslot, const Tuning &t, cudaStream_t s)
 {
     const size_t smem = stack_smem(SS, t.block);
 #define RT_EXT(MB)                                                                                                \
     {                                                                                                             \
-        auto k = k_extend<SS, DYN, CNT, MB, GEN>;                                                                 \
+        auto k = k_extend<SS, MODE, CNT, MB, GEN>;                                                                \
         k<<<grid_for(t, (const void *)k, smem), t.block, smem, s>>>(wf, sel, wslot, t.tile);                     \
     }
     if constexpr (CNT) RT_EXT(8)
@@ -229,29 +232,27 @@ static void extend_launch(const Wavefront &wf, int sel, int wslot, const Tuning 
 #undef RT_EXT
 }
 
-template <bool DYN, bool CNT, bool GEN>
+template <int MODE, bool CNT, bool GEN>
 static void extend_stack(const Wavefront &wf, int sel, int wslot, const Tuning &t, cudaStream_t s)
 {
-    if constexpr (CNT) extend_launch<0, DYN, CNT, GEN>(wf, sel, wslot, t, s);
-    else if (t.stack == 16) extend_launch<16, DYN, CNT, GEN>(wf, sel, wslot, t, s);
-    else if (t.stack == 8) extend_launch<8, DYN, CNT, GEN>(wf, sel, wslot, t, s);
-    else extend_launch<0, DYN, CNT, GEN>(wf, sel, wslot, t, s);
+    if (!CNT && t.stack == 8) extend_launch<8, MODE, CNT, GEN>(wf, sel, wslot, t, s);
+    else extend_launch<0, MODE, CNT, GEN>(wf, sel, wslot, t, s);
+}
+
+template <bool GEN>
+static void extend_mode(const Wavefront &wf, int sel, int wslot, const Tuning &t, cudaStream_t s)
+{
+    if (t.count) extend_stack<kWorkDynamic, true, GEN>(wf, sel, wslot, count_tuning(t), s);
+    else if (!t.dynamic) extend_stack<kWorkStatic, false, GEN>(wf, sel, wslot, t, s);
+    else if (t.shares) extend_stack<kWorkShares, false, GEN>(wf, sel, wslot, t, s);
+    else extend_stack<kWorkDynamic, false, GEN>(wf, sel, wslot, t, s);
 }
 
 void launch_extend(const Wavefront &wf, int sel, int level, bool gen, const Tuning &t, cudaStream_t s)
 {
     const int wslot = 3 * level;
-    if (t.count) {
-        const Tuning c = count_tuning(t);
-        if (gen) extend_stack<true, true, true>(wf, sel, wslot, c, s);
-        else extend_stack<true, true, false>(wf, sel, wslot, c, s);
-    } else if (t.dynamic) {
-        if (gen) extend_stack<true, false, true>(wf, sel, wslot, t, s);
-        else extend_stack<true, false, false>(wf, sel, wslot, t, s);
-    } else {
-        if (gen) extend_stack<false, false, true>(wf, sel, wslot, t, s);
-        else extend_stack<false, false, false>(wf, sel, wslot, t, s);
-    }
+    if (gen) extend_mode<true>(wf, sel, wslot, t, s);
+    else extend_mode<false>(wf, sel, wslot, t, s);
 }
 
 } // namespace rtg

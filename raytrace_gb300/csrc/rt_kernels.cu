@@ -92,6 +92,7 @@ template <bool DYN>
 __global__ void __launch_bounds__(128, 5) k_shade(Wavefront wf, int sel, int wslot)
 {
     if (cancelled(wf.cancel)) return;
+    stamp_start(wf.stamps, wslot);
     Counters *C = wf.C;
     const RayQueue q = wf.q[sel], qo = wf.q[sel ^ 1];
     const HitQueue hq = wf.hq;
@@ -328,6 +329,7 @@ __global__ void __launch_bounds__(128, 5) k_shade(Wavefront wf, int sel, int wsl
             }
         }
     });
+    stamp_end(wf.stamps, wslot);
 }
 
 // ---- resolve: fixed point -> float rgb and Color::put bytes ---------------------------------------
@@ -501,7 +503,7 @@ int grid_for(const Tuning &t, const void *kernel, size_t smem)
 Tuning count_tuning(const Tuning &t)
 {
     Tuning c = t;
-    c.block = 128, c.dynamic = true, c.min_blocks = 8;
+    c.block = 128, c.dynamic = true, c.shares = false, c.min_blocks = 8, c.stack = 0;
     return c;
 }
 

@@ -44,15 +44,28 @@ struct Wavefront {
     ShadowQueue sq;
     HitQueue hq;                      // the rays that hit, densely, per bounce (C->h_count)
     Counters *C;
+    int *shares;                      // per work slot, kMaxShares counters of the SM-share mode
+    unsigned long long *stamps;       // RT_FLAG_PROFILE: per work slot and warp, (~start, end) in
+                                      // globaltimer ns, combined with atomicMax (NULL = not kept)
     const volatile int *cancel;       // device cancel flag (NULL = not cancellable)
 };
+
+// warp time stamps of a profiled render: 16 work slots x kMaxStampWarps warps x 2
+constexpr int kMaxStampWarps = 16384;
+constexpr size_t kStampBytes = 16ull * kMaxStampWarps * 2 * sizeof(unsigned long long);
+
+// SM-share work counters: 16 work slots (as Counters::work) x kMaxShares shares, right after the
+// Counters in the workspace and zeroed with them
+constexpr int kMaxShares = 512;
+constexpr size_t kCounterBlockBytes = ((sizeof(Counters) + 255) / 256) * 256 + 16 * kMaxShares * sizeof(int);
 
 struct Tuning {
     int block = 128;     // threads per block of the traversal kernels
     int tile = 32;       // rays per dynamic work fetch (multiple of 32)
-    int stack = 0;       // traversal stack entries kept in shared memory per thread: 0, 8 or 16
+    int stack = 0;       // traversal stack entries kept in shared memory per thread: 0 or 8
                          // (the rest of the kStack entries in local memory)
     bool dynamic = true; // persistent grid pulling tiles from a global counter
+    bool shares = false; // with dynamic: each SM first drains its own share of the rays
     bool count = false;  // count BVH nodes / triangles / spheres
     int grid = 0;        // blocks (0 = derived from the SM count)
     int min_blocks = 8;  // 0, 6 or 8: register cap of the traversal kernels (128-thread blocks)

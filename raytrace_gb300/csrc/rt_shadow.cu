@@ -10,10 +10,11 @@ namespace rtg {
 // in one chunk): neighbouring threads aim at the same light from neighbouring hit points, so
 // their traversals stay coherent, and a chunk's lights are traced close together in time, so the
 // nodes its rays share stay in L2 between the lights.
-template <int SS, bool DYN, bool COUNT, int MINB>
+template <int SS, int MODE, bool COUNT, int MINB>
 __global__ void __launch_bounds__(MINB ? 128 : 256, MINB ? MINB : 1) k_shadow(Wavefront wf, int wslot, int tile, int chunk)
 {
     if (cancelled(wf.cancel)) return;
+    stamp_start(wf.stamps, wslot);
     Counters *C = wf.C;
     const ShadowQueue sq = wf.sq;
     // slot i holds the shadow record of hit i of this bounce, or is empty (job -1)
@@ -22,7 +23,7 @@ __global__ void __launch_bounds__(MINB ? 128 : 256, MINB ? MINB : 1) k_shadow(Wa
     WorkCount wc{0, 0, 0, 0};
     unsigned long long rays = 0;
     const int cs = chunk > 0 && chunk < n ? chunk : n;   // hits per chunk
-    for_each_ray<DYN>(n * nl, &C->work[wslot], tile, [&](int w, bool active) {
+    for_each_ray<MODE>(n * nl, &C->work[wslot], wf.shares + wslot * kMaxShares, tile, [&](int w, bool active) {
         if (!active) return;
         // chunk q holds hits [q*cs, q*cs + m), m = cs except for a shorter last chunk, as m*nl
         // items: light l of hit q*cs + r is item q*cs*nl + l*m + r
@@ -55,6 +56,7 @@ __global__ void __launch_bounds__(MINB ? 128 : 256, MINB ? MINB : 1) k_shadow(Wa
         if (nn > 0) sum = vadd(sum, vmul(Ws, vscale(vmul(mk(M.ks[0], M.ks[1], M.ks[2]), ls), powf(nn, M.shininess))));
         acc_add(J.acc, __float_as_int(p4.w), sum);
     });
+    stamp_end(wf.stamps, wslot);
     if (wc.err) atomicOr(&C->error, wc.err);
     for (int off = 16; off > 0; off >>= 1) rays += __shfl_down_sync(kFull, rays, off);
     if ((threadIdx.x & 31) == 0 && rays) atomicAdd(&C->rays_shadow, rays);
@@ -72,13 +74,13 @@ __global__ void __launch_bounds__(MINB ? 128 : 256, MINB ? MINB : 1) k_shadow(Wa
     }
 }
 
-template <int SS, bool DYN, bool CNT>
+template <int SS, int MODE, bool CNT>
 static void shadow_launch(const Wavefront &wf, int wslot, const Tuning &t, cudaStream_t s)
 {
     const size_t smem = stack_smem(SS, t.block);
 #define RT_SHD(MB)                                                                                                \
     {                                                                                                             \
-        auto k = k_shadow<SS, DYN, CNT, MB>;                                                                      \
+        auto k = k_shadow<SS, MODE, CNT, MB>;                                                                     \
         k<<<grid_for(t, (const void *)k, smem), t.block, smem, s>>>(wf, wslot, t.tile, t.shadow_chunk);          \
     }
     if constexpr (CNT) RT_SHD(8)
@@ -86,21 +88,20 @@ static void shadow_launch(const Wavefront &wf, int wslot, const Tuning &t, cudaS
 #undef RT_SHD
 }
 
-template <bool DYN, bool CNT>
+template <int MODE, bool CNT>
 static void shadow_stack(const Wavefront &wf, int wslot, const Tuning &t, cudaStream_t s)
 {
-    if constexpr (CNT) shadow_launch<0, DYN, CNT>(wf, wslot, t, s);
-    else if (t.stack == 16) shadow_launch<16, DYN, CNT>(wf, wslot, t, s);
-    else if (t.stack == 8) shadow_launch<8, DYN, CNT>(wf, wslot, t, s);
-    else shadow_launch<0, DYN, CNT>(wf, wslot, t, s);
+    if (!CNT && t.stack == 8) shadow_launch<8, MODE, CNT>(wf, wslot, t, s);
+    else shadow_launch<0, MODE, CNT>(wf, wslot, t, s);
 }
 
 void launch_shadow(const Wavefront &wf, int level, const Tuning &t, cudaStream_t s)
 {
     const int wslot = 3 * level + 2;
-    if (t.count) shadow_stack<true, true>(wf, wslot, count_tuning(t), s);
-    else if (t.dynamic) shadow_stack<true, false>(wf, wslot, t, s);
-    else shadow_stack<false, false>(wf, wslot, t, s);
+    if (t.count) shadow_stack<kWorkDynamic, true>(wf, wslot, count_tuning(t), s);
+    else if (!t.dynamic) shadow_stack<kWorkStatic, false>(wf, wslot, t, s);
+    else if (t.shares) shadow_stack<kWorkShares, false>(wf, wslot, t, s);
+    else shadow_stack<kWorkDynamic, false>(wf, wslot, t, s);
 }
 
 } // namespace rtg

@@ -18,22 +18,104 @@ __device__ __forceinline__ void acc_add(long long *acc, int pix, V3 c)
     if (c.z != 0.0f && c.z == c.z) atomicAdd(a + 2, (unsigned long long)float_to_fix32(c.z));
 }
 
-// Warp-uniform loops over the rays [0, n).
+// Warp time stamps of a profiled render (wf.stamps), taken by each warp's first lane when its
+// block starts and when the warp runs out of work; (~start, end) so both combine by max
+__device__ __forceinline__ unsigned long long global_ns()
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+__device__ __forceinline__ unsigned long long *warp_stamp(unsigned long long *stamps, int wslot)
+{
+    const unsigned w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (!stamps || (threadIdx.x & 31) != 0 || w >= (unsigned)kMaxStampWarps) return nullptr;
+    return stamps + 2 * ((size_t)wslot * kMaxStampWarps + w);
+}
+__device__ __forceinline__ void stamp_start(unsigned long long *stamps, int wslot)
+{
+    if (unsigned long long *p = warp_stamp(stamps, wslot)) atomicMax(p, ~global_ns());
+}
+__device__ __forceinline__ void stamp_end(unsigned long long *stamps, int wslot)
+{
+    if (unsigned long long *p = warp_stamp(stamps, wslot)) atomicMax(p + 1, global_ns());
+}
+
+// Warp-uniform loops over the rays [0, n). MODE picks how warps share them:
 //
-// for_each_ray: each warp first takes its own 32 rays (no atomics: a launch with at most
-// 32 x warps rays touches no counter), then the rest by grid stride (DYN false) or in `tile`-ray
-// tiles pulled from a counter (DYN true) — fine-grained, for traversal, whose cost per ray
-// varies by orders of magnitude.
-template <bool DYN, class F>
-__device__ __forceinline__ void for_each_ray(int n, int *work, int tile, F &&body)
+//   kWorkStatic  each warp first takes its own 32 rays (no atomics: a launch with at most
+//                32 x warps rays touches no counter), then the rest by grid stride;
+//   kWorkDynamic the same first 32 rays, then `tile`-ray tiles pulled from one counter —
+//                fine-grained, for traversal, whose cost per ray varies by orders of magnitude;
+//   kWorkShares  three quarters of the rays are cut into one contiguous share per SM (SM id
+//                from %smid), which that SM's warps drain in tiles from the share's counter, so
+//                the rays an SM holds at once are neighbours in the queue (neighbouring pixels,
+//                hit points, shadow rays toward one light) and share node lines in its L1; then
+//                tiles of the last quarter from one counter; then, 32 shares checked per step,
+//                tiles of any share another SM has not finished (an SM that ran no block of the
+//                launch, or a slow one). Every ray is traced once whatever the block placement.
+constexpr int kWorkStatic = 0, kWorkDynamic = 1, kWorkShares = 2;
+
+template <int MODE, class F>
+__device__ __forceinline__ void for_each_ray(int n, int *work, int *shares, int tile, F &&body)
 {
     const int lane = threadIdx.x & 31;
+    auto run_tile = [&](int start, int end) {
+        for (int base = start; base < end; base += 32) body(base + lane, base + lane < end);
+    };
+    if constexpr (MODE == kWorkShares) {
+        unsigned smid, nsmid;
+        asm volatile("mov.u32 %0, %%smid;" : "=r"(smid));
+        asm volatile("mov.u32 %0, %%nsmid;" : "=r"(nsmid));
+        const unsigned P = min(max(nsmid, 1u), (unsigned)kMaxShares);
+        // rays in the shares (a multiple of 32, as every share's start); [m, n) is the common pool
+        const long long m = ((long long)n * 3 / 4) & ~31ll;
+        auto lo = [&](unsigned p) { return (int)((m * (long long)p / (long long)P) & ~31ll); };
+        // 1. this SM's share
+        {
+            const unsigned me = smid % P;
+            const int a = lo(me), b = lo(me + 1);
+            while (true) {
+                int s = 0;
+                if (lane == 0) s = atomicAdd(&shares[me], tile);
+                s = a + __shfl_sync(kFull, s, 0);
+                if (s >= b) break;
+                run_tile(s, min(s + tile, b));
+            }
+        }
+        // 2. the common pool
+        while (true) {
+            int s = 0;
+            if (lane == 0) s = atomicAdd(work, tile);
+            s = (int)m + __shfl_sync(kFull, s, 0);
+            if (s >= n) break;
+            run_tile(s, min(s + tile, n));
+        }
+        // 3. what is left of other shares. Each round either traces a tile or moves a share's
+        // counter past its end, so the loop ends; the bound is a guard only.
+        for (unsigned base = 0; base < P; base += 32) {
+            for (int guard = 0; guard < (1 << 26); ++guard) {
+                const unsigned p = base + (unsigned)lane;
+                // the counters are read at L2, where the atomics are made
+                const bool left = p < P && __ldcg(&shares[p]) < lo(p + 1) - lo(p);
+                const unsigned ball = __ballot_sync(kFull, left);
+                if (!ball) break;
+                const unsigned q = base + (unsigned)(__ffs(ball) - 1);
+                int s = 0;
+                if (lane == 0) s = atomicAdd(&shares[q], tile);
+                s = lo(q) + __shfl_sync(kFull, s, 0);
+                const int b = lo(q + 1);
+                if (s < b) run_tile(s, min(s + tile, b));
+            }
+        }
+        return;
+    }
     const int nw = gridDim.x * (blockDim.x >> 5);
     const int w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     const int first = min(n, nw * 32);   // the static prefix
     if (w * 32 < first) body(w * 32 + lane, w * 32 + lane < first);
     if (first >= n) return;
-    if (!DYN) {
+    if constexpr (MODE == kWorkStatic) {
         for (long long base = (long long)first + (long long)w * 32; base < n; base += (long long)nw * 32)
             body((int)(base + lane), base + lane < n);
     } else {
@@ -42,9 +124,7 @@ __device__ __forceinline__ void for_each_ray(int n, int *work, int tile, F &&bod
             if (lane == 0) start = atomicAdd(work, tile);
             start = first + __shfl_sync(kFull, start, 0);
             if (start >= n) break;
-            const int end = min(start + tile, n);
-            for (int base = start; base < end; base += 32)
-                body(base + lane, base + lane < end);
+            run_tile(start, min(start + tile, n));
         }
     }
 }

@@ -168,23 +168,26 @@ def test_deterministic_and_order_independent(ctx):
     np.testing.assert_array_equal(a["rgb"].view(np.uint32), b["rgb"].view(np.uint32))
 
 
-# (stack entries in shared memory, shadow chunk, register cap, pixel tile)
-TUNINGS = [(0, 0, 8, 0), (8, 0, 8, 0), (16, 0, 8, 16), (8, 2048, 8, 8), (16, 64, 6, 7), (0, 32768, 0, 32),
-           (0, 4096, 8, 64)]
+# (stack entries in shared memory, shadow chunk, register cap, pixel tile, work mode: 1 tiles from
+# one counter, 2 static stride, 3 per-SM shares first)
+TUNINGS = [(0, 0, 8, 0, 1), (8, 0, 8, 0, 1), (8, 64, 8, 16, 3), (8, 2048, 8, 8, 2), (0, 64, 6, 7, 3),
+           (0, 32768, 0, 32, 1), (0, 4096, 8, 64, 3), (0, 0, 0, 0, 3)]
 
 
-@pytest.mark.parametrize("stack,chunk,cap,ptile", TUNINGS)
-def test_tuning_variants_give_the_same_image(ctx, stack, chunk, cap, ptile):
-    """Traversal stack entries in shared memory (0, 8, 16), shadow work in light-major chunks,
-    register caps and the pixel tiles primary rays are traced in (frames whose sides are not
-    multiples of the tile included) change only how the work runs: every variant's frame is the
-    default's bit for bit, through the plain path and through the batch path, on a deep
-    jittered frame with refraction (long traversal stacks) and on a config-3 mesh."""
+@pytest.mark.parametrize("stack,chunk,cap,ptile,work", TUNINGS)
+def test_tuning_variants_give_the_same_image(ctx, stack, chunk, cap, ptile, work):
+    """Traversal stack entries in shared memory (0, 8), shadow work in light-major chunks,
+    register caps, the pixel tiles primary rays are traced in (frames whose sides are not
+    multiples of the tile included) and how warps share the rays (one counter, static stride,
+    per-SM shares then a common pool then stealing) change only how the work runs: every
+    variant's frame is the default's bit for bit, through the plain path and through the batch
+    path, on a deep jittered frame with refraction (long traversal stacks) and on a config-3
+    mesh."""
     scene = rt.SceneHost.small(21, 14, 12, 96, 64, 2)
     mesh = rt.SceneHost.config(3, 4)
     want = [gpu_render(ctx, scene, 96, 64, 4, 4, 77, ref_tiles=False)[0],
             gpu_render(ctx, mesh, 128, 96, 1, 3, 0, ref_tiles=False)[0]]
-    ctx.set_tuning(rt.BatchTuning(128 if cap else 256, 32, stack, 1, cap, 1, 0, chunk, ptile))
+    ctx.set_tuning(rt.BatchTuning(128 if cap else 256, 32, stack, 1, cap, work, 0, chunk, ptile))
     try:
         got = [gpu_render(ctx, scene, 96, 64, 4, 4, 77, ref_tiles=False)[0],
                gpu_render(ctx, mesh, 128, 96, 1, 3, 0, ref_tiles=False)[0]]
@@ -198,7 +201,7 @@ def test_tuning_variants_give_the_same_image(ctx, stack, chunk, cap, ptile):
     rds = [ctx.render_desc(96, 64, 4, 4, flags=rt.RT_FLAG_HIT_PLANES, seed=77),
            ctx.render_desc(128, 96, 1, 3, flags=rt.RT_FLAG_HIT_PLANES)]
     try:
-        ctx.batch(sids, fids, rds, tuning=rt.BatchTuning(128 if cap else 256, 64, stack, 1, cap, 1, 0, chunk, ptile))
+        ctx.batch(sids, fids, rds, tuning=rt.BatchTuning(128 if cap else 256, 64, stack, 1, cap, work, 0, chunk, ptile))
         for f, (w, h), ref in zip(fids, [(96, 64), (128, 96)], want):
             got_b = ctx.download(f, w, h)
             np.testing.assert_array_equal(got_b["rgb"].view(np.uint32), ref["rgb"].view(np.uint32))
@@ -208,6 +211,29 @@ def test_tuning_variants_give_the_same_image(ctx, stack, chunk, cap, ptile):
             ctx.release_frame(f)
         for s in sids:
             ctx.release_scene(s)
+
+
+def test_profile_reports_kernel_times_and_idle_shares(ctx):
+    """RT_FLAG_PROFILE: event times per kernel kind and, from each warp's start and end stamps,
+    the share of the traversal and shading launches' warp time spent idle (before a block
+    started or after a warp ran out of work); the image is the unprofiled one."""
+    scene = rt.SceneHost.config(1).with_camera(256, 192)
+    plain, _ = gpu_render(ctx, scene, 256, 192, 1, 3, 1)
+    sid = ctx.upload(scene)
+    fid = ctx.frame(256, 192)
+    try:
+        st = ctx.render(sid, fid, ctx.render_desc(256, 192, 1, 3, flags=rt.RT_FLAG_PROFILE | rt.RT_FLAG_HIT_PLANES))
+        prof = ctx.download(fid, 256, 192)
+        d = st.as_dict()
+        for k in ("extend", "shade", "shadow"):
+            assert d["kernel_ms"][k] > 0 and d["kernel_launches"][k] == 4
+            assert 0.0 < d["kernel_idle"][k] < 1.0, d["kernel_idle"]
+        st2 = ctx.render(sid, fid, ctx.render_desc(256, 192, 1, 3))   # unprofiled: no idle shares
+        assert all(v == 0.0 for v in st2.as_dict()["kernel_idle"].values())
+    finally:
+        ctx.release_frame(fid)
+        ctx.release_scene(sid)
+    np.testing.assert_array_equal(prof["rgb"].view(np.uint32), plain["rgb"].view(np.uint32))
 
 
 def test_render_host_equals_device_path(ctx):
