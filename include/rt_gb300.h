@@ -277,6 +277,12 @@ typedef struct rt_batch_tuning {
                                     default tuning uses 4096) */
     int32_t pixel_tile;          /* primary rays traced in square pixel tiles of this edge, 0 (row by
                                     row) or 2..64; the image does not depend on it */
+    int32_t lanes;               /* batch: consecutive waves go in turn to this many workspaces, each
+                                    with its own stream, so one wave's kernels can use the SMs the
+                                    other's leave idle while they drain: 1 or 2 (0 = 2; a profiled
+                                    batch uses 1). Each lane holds a wave workspace (wave_rays
+                                    entries x 292 B) */
+    int32_t reserved;            /* 0 */
 } rt_batch_tuning;
 
 /* kernel tuning of the plain per-scene path (rt_render); NULL restores the defaults */
@@ -291,8 +297,8 @@ int rt_batch_render(rt_ctx *ctx, int32_t n, const int32_t *scene_ids, const int3
 int rt_batch_render_plain(rt_ctx *ctx, int32_t n, const int32_t *scene_ids,
                           const int32_t *frame_ids, const rt_render_desc *rds);
 /* pick block size, register cap and ray tile (or the static stride) for these jobs by timing
- * candidates, then per-SM shares of the rays, the short-stack depth in shared memory, the
- * pixel tile, the shadow chunk and the wave size.
+ * candidates, then per-SM shares of the rays, the wave lanes, the short-stack depth in shared
+ * memory, the pixel tile, the shadow chunk and the wave size.
  * Writes the choice. */
 int rt_batch_autotune(rt_ctx *ctx, int32_t n, const int32_t *scene_ids, const int32_t *frame_ids,
                       const rt_render_desc *rds, rt_batch_tuning *out);
@@ -384,6 +390,9 @@ int    rt_server_stats(rt_server *srv, rt_serve_stats *stats);
 /* frame latencies (ms, completion order) behind the current stats; *n = their count, at most
  * `cap` are copied (replicas merge these to exact percentiles across GPUs) */
 int    rt_server_latencies(rt_server *srv, double *ms, int64_t cap, int64_t *n);
+/* device time (ms, CUDA events) of each wave harvested since the current stats began, in the
+ * order the waves ran; *n = their count, at most `cap` are copied */
+int    rt_server_wave_ms(rt_server *srv, float *ms, int64_t cap, int64_t *n);
 /* a Poisson stream of requests in real time over the registered scenes: scene uniform, camera
  * orbiting the world origin at the distance of the scene's own camera (azimuth U[0,360),
  * elevation U[10,60] degrees), resolution uniform over 256^2, 512^2, 1024x768, 1920x1080.

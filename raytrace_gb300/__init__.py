@@ -92,10 +92,11 @@ class RenderStats(C.Structure):
 class BatchTuning(C.Structure):
     _fields_ = [("block", C.c_int32), ("tile", C.c_int32), ("stack", C.c_int32), ("use_graph", C.c_int32),
                 ("min_blocks", C.c_int32), ("dynamic", C.c_int32), ("wave_rays", C.c_int64),
-                ("shadow_chunk", C.c_int32), ("pixel_tile", C.c_int32)]
+                ("shadow_chunk", C.c_int32), ("pixel_tile", C.c_int32), ("lanes", C.c_int32),
+                ("reserved", C.c_int32)]
 
     def as_dict(self) -> dict:
-        return {k: getattr(self, k) for k, _ in self._fields_}
+        return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
 
 
 class ServerConfig(C.Structure):
@@ -171,6 +172,7 @@ _SIGS = {
     "rt_server_last_error": (C.c_char_p, [P]),
     "rt_server_stats": (C.c_int, [P, C.POINTER(ServeStats)]),
     "rt_server_latencies": (C.c_int, [P, P, C.c_int64, C.POINTER(C.c_int64)]),
+    "rt_server_wave_ms": (C.c_int, [P, P, C.c_int64, C.POINTER(C.c_int64)]),
     "rt_orbit_camera": (C.c_int, [C.POINTER(Camera), C.c_double, C.c_double, C.c_int32, C.c_int32,
                                   C.POINTER(Camera)]),
     "rt_server_add_scene": (C.c_int, [P, C.POINTER(SceneDesc), C.POINTER(C.c_int32)]),
@@ -625,6 +627,14 @@ class Server:
         self._ck(lib.rt_server_latencies(self._h, None, 0, C.byref(n)), "rt_server_latencies")
         out = np.empty(n.value, np.float64)
         self._ck(lib.rt_server_latencies(self._h, _ptr(out), out.size, C.byref(n)), "rt_server_latencies")
+        return out
+
+    def wave_ms(self) -> np.ndarray:
+        """Device time (ms) of each wave behind the current stats, in the order they ran."""
+        n = C.c_int64()
+        self._ck(lib.rt_server_wave_ms(self._h, None, 0, C.byref(n)), "rt_server_wave_ms")
+        out = np.empty(n.value, np.float32)
+        self._ck(lib.rt_server_wave_ms(self._h, _ptr(out), out.size, C.byref(n)), "rt_server_wave_ms")
         return out
 
     def run_poisson(self, lam: float, duration_s: float, seed: int = 4) -> dict:

@@ -30,6 +30,14 @@ WaveRunner::~WaveRunner()
         cudaEventDestroy(ftab_copied);
     }
     if (ftab_host) cudaFreeHost(ftab_host);
+    for (WaveLane &L : lanes) {
+        if (L.stream) {
+            cudaStreamSynchronize(L.stream);
+            cudaStreamDestroy(L.stream);
+        }
+        if (L.last) cudaEventDestroy(L.last);
+    }
+    if (go) cudaEventDestroy(go);
 }
 
 // A sample's rays at bounce l number at most b^l (b = children per hit, one queue holds one
@@ -40,7 +48,21 @@ long long wave_weight(int branching, int max_level)
     return branching >= 2 ? 1ll << max_level : 1ll;
 }
 
-size_t wave_runner_bytes(const WaveRunner &R) { return R.ws.mem.bytes + R.ftab_dev.bytes; }
+size_t wave_runner_bytes(const WaveRunner &R)
+{
+    size_t b = R.ftab_dev.bytes;
+    for (const WaveLane &L : R.lanes) b += L.ws.mem.bytes;
+    return b;
+}
+
+void wave_join(WaveRunner &R, cudaStream_t s)
+{
+    for (WaveLane &L : R.lanes)
+        if (L.stream && L.pending) {
+            cudaStreamWaitEvent(s, L.last, 0);
+            L.pending = false;
+        }
+}
 
 static int stage_harvest(rt_ctx *ctx, WaveRunner &R, WaveStage &st, bool wait)
 {
@@ -75,18 +97,42 @@ int wave_harvest(rt_ctx *ctx, WaveRunner &R, bool wait)
     return RT_OK;
 }
 
-int wave_runner_init(rt_ctx *ctx, WaveRunner &R, long long qcap, int jobcap, int n_stages)
+int wave_runner_init(rt_ctx *ctx, WaveRunner &R, long long qcap, int jobcap, int n_stages, int n_lanes)
 {
-    if (R.ws.mem.p && qcap <= R.ws.qcap && jobcap <= R.jobcap && (int)R.stages.size() >= n_stages) return RT_OK;
+    n_lanes = std::max(1, std::min(n_lanes, 2));
+    const bool fits = !R.lanes.empty() && (int)R.lanes.size() == n_lanes && R.lanes[0].ws.mem.p &&
+                      qcap <= R.lanes[0].ws.qcap && jobcap <= R.jobcap && (int)R.stages.size() >= n_stages;
+    if (fits) return RT_OK;
     int rc = wave_harvest(ctx, R, true);
     if (rc) return rc;
-    qcap = std::max(qcap, R.ws.qcap);
+    if (!R.lanes.empty()) qcap = std::max(qcap, R.lanes[0].ws.qcap);
     jobcap = std::max(jobcap, R.jobcap);
     n_stages = std::max(n_stages, (int)R.stages.size());
-    rc = ws_ensure(ctx, R.ws, qcap, jobcap);
-    if (rc) return rc;
-    R.graphs.clear();   // captured graphs point into the old workspace
-    R.ws.wf.cancel = nullptr;   // rt_batch_render arms and sets the context's flag
+    if ((int)R.lanes.size() != n_lanes) {   // a lane count change starts from new lanes
+        for (WaveLane &L : R.lanes) {
+            if (L.stream) {
+                cudaStreamSynchronize(L.stream);
+                cudaStreamDestroy(L.stream);
+            }
+            if (L.last) cudaEventDestroy(L.last);
+        }
+        R.lanes.clear();
+        R.lanes.resize((size_t)n_lanes);
+        R.next_lane = 0;
+        if (n_lanes > 1) {
+            for (WaveLane &L : R.lanes) {
+                CK(ctx, cudaStreamCreateWithFlags(&L.stream, cudaStreamNonBlocking));
+                CK(ctx, cudaEventCreateWithFlags(&L.last, cudaEventDisableTiming));
+            }
+            if (!R.go) CK(ctx, cudaEventCreateWithFlags(&R.go, cudaEventDisableTiming));
+        }
+    }
+    for (WaveLane &L : R.lanes) {
+        rc = ws_ensure(ctx, L.ws, qcap, jobcap);
+        if (rc) return rc;
+        L.graphs.clear();   // captured graphs point into the old workspace
+        L.ws.wf.cancel = nullptr;   // rt_batch_render arms and sets the context's flag
+    }
     for (WaveStage &st : R.stages) {
         if (st.jobs) cudaFreeHost(st.jobs);
         if (st.done) cudaEventDestroy(st.done);
@@ -112,7 +158,7 @@ int wave_runner_init(rt_ctx *ctx, WaveRunner &R, long long qcap, int jobcap, int
     return RT_OK;
 }
 
-static int wave_graph(rt_ctx *ctx, WaveRunner &R, int max_level, const Tuning &t, cudaGraphExec_t &exec)
+static int wave_graph(rt_ctx *ctx, WaveLane &R, int max_level, const Tuning &t, cudaGraphExec_t &exec)
 {
     const long long key = tuning_key(max_level, t);
     auto it = R.graphs.find(key);
@@ -145,7 +191,8 @@ int wave_enqueue(rt_ctx *ctx, WaveRunner &R, const std::vector<WaveJob *> &jobs,
     WaveStage &st = R.stages[R.next];
     int rc = stage_harvest(ctx, R, st, true);   // the ring is full: wait for its oldest wave
     if (rc) return rc;
-    const long long Q = R.ws.qcap;
+    WaveLane &lane = R.lanes[R.next_lane];
+    const long long Q = lane.ws.qcap;
     long long used = 0, samples = 0;
     int n = 0, n_scenes = 0, max_level = 0, max_lights = 0;
     std::vector<const SceneDev *> seen;
@@ -182,7 +229,12 @@ int wave_enqueue(rt_ctx *ctx, WaveRunner &R, const std::vector<WaveJob *> &jobs,
     st.scalars[3] = max_lights;
     st.n_jobs = n;
     st.samples = samples;
-    Workspace &ws = R.ws;
+    Workspace &ws = lane.ws;
+    if (lane.stream) {   // after what the caller enqueued on s (frame preparation, the cancel clear)
+        CK(ctx, cudaEventRecord(R.go, s));
+        CK(ctx, cudaStreamWaitEvent(lane.stream, R.go, 0));
+        s = lane.stream;
+    }
     CK(ctx, cudaEventRecord(st.start, s));
     CK(ctx, cudaMemcpyAsync(ws.scenes, st.scenes, sizeof(DevScene) * n_scenes, cudaMemcpyHostToDevice, s));
     CK(ctx, cudaMemcpyAsync(ws.jobs, st.jobs, sizeof(DevJob) * n, cudaMemcpyHostToDevice, s));
@@ -190,7 +242,7 @@ int wave_enqueue(rt_ctx *ctx, WaveRunner &R, const std::vector<WaveJob *> &jobs,
     CK(ctx, cudaMemcpyAsync(ws.scalars, st.scalars, 32, cudaMemcpyHostToDevice, s));
     cudaGraphExec_t exec = nullptr;
     if (use_graph) {
-        rc = wave_graph(ctx, R, max_level, t, exec);
+        rc = wave_graph(ctx, lane, max_level, t, exec);
         if (rc) return rc;
         CK(ctx, cudaGraphLaunch(exec, s));
     } else {
@@ -199,7 +251,13 @@ int wave_enqueue(rt_ctx *ctx, WaveRunner &R, const std::vector<WaveJob *> &jobs,
     }
     CK(ctx, cudaMemcpyAsync(st.counters, ws.wf.C, sizeof(Counters), cudaMemcpyDeviceToHost, s));
     CK(ctx, cudaEventRecord(st.done, s));
+    if (lane.stream) {
+        CK(ctx, cudaEventRecord(lane.last, s));
+        lane.pending = true;
+    }
+    st.lane = (int)R.next_lane;
     st.busy = true;
+    R.next_lane = (R.next_lane + 1) % R.lanes.size();
     R.next = (R.next + 1) % R.stages.size();
     R.waves++;
     R.wave_jobs += n;
@@ -245,15 +303,17 @@ static int batch_core(rt_ctx *ctx, int32_t n, const int32_t *scene_ids, const in
     WaveRunner &R = *ctx->batch;
     const long long cap = wave_rays > 0 ? wave_rays : kBatchQueue;
     const long long qcap = std::max(std::min(weighted, cap), std::max<long long>(heaviest, 4096));
-    int rc = wave_runner_init(ctx, R, qcap, std::max(n, 64), 2);
-    if (rc) return rc;
     bool profile = false;
     for (int i = 0; i < n; ++i) profile |= (rds[i].flags & RT_FLAG_PROFILE) != 0;
+    // a profiled batch runs its waves one after another, so kernel times do not overlap
+    const int lanes = profile ? 1 : t.lanes;
+    int rc = wave_runner_init(ctx, R, qcap, std::max(n, 64), 2 * lanes, lanes);
+    if (rc) return rc;
     ctx->prof.reset(profile);
     if (profile) use_graph = false;
     KernelProfiler *P = profile ? &ctx->prof : nullptr;
     cudaStream_t s = ctx->stream;
-    R.ws.wf.cancel = ctx->cancel_dev;
+    for (WaveLane &L : R.lanes) L.ws.wf.cancel = ctx->cancel_dev;
     rc = cancel_arm(ctx, ctx->cancel_count.load());
     if (rc) return rc;
     R.rays_primary = R.rays_secondary = R.rays_shadow = 0;
@@ -292,6 +352,7 @@ static int batch_core(rt_ctx *ctx, int32_t n, const int32_t *scene_ids, const in
         if (rc) return rc;
         if (!got) break;
     }
+    wave_join(R, s);   // the resolve reads what every wave accumulated
     if (P) P->begin(RT_KERNEL_RESOLVE, s);
     launch_frames_resolve(ftab, n, quads, s);
     if (P) P->end(s);
@@ -353,8 +414,8 @@ extern "C" int rt_batch_autotune(rt_ctx *ctx, int32_t n, const int32_t *scene_id
     if (!ctx || !out) return RT_ERR_INVALID;
     // Coordinate search, each candidate timed as the best of three batches after a warm one
     // (which captures its graph): (threads per block, register cap as resident blocks per SM) x
-    // rays per tile fetch (0 = the static grid stride), then per-SM shares of the rays, then the
-    // traversal stack entries kept in shared memory, then the primary rays' pixel tile, then the
+    // rays per tile fetch (0 = the static grid stride), then per-SM shares of the rays, then one
+    // wave lane instead of two, then the traversal stack entries kept in shared memory, then the primary rays' pixel tile, then the
     // shadow work chunk, then the wave size. The caller picks the jobs: tuning on a sample of the
     // workload and measuring on the rest keeps the choice honest.
     const int shapes[][2] = {{128, 8}, {128, 6}, {64, 8}, {256, 0}};
@@ -387,6 +448,12 @@ extern "C" int rt_batch_autotune(rt_ctx *ctx, int32_t n, const int32_t *scene_id
     if (best_t.dynamic == 1) {   // the tiles of each SM's own share of the rays first
         rt_batch_tuning t = best_t;
         t.dynamic = 3;
+        int rc = trial(t);
+        if (rc) return rc;
+    }
+    {   // waves one after another on one workspace instead of in turn on two
+        rt_batch_tuning t = best_t;
+        t.lanes = 1;
         int rc = trial(t);
         if (rc) return rc;
     }

@@ -1107,6 +1107,8 @@ int tuning_from(rt_ctx *ctx, const rt_batch_tuning *in, Tuning &t)
     t.min_blocks = in->min_blocks;
     t.shadow_chunk = in->shadow_chunk;
     t.pixel_tile = in->pixel_tile;
+    if (in->lanes) t.lanes = in->lanes;
+    if (t.lanes != 1 && t.lanes != 2) return ctx_fail(ctx, RT_ERR_INVALID, "lanes %d: use 0 (default), 1 or 2", t.lanes);
     if (in->dynamic < 0 || in->dynamic > 3) return ctx_fail(ctx, RT_ERR_INVALID, "dynamic %d: use 0..3", in->dynamic);
     t.dynamic = in->dynamic != 2;
     t.shares = in->dynamic == 3;
@@ -1138,7 +1140,7 @@ extern "C" int rt_ctx_get_tuning(const rt_ctx *ctx, rt_batch_tuning *out)
     if (!ctx || !out) return RT_ERR_INVALID;
     const Tuning &t = ctx->plain_tuning;
     *out = rt_batch_tuning{t.block, t.tile, t.stack, 1, t.min_blocks, t.dynamic ? (t.shares ? 3 : 1) : 2, 0,
-                           t.shadow_chunk, t.pixel_tile};
+                           t.shadow_chunk, t.pixel_tile, t.lanes, 0};
     return RT_OK;
 }
 

@@ -157,21 +157,35 @@ struct WaveStage {
     rtg::Counters *counters = nullptr;
     cudaEvent_t start = nullptr;         // recorded before the wave's table copies
     cudaEvent_t done = nullptr;
+    int lane = 0;
     bool busy = false;
     int n_jobs = 0;
     long long samples = 0;
 };
 
-// waves of chunks traced through one workspace: the per-bounce sequence is a CUDA graph
+// One wave lane: a workspace, the graphs captured against it and, when the runner has more than
+// one lane, a stream of its own. Waves go to the lanes in turn, so a wave's kernels can take the
+// SMs the previous wave's kernels leave idle while they drain (every wavefront kernel ends with
+// warps out of work waiting for the slowest tile).
+struct WaveLane {
+    Workspace ws;
+    std::map<long long, std::unique_ptr<GraphEntry>> graphs;
+    cudaStream_t stream = nullptr;       // own stream of a multi-lane runner (NULL: the caller's)
+    cudaEvent_t last = nullptr;          // after the lane's last wave
+    bool pending = false;                // a wave was enqueued since the caller's stream joined it
+};
+
+// waves of chunks traced through the lanes' workspaces: the per-bounce sequence is a CUDA graph
 // replayed per wave, tables are staged through a ring of pinned buffers so the host can run
 // ahead of the device by `stages` waves, and the queue never overflows because each wave's
 // chunks are sized against the capacity with every sample's branching bound
 struct WaveRunner {
-    Workspace ws;
+    std::vector<WaveLane> lanes;         // at least one after wave_runner_init
+    size_t next_lane = 0;
+    cudaEvent_t go = nullptr;            // the caller's stream before a wave on a lane's own stream
     std::vector<WaveStage> stages;
     size_t next = 0;
     int jobcap = 0;
-    std::map<long long, std::unique_ptr<GraphEntry>> graphs;
     // totals of harvested waves
     unsigned long long rays_primary = 0, rays_secondary = 0, rays_shadow = 0;
     int overflow = 0, error = 0;
@@ -191,11 +205,15 @@ struct WaveRunner {
 };
 
 long long wave_weight(int branching, int max_level);
-int wave_runner_init(rt_ctx *ctx, WaveRunner &R, long long qcap, int jobcap, int stages);
-// plan and enqueue the next wave from `jobs` (taken in order) on stream s; waits only when the
-// staging ring is full. Sets *samples to the samples enqueued (0 = nothing left to trace).
+// lanes: 1, or 2 (each with its own workspace of qcap entries and its own stream)
+int wave_runner_init(rt_ctx *ctx, WaveRunner &R, long long qcap, int jobcap, int stages, int lanes = 1);
+// plan and enqueue the next wave from `jobs` (taken in order) after the work already on stream s
+// (on the next lane's stream, or on s itself with one lane); waits only when the staging ring is
+// full. Sets *samples to the samples enqueued (0 = nothing left to trace).
 int wave_enqueue(rt_ctx *ctx, WaveRunner &R, const std::vector<WaveJob *> &jobs, const rtg::Tuning &t, bool use_graph,
                  cudaStream_t s, long long *samples, KernelProfiler *prof = nullptr);
+// make stream s wait for every wave enqueued so far (work on s that reads the waves' frames)
+void wave_join(WaveRunner &R, cudaStream_t s);
 // harvest every finished wave (wait = block until all enqueued waves are done)
 int wave_harvest(rt_ctx *ctx, WaveRunner &R, bool wait);
 size_t wave_runner_bytes(const WaveRunner &R);

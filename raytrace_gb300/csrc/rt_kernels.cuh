@@ -71,6 +71,7 @@ struct Tuning {
     int min_blocks = 8;  // 0, 6 or 8: register cap of the traversal kernels (128-thread blocks)
     int shadow_chunk = 4096;   // shadow work in light-major chunks of this many hits (0 = one chunk)
     int pixel_tile = 0;     // primary rays in square pixel tiles of this edge (0 = row by row)
+    int lanes = 2;          // batch: waves in turn on this many workspaces and streams (1 or 2)
 };
 
 int sm_count();

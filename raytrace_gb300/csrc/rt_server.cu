@@ -903,6 +903,16 @@ int rt_server_latencies(rt_server *srv, double *ms, int64_t cap, int64_t *n)
     return RT_OK;
 }
 
+int rt_server_wave_ms(rt_server *srv, float *ms, int64_t cap, int64_t *n)
+{
+    if (!srv || !n || cap < 0 || (cap && !ms)) return RT_ERR_INVALID;
+    const std::vector<float> &w = srv->runner.wave_ms;
+    *n = (int64_t)w.size();
+    const size_t k = std::min(w.size(), (size_t)cap);
+    if (k) std::memcpy(ms, w.data(), k * sizeof(float));
+    return RT_OK;
+}
+
 int rt_server_run_poisson(rt_server *srv, double lambda, double duration, uint64_t seed, rt_serve_stats *stats)
 {
     if (!srv || !stats || !(lambda > 0) || !(duration > 0) || srv->scenes.empty()) return RT_ERR_INVALID;

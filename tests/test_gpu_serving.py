@@ -57,6 +57,31 @@ def test_batch_equals_plain_renders(ctx):
             ctx.release_scene(s)
 
 
+@pytest.mark.parametrize("lanes", [1, 2])
+def test_batch_split_over_many_waves_equals_plain(ctx, lanes):
+    """Queues of 2^14 entries cut the batch into dozens of waves; with two lanes consecutive
+    waves run on two workspaces and streams at once. Every frame is still its plain render."""
+    scenes = [rt.SceneHost.config(3, i) for i in (0, 2, 4)] + small_scenes()[:2]
+    sizes = [(160, 120), (128, 128), (96, 96), (128, 96), (100, 60)]
+    sids = [ctx.upload(sc) for sc in scenes]
+    fids = [ctx.frame(w, h) for w, h in sizes]
+    rds = [ctx.render_desc(w, h, 1, 3) for w, h in sizes]
+    try:
+        t = rt.BatchTuning(128, 32, 0, 1, 8, 1, 1 << 14, 4096, 0, lanes)
+        ctx.batch(sids, fids, rds, tuning=t)
+        st = ctx.wait()   # the batch's counters, before plain renders replace them
+        assert st.rays_primary == sum(w * h for w, h in sizes)
+        for sc, fid, (w, h) in zip(scenes, fids, sizes):
+            got = ctx.download(fid, w, h, planes=False)
+            ref = plain_render(ctx, sc, w, h)
+            np.testing.assert_array_equal(got["rgb"].view(np.uint32), ref["rgb"].view(np.uint32))
+    finally:
+        for f in fids:
+            ctx.release_frame(f)
+        for sd in sids:
+            ctx.release_scene(sd)
+
+
 def test_plain_render_after_workspace_growth():
     """A render whose frame needs a larger ray workspace than the last one re-lays the
     workspace out; the cached launch graph must follow even when the new allocation comes back
