@@ -74,7 +74,7 @@ class ClockSampler:
 
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
               "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
-              "clocks_event_reasons.sw_power_cap")
+              "clocks_event_reasons.sw_power_cap,clocks.mem")
 
     def __init__(self, gpu: int):
         self.gpu = gpu
@@ -100,7 +100,7 @@ class ClockSampler:
                 self.out, _ = self.proc.communicate()
 
     def summary(self) -> dict:
-        sm, mx, reasons = [], [], set()
+        sm, mx, mem, power, reasons = [], [], [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for line in (getattr(self, "out", "") or "").splitlines():
             p = [x.strip() for x in line.split(",")]
@@ -111,12 +111,19 @@ class ClockSampler:
                 mx.append(float(p[2]))
             except ValueError:
                 continue
+            try:
+                power.append(float(p[3]))
+                mem.append(float(p[9]))
+            except (ValueError, IndexError):
+                pass
             for n, v in zip(names, p[5:9]):
                 if v.lower() == "active":
                     reasons.add(n)
         if not sm:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
-        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons), "samples": len(sm)}
+        med = lambda v: statistics.median(v) if v else None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "mem_mhz": med(mem),
+                "power_w_median": med(power), "reasons": sorted(reasons), "samples": len(sm)}
 
 
 def measured_peaks() -> tuple[float, str]:
@@ -357,8 +364,12 @@ def run_batched(ctx, n_scenes: int, reps: int) -> dict:
 SATURATED_REPEATS = 3
 
 
-def run_served(ctx, seconds: float) -> dict:
-    """Config 4: Poisson request streams over 64 resident scenes, batched server vs plain server."""
+def run_served(ctx, seconds: float, gpu: int) -> dict:
+    """Config 4: Poisson request streams over 64 resident scenes, batched server vs plain server.
+
+    The saturated repeats follow an untimed saturated burst of their own (another seed): after
+    the light streams the GPU's power draw ramps from a few hundred watts, and the first
+    saturated wave after a long light phase ran slower for about a second."""
     import raytrace_gb300 as rt
 
     scenes = gen_scenes(4, 64)
@@ -379,8 +390,11 @@ def run_served(ctx, seconds: float) -> dict:
                 out.setdefault(f"lambda_{lam}", {})[arm] = pick(srv.run_poisson(float(lam), seconds, seed=4))
             # ~10000 requests arriving within 0.5 s: sustained peak throughput, repeated with
             # other seeds (other request mixes)
-            reps = [pick(srv.run_poisson(20000.0, 0.5, seed=5 + r)) for r in range(SATURATED_REPEATS)]
+            srv.run_poisson(20000.0, 0.5, seed=99)   # untimed warm-up burst
+            with ClockSampler(gpu) as clk:
+                reps = [pick(srv.run_poisson(20000.0, 0.5, seed=5 + r)) for r in range(SATURATED_REPEATS)]
             out.setdefault("saturated", {})[arm] = {
+                "clocks": clk.summary(),
                 "median_mrays_per_s": round(statistics.median(r["mrays_per_s"] for r in reps), 2),
                 "min_mrays_per_s": round(min(r["mrays_per_s"] for r in reps), 2),
                 "max_mrays_per_s": round(max(r["mrays_per_s"] for r in reps), 2),
@@ -579,7 +593,7 @@ def run_gpu(args) -> None:
     # 256-scene batch and the CPU sample in the same process its saturated stream has measured
     # 10-15 % slower in some runs (the plain arm and the batch leg do not move)
     if world == 1 and not args.skip_served:
-        out["served"] = run_served(ctx, args.served_seconds)
+        out["served"] = run_served(ctx, args.served_seconds, local)
     if world == 1 and not args.skip_batched:
         out["batched"] = run_batched(ctx, args.batched_scenes, 2)
     if world == 1 and not args.skip_cpu:

@@ -277,10 +277,10 @@ typedef struct rt_batch_tuning {
                                     default tuning uses 4096) */
     int32_t pixel_tile;          /* primary rays traced in square pixel tiles of this edge, 0 (row by
                                     row) or 2..64; the image does not depend on it */
-    int32_t lanes;               /* batch: consecutive waves go in turn to this many workspaces, each
+    int32_t lanes;               /* batch and server: consecutive waves go in turn to this many workspaces, each
                                     with its own stream, so one wave's kernels can use the SMs the
-                                    other's leave idle while they drain: 1 or 2 (0 = 2; a profiled
-                                    batch uses 1). Each lane holds a wave workspace (wave_rays
+                                    other's leave idle while they drain: 1 or 2 (0 = 2 for a batch,
+                                    1 for a server; a profiled batch uses 1). Each lane holds a wave workspace (wave_rays
                                     entries x 292 B) */
     int32_t reserved;            /* 0 */
 } rt_batch_tuning;
@@ -320,11 +320,12 @@ typedef struct rt_server_config {
     int32_t max_level;           /* recursion depth of every request */
     int32_t spp;                 /* samples per pixel of every request (>= 1) */
     int32_t plain;               /* 1: one request at a time through rt_render (comparison path) */
-    int64_t queue_rays;          /* ray-queue entries of one wave, 292 B each (0 = 2^27, halved
-                                    until the queues take at most a third of the budget) */
+    int64_t queue_rays;          /* ray-queue entries of one wave, 292 B each, per lane (0 = 2^27,
+                                    halved until the queues take at most a third of the
+                                    budget) */
     int64_t max_pixels;          /* largest width*height of a request (0 = 1920*1080) */
     int32_t keep_images;         /* 1: keep finished images in host memory until rt_server_result */
-    int32_t stages;              /* waves the host may enqueue ahead of the device (0 = 2) */
+    int32_t stages;              /* waves the host may enqueue ahead of the device (0 = 2 per lane) */
 } rt_server_config;
 
 typedef struct rt_request {
@@ -370,7 +371,9 @@ int    rt_server_create(rt_ctx *ctx, const rt_server_config *cfg, rt_server **ou
 void   rt_server_destroy(rt_server *srv);
 const char *rt_server_last_error(const rt_server *srv);
 /* kernel tuning of the server's waves (NULL = the defaults; the plain mode sets the context's
- * tuning, which its renders use); requests admitted from now on use it. Images do not depend on it. */
+ * tuning, which its renders use); requests admitted from now on use it. Images do not depend on it.
+ * A new lane count takes an idle server (RT_ERR_BUSY while requests are pending) and keeps the
+ * queue size of a lane (RT_ERR_BUDGET when the new lanes do not fit the budget). */
 int    rt_server_set_tuning(rt_server *srv, const rt_batch_tuning *tuning);
 /* register a scene (deep copy kept for rebuilds); it is uploaded now if the budget allows */
 int    rt_server_add_scene(rt_server *srv, const rt_scene_desc *desc, int32_t *scene);

@@ -64,6 +64,18 @@ void wave_join(WaveRunner &R, cudaStream_t s)
         }
 }
 
+void wave_join_all_but_last(WaveRunner &R, cudaStream_t s)
+{
+    const size_t n = R.lanes.size(), last = (R.next_lane + n - 1) % n;
+    for (size_t k = 0; k < n; ++k) {
+        WaveLane &L = R.lanes[k];
+        if (k != last && L.stream && L.pending) {
+            cudaStreamWaitEvent(s, L.last, 0);
+            L.pending = false;
+        }
+    }
+}
+
 static int stage_harvest(rt_ctx *ctx, WaveRunner &R, WaveStage &st, bool wait)
 {
     if (!st.busy) return RT_OK;

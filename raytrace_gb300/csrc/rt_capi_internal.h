@@ -214,6 +214,9 @@ int wave_enqueue(rt_ctx *ctx, WaveRunner &R, const std::vector<WaveJob *> &jobs,
                  cudaStream_t s, long long *samples, KernelProfiler *prof = nullptr);
 // make stream s wait for every wave enqueued so far (work on s that reads the waves' frames)
 void wave_join(WaveRunner &R, cudaStream_t s);
+// make stream s wait for every wave enqueued so far but the last one: the frames finished by the
+// previous wave can be resolved on s while the last wave runs on its own lane
+void wave_join_all_but_last(WaveRunner &R, cudaStream_t s);
 // harvest every finished wave (wait = block until all enqueued waves are done)
 int wave_harvest(rt_ctx *ctx, WaveRunner &R, bool wait);
 size_t wave_runner_bytes(const WaveRunner &R);

@@ -5,8 +5,12 @@
 // the HBM budget allow (evicting idle scenes least-recently-used first and rebuilding an
 // evicted scene's LBVH when a request needs it again), and enqueues one wave made of sample
 // chunks of every admitted request: requests admitted at different times trace in the same
-// kernels. A request whose last chunk is enqueued is resolved on the compute stream and copied
-// to pinned host memory on a copy stream, overlapping the next waves. Colours accumulate as
+// kernels. With two lanes (a workspace and a stream each; the tuning's lane count, 1 by
+// default) waves go to them in turn, so a wave's kernels can fill the SMs the previous wave's
+// kernels leave idle as they drain. A request whose last chunk is enqueued is resolved on the
+// compute stream once the waves that traced it are done (with two lanes, in the next step,
+// after the next wave is enqueued, so the resolve never holds back a wave), and copied to
+// pinned host memory on a copy stream, overlapping the next waves. Colours accumulate as
 // exact fixed-point sums, so a frame is bit-identical alone, in any mix and split over any
 // waves. The plain mode renders one request at a time through rt_render, for comparison.
 //
@@ -111,7 +115,7 @@ struct rt_server {
     double base_s = 0.0;          // server clock at base_ev
     cudaStream_t copy = nullptr;
     WaveRunner runner;
-    Tuning tuning;
+    Tuning tuning;                // lanes: 1 unless set (two concurrent waves served fewer rays a second)
     std::vector<SrvScene> scenes;
     std::vector<DevSlot> dslots;
     // free frame slots, oldest freed first: a slot's image copy to the host must finish before
@@ -121,6 +125,7 @@ struct rt_server {
     std::vector<HostSlot> hslots;
     std::deque<Request *> queue;
     std::vector<Request *> inflight;    // admission order
+    std::vector<Request *> deferred;    // last chunk in the last wave: resolved in the next step
     std::deque<Request *> resolving;    // enqueue order
     std::unordered_map<int64_t, std::unique_ptr<Request>> reqs;
     std::vector<cudaEvent_t> ev_pool;
@@ -284,7 +289,7 @@ static int admit(rt_server *srv)
         srv->hslots[(size_t)hs].used = true;
         r->dev_slot = ds, r->host_slot = hs;
         r->rebuilt = rebuilt;
-        if (!srv->inflight.empty() || !srv->resolving.empty()) srv->admitted_busy++;
+        if (!srv->inflight.empty() || !srv->deferred.empty() || !srv->resolving.empty()) srv->admitted_busy++;
         r->admit_s = srv->now();
         r->state = kInflight;
         sc.users++;
@@ -322,8 +327,8 @@ static int launch_frames(rt_server *srv, std::vector<FrameJob> &jobs, bool resol
     return RT_OK;
 }
 
-// the last chunk of r is enqueued: free its device slot; its resolve and copy-out follow in
-// resolve_finished
+// the last chunk of r is enqueued and every wave that traced it is joined to the compute stream:
+// its resolve, copy-out and the release of its device slot follow in resolve_finished
 static int finish(rt_server *srv, Request *r)
 {
     DevSlot &slot = srv->dslots[(size_t)r->dev_slot];
@@ -474,7 +479,31 @@ static int step_plain(rt_server *srv)
 
 static int pending(const rt_server *srv)
 {
-    return (int)(srv->queue.size() + srv->inflight.size() + srv->resolving.size());
+    return (int)(srv->queue.size() + srv->inflight.size() + srv->deferred.size() + srv->resolving.size());
+}
+
+// nothing is admitted, traced or resolving: the head of a non-empty queue can never be admitted
+static bool stuck(const rt_server *srv)
+{
+    return !srv->cfg.plain && srv->inflight.empty() && srv->deferred.empty() && srv->resolving.empty() &&
+           !srv->queue.empty();
+}
+
+// resolve the requests the last wave finished; all_waves: no newer wave was enqueued, join every
+// lane (else every lane but the newest wave's, which runs on while they resolve). The join is
+// made in every step, requests or not, so the compute stream has always waited for each wave but
+// the newest: a request's earlier chunks may have run in any older wave.
+static int resolve_deferred(rt_server *srv, bool all_waves)
+{
+    if (all_waves) wave_join(srv->runner, srv->ctx->stream);
+    else wave_join_all_but_last(srv->runner, srv->ctx->stream);
+    if (srv->deferred.empty()) return RT_OK;
+    for (Request *r : srv->deferred) {
+        int rc = finish(srv, r);
+        if (rc) return rc;
+    }
+    srv->deferred.clear();
+    return resolve_finished(srv);
 }
 
 static void wave_order(const rt_server *srv, std::vector<WaveJob *> &order)
@@ -496,6 +525,10 @@ static int step_batched(rt_server *srv)
     if (rc) return rc;
     std::vector<WaveJob *> order;
     wave_order(srv, order);
+    if (order.empty()) {   // no wave to enqueue: the last wave's requests resolve now
+        rc = resolve_deferred(srv, true);
+        if (rc) return rc;
+    }
     if (order.empty() && !srv->resolving.empty()) {
         rc = retire(srv, true);
         if (rc) return rc;
@@ -509,13 +542,18 @@ static int step_batched(rt_server *srv)
         long long got = 0;
         rc = wave_enqueue(ctx, srv->runner, order, srv->tuning, true, ctx->stream, &got);
         if (rc) return rc;
+        // the previous wave's requests resolve behind the wave just enqueued
+        rc = resolve_deferred(srv, false);
+        if (rc) return rc;
+        const bool one_lane = srv->runner.lanes.size() == 1;   // one stream: resolve right behind the wave
         std::vector<Request *> still;
         for (Request *r : srv->inflight) {
-            if (r->wj.cursor >= r->wj.total) {
+            if (r->wj.cursor < r->wj.total) still.push_back(r);
+            else if (!one_lane) srv->deferred.push_back(r);
+            else {
                 rc = finish(srv, r);
                 if (rc) return rc;
-            } else
-                still.push_back(r);
+            }
         }
         srv->inflight.swap(still);
         rc = resolve_finished(srv);
@@ -629,13 +667,15 @@ static int server_init(rt_server *srv)
 {
     rt_ctx *ctx = srv->ctx;
     rt_server_config &c = srv->cfg;
+    const int lanes = srv->tuning.lanes;
     if (c.max_inflight <= 0) c.max_inflight = 64;
     if (c.queue_rays <= 0) {   // 2^27 entries, halved until the wave queues take at most a third of the budget
         c.queue_rays = 1ll << 27;
-        while (c.queue_rays > (1ll << 16) && kWsBytesPerEntry * c.queue_rays > c.hbm_budget_bytes / 3) c.queue_rays >>= 1;
+        while (c.queue_rays > (1ll << 16) && lanes * kWsBytesPerEntry * c.queue_rays > c.hbm_budget_bytes / 3)
+            c.queue_rays >>= 1;
     }
     if (c.max_pixels <= 0) c.max_pixels = 1920ll * 1080;
-    if (c.stages <= 0) c.stages = 2;
+    if (c.stages <= 0) c.stages = 2 * lanes;
     if (c.spp < 1 || c.spp > 1024 || c.max_level < 0 || c.max_level > 4 || c.max_inflight > 4096 ||
         c.queue_rays > (1ll << 27) || c.queue_rays < (1ll << c.max_level) || c.max_pixels > (1ll << 26) ||
         c.stages > 8 || c.hbm_budget_bytes <= 0)
@@ -677,7 +717,7 @@ static int server_init(rt_server *srv)
             CK(ctx, T.dev[k].ensure(sizeof(FrameJob) * (size_t)T.cap));
             srv->fixed_bytes += (int64_t)T.dev[k].bytes;
         }
-        int rc = wave_runner_init(ctx, srv->runner, c.queue_rays, c.max_inflight, c.stages);
+        int rc = wave_runner_init(ctx, srv->runner, c.queue_rays, c.max_inflight, c.stages, lanes);
         if (rc) return rc;
         srv->fixed_bytes += (int64_t)wave_runner_bytes(srv->runner);
     }
@@ -699,6 +739,7 @@ int rt_server_create(rt_ctx *ctx, const rt_server_config *cfg, rt_server **out)
     rt_server *srv = new rt_server();
     srv->ctx = ctx;
     srv->cfg = *cfg;
+    srv->tuning.lanes = 1;
     int rc = server_init(srv);
     if (rc) {
         std::string msg = ctx->err;
@@ -748,8 +789,24 @@ int rt_server_set_tuning(rt_server *srv, const rt_batch_tuning *tuning)
         int rc = tuning_from(srv->ctx, tuning, t);
         if (rc) return rc;
     }
+    if (!tuning || !tuning->lanes) t.lanes = 1;   // the server's default
     // the plain mode renders through rt_render, which takes the context's tuning
     if (srv->cfg.plain) return rt_ctx_set_tuning(srv->ctx, tuning);
+    WaveRunner &R = srv->runner;
+    if ((size_t)t.lanes != R.lanes.size()) {   // new lanes of the same queue size, on an idle server
+        if (pending(srv) > 0) return srv_fail(srv, RT_ERR_BUSY, "lanes change with requests pending");
+        const int64_t lane_bytes = (int64_t)R.lanes[0].ws.mem.bytes;
+        const int64_t grow = lane_bytes * ((int64_t)t.lanes - (int64_t)R.lanes.size());
+        if (used_bytes(srv) + grow > srv->cfg.hbm_budget_bytes)
+            return srv_fail(srv, RT_ERR_BUDGET, "%d lanes need %lld more bytes, over the budget", t.lanes,
+                            (long long)grow);
+        srv->fixed_bytes -= (int64_t)wave_runner_bytes(R);
+        int rc = wave_runner_init(srv->ctx, R, R.lanes[0].ws.qcap, R.jobcap,
+                                  std::max<int>(srv->cfg.stages, 2 * t.lanes), t.lanes);
+        srv->fixed_bytes += (int64_t)wave_runner_bytes(R);
+        if (rc) return rc;
+        note_peak(srv);
+    }
     srv->tuning = t;
     return RT_OK;
 }
@@ -842,7 +899,7 @@ int rt_server_drain(rt_server *srv)
         int rc = rt_server_step(srv, &n);
         if (rc) return rc;
         if (n == 0) break;
-        if (!srv->cfg.plain && srv->inflight.empty() && srv->resolving.empty() && !srv->queue.empty()) {
+        if (stuck(srv)) {
             // nothing runs and the head request cannot be admitted: it never will be
             return srv_fail(srv, RT_ERR_BUSY, "queued requests cannot be admitted (result slots full?)");
         }
@@ -970,7 +1027,7 @@ int rt_server_run_poisson(rt_server *srv, double lambda, double duration, uint64
             int32_t n = 0;
             rc = rt_server_step(srv, &n);
             if (rc) return rc;
-            if (!srv->cfg.plain && srv->inflight.empty() && srv->resolving.empty() && !srv->queue.empty())
+            if (stuck(srv))
                 return srv_fail(srv, RT_ERR_BUSY, "queued requests cannot be admitted (result slots full?)");
         } else if (k < arr.size()) {
             const double wait = arr[k].t - (srv->now() - start);

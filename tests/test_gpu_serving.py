@@ -182,23 +182,39 @@ def test_server_request_alone_equals_in_mix(ctx):
 
 def test_server_tuning_changes_no_image(ctx):
     """A server whose waves run another tuning (stack entries in shared memory, pixel tiles,
-    shadow chunks, tiles) gives every request the image of the default tuning."""
+    shadow chunks, tiles, two lanes instead of one) gives every request the image of the default
+    tuning."""
     scenes = small_scenes()[:3]
     images = []
-    for tuning in (None, rt.BatchTuning(128, 64, 8, 1, 8, 1, 0, 2048, 16)):
+    for tuning in (None, rt.BatchTuning(128, 64, 8, 1, 8, 1, 0, 2048, 16),
+                   rt.BatchTuning(128, 32, 0, 1, 8, 1, 0, 4096, 0, 2)):
         with rt.Server(ctx, 8 << 30, max_inflight=4, queue_rays=1 << 14, max_pixels=128 * 128) as srv:
             if tuning is not None:
                 srv.set_tuning(tuning)
             ids = [srv.add_scene(s) for s in scenes]
-            rids = [srv.submit(*r) for r in mixed_requests(srv, ids)[:6]]
+            rids = []
+            for k, r in enumerate(mixed_requests(srv, ids)[:6]):
+                rids.append(srv.submit(*r))
+                if k % 2:
+                    srv.step()   # requests finish in different waves, on both lanes
             srv.drain()
+            st = srv.stats()
             images.append([srv.result(r)["rgb"] for r in rids])
-    for a, b in zip(*images):
-        np.testing.assert_array_equal(a.view(np.uint32), b.view(np.uint32))
+        assert st["waves"] > 6, st
+    for other in images[1:]:
+        for a, b in zip(images[0], other):
+            np.testing.assert_array_equal(a.view(np.uint32), b.view(np.uint32))
     with rt.Server(ctx, 8 << 30, max_inflight=4) as srv:
         with pytest.raises(rt.RTError) as e:
             srv.set_tuning(rt.BatchTuning(128, 32, 5, 1, 8, 1, 0, 0, 0))   # 5 stack entries: not offered
         assert e.value.code == rt.RT_ERR_INVALID
+        sid = srv.add_scene(scenes[0])
+        srv.submit(sid, 32, 32)
+        with pytest.raises(rt.RTError) as e:   # the lane count changes only on an idle server
+            srv.set_tuning(rt.BatchTuning(128, 32, 0, 1, 8, 1, 0, 0, 0, 2))
+        assert e.value.code == rt.RT_ERR_BUSY
+        srv.drain()
+        srv.set_tuning(rt.BatchTuning(128, 32, 0, 1, 8, 1, 0, 0, 0, 2))
 
 
 def test_server_plain_mode_matches_batched(ctx):
