@@ -7,10 +7,11 @@
 // chunks of every admitted request: requests admitted at different times trace in the same
 // kernels. With two lanes (a workspace and a stream each; the tuning's lane count, 1 by
 // default) waves go to them in turn, so a wave's kernels can fill the SMs the previous wave's
-// kernels leave idle as they drain. A request whose last chunk is enqueued is resolved on the
-// compute stream once the waves that traced it are done (with two lanes, in the next step,
-// after the next wave is enqueued, so the resolve never holds back a wave), and copied to
-// pinned host memory on a copy stream, overlapping the next waves. Colours accumulate as
+// kernels leave idle as they drain. The frames admitted in a step are prepared on a stream of
+// their own while the previous wave runs; a request whose last chunk is enqueued is resolved on
+// another stream once the waves that traced it are done (with two lanes, in the next step, after
+// the next wave is enqueued), so neither holds back a wave, and copied to pinned host memory on
+// a copy stream. Its frame slot is reused once that copy is done. Colours accumulate as
 // exact fixed-point sums, so a frame is bit-identical alone, in any mix and split over any
 // waves. The plain mode renders one request at a time through rt_render, for comparison.
 //
@@ -54,8 +55,7 @@ struct SrvScene {
 struct DevSlot {
     DevBuf mem;
     FrameBufs fb{};
-    cudaEvent_t copied = nullptr;   // the last image copy out of this slot
-    bool used = false;
+    bool used = false;              // until the image copy out of it is done
 };
 
 struct HostSlot {
@@ -94,9 +94,10 @@ struct SplitMix {
 
 const int kServeRes[4][2] = {{256, 256}, {512, 512}, {1024, 768}, {1920, 1080}};
 
-// Frame tables of the per-step prepare and resolve launches (every request admitted in a step
+// Frame tables of the per-step prepare or resolve launches (every request admitted in a step
 // is prepared by one launch, every request finished in a step is resolved by one): pinned host
-// copies in a small ring, each rewritten once the copy out of it has run.
+// copies in a small ring, each rewritten once the copy out of it has run. Each ring serves one
+// stream, so a device table is rewritten only after the kernel that read it.
 struct TableRing {
     static constexpr int kSlots = 4;
     FrameJob *host[kSlots] = {};
@@ -114,14 +115,15 @@ struct rt_server {
     cudaEvent_t base_ev = nullptr;
     double base_s = 0.0;          // server clock at base_ev
     cudaStream_t copy = nullptr;
+    cudaStream_t prep = nullptr;      // frame preparation of the admitted requests
+    cudaStream_t rsv = nullptr;       // resolves of the finished requests
+    cudaEvent_t prep_ev = nullptr;    // the last preparation, before the next wave
+    cudaEvent_t wave_ev = nullptr;    // the last wave of a one-lane runner, before its resolves
     WaveRunner runner;
     Tuning tuning;                // lanes: 1 unless set (two concurrent waves served fewer rays a second)
     std::vector<SrvScene> scenes;
     std::vector<DevSlot> dslots;
-    // free frame slots, oldest freed first: a slot's image copy to the host must finish before
-    // the next request's resolve writes it, and the oldest copy is the likeliest to have
-    // finished (waiting for the copies of the slots freed last had stalled the compute stream)
-    std::deque<int> free_dslots;
+    std::deque<int> free_dslots;        // oldest freed first
     std::vector<HostSlot> hslots;
     std::deque<Request *> queue;
     std::vector<Request *> inflight;    // admission order
@@ -129,7 +131,7 @@ struct rt_server {
     std::deque<Request *> resolving;    // enqueue order
     std::unordered_map<int64_t, std::unique_ptr<Request>> reqs;
     std::vector<cudaEvent_t> ev_pool;
-    TableRing tables;
+    TableRing tables[2];                // prepare (on prep), resolve (on rsv)
     std::vector<FrameJob> to_prepare, to_resolve;   // this step's frames
     std::vector<Request *> resolved;                // requests of to_resolve
     int64_t next_id = 0;
@@ -299,13 +301,14 @@ static int admit(rt_server *srv)
     return RT_OK;
 }
 
-// one launch over this step's frames of `jobs` (prepare, or resolve), its table staged through
-// the ring
+// one launch over this step's frames of `jobs` (prepare on prep, or resolve on rsv), its table
+// staged through that stream's ring
 static int launch_frames(rt_server *srv, std::vector<FrameJob> &jobs, bool resolve)
 {
     rt_ctx *ctx = srv->ctx;
     if (jobs.empty()) return RT_OK;
-    TableRing &T = srv->tables;
+    TableRing &T = srv->tables[resolve ? 1 : 0];
+    cudaStream_t s = resolve ? srv->rsv : srv->prep;
     const int k = T.next;
     T.next = (k + 1) % TableRing::kSlots;
     if (!T.copied[k]) CK(ctx, cudaEventCreateWithFlags(&T.copied[k], cudaEventDisableTiming));
@@ -317,18 +320,18 @@ static int launch_frames(rt_server *srv, std::vector<FrameJob> &jobs, bool resol
         jobs[i].quad_end = quads;
         T.host[k][i] = jobs[i];
     }
-    CK(ctx, cudaMemcpyAsync(T.dev[k].p, T.host[k], sizeof(FrameJob) * jobs.size(), cudaMemcpyHostToDevice, ctx->stream));
-    CK(ctx, cudaEventRecord(T.copied[k], ctx->stream));
+    CK(ctx, cudaMemcpyAsync(T.dev[k].p, T.host[k], sizeof(FrameJob) * jobs.size(), cudaMemcpyHostToDevice, s));
+    CK(ctx, cudaEventRecord(T.copied[k], s));
     const FrameJob *d = (const FrameJob *)T.dev[k].p;
-    if (resolve) launch_frames_resolve(d, (int)jobs.size(), quads, ctx->stream);
-    else launch_frames_prepare(d, (int)jobs.size(), quads, ctx->stream);
+    if (resolve) launch_frames_resolve(d, (int)jobs.size(), quads, s);
+    else launch_frames_prepare(d, (int)jobs.size(), quads, s);
     CK(ctx, cudaGetLastError());
     jobs.clear();
     return RT_OK;
 }
 
-// the last chunk of r is enqueued and every wave that traced it is joined to the compute stream:
-// its resolve, copy-out and the release of its device slot follow in resolve_finished
+// the last chunk of r is enqueued and every wave that traced it is joined to the resolve stream:
+// its resolve and copy-out follow in resolve_finished
 static int finish(rt_server *srv, Request *r)
 {
     DevSlot &slot = srv->dslots[(size_t)r->dev_slot];
@@ -340,19 +343,16 @@ static int finish(rt_server *srv, Request *r)
     return RT_OK;
 }
 
-// resolve the frames finished in this step with one launch, then copy each out on the copy
-// stream; a slot is reused only after its copy (slot.copied)
+// resolve the frames finished in this step with one launch on rsv, then copy each out on the
+// copy stream; a slot is reused only after its copy (complete)
 static int resolve_finished(rt_server *srv)
 {
     rt_ctx *ctx = srv->ctx;
     if (srv->resolved.empty()) return RT_OK;
-    // the resolve writes the slots' images: the previous images must have left them (the
-    // prepare at admission writes only accumulators and axis tables, which no copy reads)
-    for (Request *r : srv->resolved) CK(ctx, cudaStreamWaitEvent(ctx->stream, srv->dslots[(size_t)r->dev_slot].copied, 0));
     int rc = launch_frames(srv, srv->to_resolve, true);
     if (rc) return rc;
     cudaEvent_t resolved = take_event(srv);
-    CK(ctx, cudaEventRecord(resolved, ctx->stream));
+    CK(ctx, cudaEventRecord(resolved, srv->rsv));
     CK(ctx, cudaStreamWaitEvent(srv->copy, resolved, 0));
     srv->ev_pool.push_back(resolved);   // re-recording later does not affect the wait above
     for (Request *r : srv->resolved) {
@@ -364,13 +364,8 @@ static int resolve_finished(rt_server *srv)
         if (srv->cfg.keep_images)
             CK(ctx, cudaMemcpyAsync(hs.rgb, slot.fb.rgb, 12 * np, cudaMemcpyDeviceToHost, srv->copy));
         CK(ctx, cudaMemcpyAsync(hs.rgb8, slot.fb.rgb8, 3 * np, cudaMemcpyDeviceToHost, srv->copy));
-        CK(ctx, cudaEventRecord(slot.copied, srv->copy));
         r->done_ev = take_event(srv);
         CK(ctx, cudaEventRecord(r->done_ev, srv->copy));
-        slot.used = false;   // reuse waits on slot.copied
-        srv->free_dslots.push_back(r->dev_slot);
-        r->dev_slot = -1;
-        srv->scenes[(size_t)r->scene].users--;
         r->state = kResolving;
         srv->resolving.push_back(r);
     }
@@ -378,8 +373,16 @@ static int resolve_finished(rt_server *srv)
     return RT_OK;
 }
 
+// r's image is in host memory: every wave, the resolve and the copy that used its frame slot
+// are done, so the slot can be prepared for another request and its scene evicted
 static void complete(rt_server *srv, Request *r, double done_s)
 {
+    if (r->dev_slot >= 0) {
+        srv->dslots[(size_t)r->dev_slot].used = false;
+        srv->free_dslots.push_back(r->dev_slot);
+        r->dev_slot = -1;
+        srv->scenes[(size_t)r->scene].users--;
+    }
     r->done_s = done_s;
     r->state = kDone;
     srv->n_completed++;
@@ -491,12 +494,12 @@ static bool stuck(const rt_server *srv)
 
 // resolve the requests the last wave finished; all_waves: no newer wave was enqueued, join every
 // lane (else every lane but the newest wave's, which runs on while they resolve). The join is
-// made in every step, requests or not, so the compute stream has always waited for each wave but
+// made in every step, requests or not, so the resolve stream has always waited for each wave but
 // the newest: a request's earlier chunks may have run in any older wave.
 static int resolve_deferred(rt_server *srv, bool all_waves)
 {
-    if (all_waves) wave_join(srv->runner, srv->ctx->stream);
-    else wave_join_all_but_last(srv->runner, srv->ctx->stream);
+    if (all_waves) wave_join(srv->runner, srv->rsv);
+    else wave_join_all_but_last(srv->runner, srv->rsv);
     if (srv->deferred.empty()) return RT_OK;
     for (Request *r : srv->deferred) {
         int rc = finish(srv, r);
@@ -536,8 +539,12 @@ static int step_batched(rt_server *srv)
         if (rc) return rc;
         wave_order(srv, order);
     }
-    rc = launch_frames(srv, srv->to_prepare, false);   // the admitted frames, before their first wave
-    if (rc) return rc;
+    if (!srv->to_prepare.empty()) {   // the admitted frames, before their first wave
+        rc = launch_frames(srv, srv->to_prepare, false);
+        if (rc) return rc;
+        CK(ctx, cudaEventRecord(srv->prep_ev, srv->prep));
+        CK(ctx, cudaStreamWaitEvent(ctx->stream, srv->prep_ev, 0));
+    }
     if (!order.empty()) {
         long long got = 0;
         rc = wave_enqueue(ctx, srv->runner, order, srv->tuning, true, ctx->stream, &got);
@@ -546,6 +553,10 @@ static int step_batched(rt_server *srv)
         rc = resolve_deferred(srv, false);
         if (rc) return rc;
         const bool one_lane = srv->runner.lanes.size() == 1;   // one stream: resolve right behind the wave
+        if (one_lane) {
+            CK(ctx, cudaEventRecord(srv->wave_ev, ctx->stream));
+            CK(ctx, cudaStreamWaitEvent(srv->rsv, srv->wave_ev, 0));
+        }
         std::vector<Request *> still;
         for (Request *r : srv->inflight) {
             if (r->wj.cursor < r->wj.total) still.push_back(r);
@@ -683,6 +694,10 @@ static int server_init(rt_server *srv)
     srv->t0 = Clock::now();
     CK(ctx, cudaSetDevice(ctx->device));
     CK(ctx, cudaStreamCreateWithFlags(&srv->copy, cudaStreamNonBlocking));
+    CK(ctx, cudaStreamCreateWithFlags(&srv->prep, cudaStreamNonBlocking));
+    CK(ctx, cudaStreamCreateWithFlags(&srv->rsv, cudaStreamNonBlocking));
+    CK(ctx, cudaEventCreateWithFlags(&srv->prep_ev, cudaEventDisableTiming));
+    CK(ctx, cudaEventCreateWithFlags(&srv->wave_ev, cudaEventDisableTiming));
     const size_t P = (size_t)c.max_pixels;
     const int n_slots = c.plain ? 1 : c.max_inflight;
     srv->dslots.resize(c.plain ? 0 : (size_t)n_slots);
@@ -699,8 +714,6 @@ static int server_init(rt_server *srv)
         d.fb.rgb = keep ? (float *)(b + o_rgb) : nullptr;
         d.fb.rgb8 = (uint8_t *)(b + o_rgb8);
         d.fb.axis = (float *)(b + o_axis);
-        CK(ctx, cudaEventCreate(&d.copied));
-        CK(ctx, cudaEventRecord(d.copied, srv->copy));
         srv->fixed_bytes += (int64_t)d.mem.bytes;
     }
     srv->hslots.resize((size_t)n_slots);
@@ -710,12 +723,13 @@ static int server_init(rt_server *srv)
         h.rgb8 = (uint8_t *)h.mem + (keep ? 12 * P : 0);
     }
     if (!c.plain) {
-        TableRing &T = srv->tables;
-        T.cap = c.max_inflight;
-        for (int k = 0; k < TableRing::kSlots; ++k) {
-            CK(ctx, cudaHostAlloc((void **)&T.host[k], sizeof(FrameJob) * (size_t)T.cap, cudaHostAllocDefault));
-            CK(ctx, T.dev[k].ensure(sizeof(FrameJob) * (size_t)T.cap));
-            srv->fixed_bytes += (int64_t)T.dev[k].bytes;
+        for (TableRing &T : srv->tables) {
+            T.cap = c.max_inflight;
+            for (int k = 0; k < TableRing::kSlots; ++k) {
+                CK(ctx, cudaHostAlloc((void **)&T.host[k], sizeof(FrameJob) * (size_t)T.cap, cudaHostAllocDefault));
+                CK(ctx, T.dev[k].ensure(sizeof(FrameJob) * (size_t)T.cap));
+                srv->fixed_bytes += (int64_t)T.dev[k].bytes;
+            }
         }
         int rc = wave_runner_init(ctx, srv->runner, c.queue_rays, c.max_inflight, c.stages, lanes);
         if (rc) return rc;
@@ -756,26 +770,29 @@ void rt_server_destroy(rt_server *srv)
     if (!srv) return;
     rt_ctx *ctx = srv->ctx;
     cudaStreamSynchronize(ctx->stream);
-    if (srv->copy) cudaStreamSynchronize(srv->copy);
+    for (cudaStream_t s : {srv->prep, srv->rsv, srv->copy})
+        if (s) cudaStreamSynchronize(s);
     wave_harvest(ctx, srv->runner, true);
     for (SrvScene &s : srv->scenes) {
         if (s.ctx_id >= 0) rt_scene_release(ctx, s.ctx_id);
         rt_scene_host_free(s.host);
     }
     for (auto &kv : srv->plain_frames) rt_frame_release(ctx, kv.second);
-    for (DevSlot &d : srv->dslots)
-        if (d.copied) cudaEventDestroy(d.copied);
     for (HostSlot &h : srv->hslots)
         if (h.mem) cudaFreeHost(h.mem);
     for (auto &kv : srv->reqs)
         if (kv.second->done_ev) cudaEventDestroy(kv.second->done_ev);
     for (cudaEvent_t e : srv->ev_pool) cudaEventDestroy(e);
-    for (int k = 0; k < TableRing::kSlots; ++k) {
-        if (srv->tables.copied[k]) cudaEventDestroy(srv->tables.copied[k]);
-        if (srv->tables.host[k]) cudaFreeHost(srv->tables.host[k]);
-    }
+    for (TableRing &T : srv->tables)
+        for (int k = 0; k < TableRing::kSlots; ++k) {
+            if (T.copied[k]) cudaEventDestroy(T.copied[k]);
+            if (T.host[k]) cudaFreeHost(T.host[k]);
+        }
     if (srv->base_ev) cudaEventDestroy(srv->base_ev);
-    if (srv->copy) cudaStreamDestroy(srv->copy);
+    for (cudaEvent_t e : {srv->prep_ev, srv->wave_ev})
+        if (e) cudaEventDestroy(e);
+    for (cudaStream_t s : {srv->prep, srv->rsv, srv->copy})
+        if (s) cudaStreamDestroy(s);
     delete srv;
 }
 
