@@ -82,6 +82,34 @@ def test_batch_split_over_many_waves_equals_plain(ctx, lanes):
             ctx.release_scene(sd)
 
 
+def test_autotune_returns_offered_values_and_the_same_images(ctx):
+    """The autotuner's choice is one of the values it offers, with the lane count stated, and a
+    batch rendered with it gives the images of the defaults bit for bit."""
+    scenes = [rt.SceneHost.config(3, i) for i in (1, 3)] + small_scenes()[:2]
+    sizes = [(128, 96), (96, 96), (80, 64), (64, 64)]
+    sids = [ctx.upload(sc) for sc in scenes]
+    fids = [ctx.frame(w, h) for w, h in sizes]
+    rds = [ctx.render_desc(w, h, 1, 3) for w, h in sizes]
+    try:
+        t = ctx.autotune(sids, fids, rds)
+        assert (t.block, t.min_blocks) in {(128, 8), (128, 6), (64, 8), (256, 0)}, t.as_dict()
+        assert t.tile in (32, 64, 128, 256) and t.dynamic in (1, 2, 3), t.as_dict()
+        assert t.stack in (0, 8) and t.pixel_tile in (0, 8, 16, 32), t.as_dict()
+        assert t.shadow_chunk in (0, 1024, 4096, 16384) and t.lanes in (1, 2), t.as_dict()
+        assert t.wave_rays in (0, 1 << 25, 1 << 27), t.as_dict()
+        images = []
+        for tuning in (None, t):
+            ctx.batch(sids, fids, rds, tuning=tuning)
+            images.append([ctx.download(f, w, h, planes=False)["rgb"] for f, (w, h) in zip(fids, sizes)])
+        for a, b in zip(*images):
+            np.testing.assert_array_equal(a.view(np.uint32), b.view(np.uint32))
+    finally:
+        for f in fids:
+            ctx.release_frame(f)
+        for sd in sids:
+            ctx.release_scene(sd)
+
+
 def test_plain_render_after_workspace_growth():
     """A render whose frame needs a larger ray workspace than the last one re-lays the
     workspace out; the cached launch graph must follow even when the new allocation comes back
