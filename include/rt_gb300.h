@@ -276,7 +276,8 @@ typedef struct rt_batch_tuning {
                                     multiple of 32 (0 = all of a bounce's hits in one chunk; the
                                     default tuning uses 4096) */
     int32_t pixel_tile;          /* primary rays traced in square pixel tiles of this edge, 0 (row by
-                                    row) or 2..64; the image does not depend on it */
+                                    row) or 2..64; the image does not depend on it (with no tuning
+                                    given, batches and batched servers use 8, plain renders 0) */
     int32_t lanes;               /* batch and server: consecutive waves go in turn to this many workspaces, each
                                     with its own stream, so one wave's kernels can use the SMs the
                                     other's leave idle while they drain: 1 or 2 (0 = 2 for a batch,
@@ -370,8 +371,10 @@ typedef struct rt_serve_stats {
 int    rt_server_create(rt_ctx *ctx, const rt_server_config *cfg, rt_server **out);
 void   rt_server_destroy(rt_server *srv);
 const char *rt_server_last_error(const rt_server *srv);
-/* kernel tuning of the server's waves (NULL = the defaults; the plain mode sets the context's
- * tuning, which its renders use); requests admitted from now on use it. Images do not depend on it.
+/* kernel tuning of the server's waves, or of the plain mode's renders (NULL = the server's
+ * defaults: one lane; primary rays in 8x8 pixel tiles, row by row in the plain mode); requests
+ * admitted from now on use it.
+ * Images do not depend on it.
  * A new lane count takes an idle server (RT_ERR_BUSY while requests are pending) and keeps the
  * queue size of a lane (RT_ERR_BUDGET when the new lanes do not fit the budget). */
 int    rt_server_set_tuning(rt_server *srv, const rt_batch_tuning *tuning);

@@ -222,6 +222,8 @@ int wave_harvest(rt_ctx *ctx, WaveRunner &R, bool wait);
 size_t wave_runner_bytes(const WaveRunner &R);
 
 constexpr size_t kPlainStageBytes = 4096;
+// primary-ray pixel tile of the wave paths (batch, batched server) when no tuning says otherwise
+constexpr int kWavePixelTile = 8;
 // workspace bytes per ray-queue entry: two ray queues (64 B each), the shadow queue (80 B) and
 // the hit queue (84 B)
 constexpr long long kWsBytesPerEntry = 292;

@@ -120,7 +120,10 @@ struct rt_server {
     cudaEvent_t prep_ev = nullptr;    // the last preparation, before the next wave
     cudaEvent_t wave_ev = nullptr;    // the last wave of a one-lane runner, before its resolves
     WaveRunner runner;
-    Tuning tuning;                // lanes: 1 unless set (two concurrent waves served fewer rays a second)
+    // lanes 1 (two concurrent waves served no more rays a second); the waves make primary rays
+    // in 8x8 pixel tiles (the served request mix traced 2.7 % faster than row by row), the plain
+    // mode row by row (its single-request renders were 3.5 % slower in tiles)
+    Tuning tuning;
     std::vector<SrvScene> scenes;
     std::vector<DevSlot> dslots;
     std::deque<int> free_dslots;        // oldest freed first
@@ -463,7 +466,10 @@ static int step_plain(rt_server *srv)
     r->rebuilt = rebuilt;
     r->state = kInflight;
     rt_render_stats st{};
+    const Tuning keep = ctx->plain_tuning;   // the render takes the server's tuning
+    ctx->plain_tuning = srv->tuning;
     rc = rt_render(ctx, sc.ctx_id, it->second, &rd);
+    ctx->plain_tuning = keep;
     if (!rc) rc = rt_render_wait(ctx, &st);
     if (rc) {
         reject(srv, r, rc);
@@ -754,6 +760,7 @@ int rt_server_create(rt_ctx *ctx, const rt_server_config *cfg, rt_server **out)
     srv->ctx = ctx;
     srv->cfg = *cfg;
     srv->tuning.lanes = 1;
+    srv->tuning.pixel_tile = cfg->plain ? 0 : kWavePixelTile;
     int rc = server_init(srv);
     if (rc) {
         std::string msg = ctx->err;
@@ -806,9 +813,12 @@ int rt_server_set_tuning(rt_server *srv, const rt_batch_tuning *tuning)
         int rc = tuning_from(srv->ctx, tuning, t);
         if (rc) return rc;
     }
-    if (!tuning || !tuning->lanes) t.lanes = 1;   // the server's default
-    // the plain mode renders through rt_render, which takes the context's tuning
-    if (srv->cfg.plain) return rt_ctx_set_tuning(srv->ctx, tuning);
+    if (!tuning) t.pixel_tile = srv->cfg.plain ? 0 : kWavePixelTile;   // the server's defaults
+    if (!tuning || !tuning->lanes) t.lanes = 1;
+    if (srv->cfg.plain) {   // its renders take the tuning one at a time; it has no wave lanes
+        srv->tuning = t;
+        return RT_OK;
+    }
     WaveRunner &R = srv->runner;
     if ((size_t)t.lanes != R.lanes.size()) {   // new lanes of the same queue size, on an idle server
         if (pending(srv) > 0) return srv_fail(srv, RT_ERR_BUSY, "lanes change with requests pending");
