@@ -243,6 +243,16 @@ def test_server_tuning_changes_no_image(ctx):
         assert e.value.code == rt.RT_ERR_BUSY
         srv.drain()
         srv.set_tuning(rt.BatchTuning(128, 32, 0, 1, 8, 1, 0, 0, 0, 2))
+    # the plain mode renders with the server's tuning, leaving the context's own as it was
+    before = ctx.tuning().as_dict()
+    with rt.Server(ctx, 8 << 30, max_inflight=4, plain=True, max_pixels=128 * 128) as srv:
+        srv.set_tuning(rt.BatchTuning(128, 32, 0, 1, 8, 1, 0, 1024, 16, 1))
+        sid = srv.add_scene(scenes[0])
+        sid_, w, h, cam, seed = mixed_requests(srv, [sid])[0]
+        rid = srv.submit(sid, w, h, cam, seed)
+        srv.drain()
+        np.testing.assert_array_equal(srv.result(rid)["rgb"].view(np.uint32), images[0][0].view(np.uint32))
+    assert ctx.tuning().as_dict() == before
 
 
 def test_server_plain_mode_matches_batched(ctx):
