@@ -251,6 +251,55 @@ def cpu_scene_sample(scenes, tiles_per_scene: int, threads: int) -> dict:
     return {"mrays_per_s": round(rays / secs / 1e6, 4), "rays": rays, "seconds": round(secs, 3), "scenes": out}
 
 
+def run_small_configs(ctx, flush, cores: int, with_cpu: bool) -> dict:
+    """Configs 0 (512^2) and 1 (1024x768, 81,920-triangle icosphere), 1 spp, depth 3: device time
+    per frame with L2 flushed between frames (both scenes fit in L2), against the CPU oracle on the
+    whole frame."""
+    import statistics
+
+    import torch
+
+    import raytrace_gb300 as rt
+    from oracle import port
+
+    out = {}
+    for cfg in (0, 1):
+        sc = rt.SceneHost.config(cfg)
+        cam = sc.desc.camera
+        w, h = cam.width, cam.height
+        sid, fid = ctx.upload(sc), ctx.frame(w, h)
+        rd = ctx.render_desc(w, h, 1, 3)
+        cnt = ctx.render(sid, fid, ctx.render_desc(w, h, 1, 3, flags=rt.RT_FLAG_COUNT_WORK))
+        for _ in range(3):
+            ctx.render(sid, fid, rd)
+        ms, rays = [], 0
+        for _ in range(20):
+            flush.fill_(1.0)
+            torch.cuda.synchronize()
+            st = ctx.render(sid, fid, rd)
+            ms.append(st.ms)
+            rays = st.total_rays()
+        med = statistics.median(ms)
+        r = {"resolution": f"{w}x{h}", "triangles": int(sc.desc.n_tris), "objects": int(sc.desc.n_objects),
+             "ms_per_frame_median": round(med, 4), "ms_per_frame_min": round(min(ms), 4),
+             "mrays_per_s": round(rays / med / 1e3, 2), "primary_mrays_per_s": round(w * h / med / 1e3, 2),
+             "rays_per_frame": {"primary": cnt.rays_primary, "secondary": cnt.rays_secondary, "shadow": cnt.rays_shadow},
+             "nodes_per_ray": round(cnt.nodes_visited / max(1, cnt.rays_primary + cnt.rays_secondary), 2),
+             "shadow_nodes_per_ray": round(cnt.shadow_nodes_visited / max(1, cnt.rays_shadow), 2),
+             "timing": "median of 20 event-timed frames after 3 warm ones, 256 MB L2 flush before each"}
+        ctx.release_frame(fid)
+        ctx.release_scene(sid)
+        if with_cpu:
+            c = port.render(sc, w, h, 1, 3, 0, ref_tiles=True, threads=cores, check=False, block=8)
+            n = int(c["counts"].sum())
+            r["cpu_baseline"] = {"value": round(n / c["seconds"] / 1e6, 4), "unit": "Mrays/s", "cores": cores,
+                                 "kind": "port", "sample": f"the whole {w}x{h} frame, {n} rays in "
+                                                           f"{c['seconds']:.3f} s wall on {cores} threads"}
+            r["gpu_over_cpu"] = round(r["mrays_per_s"] / max(r["cpu_baseline"]["value"], 1e-9), 1)
+        out[f"config{cfg}"] = r
+    return out
+
+
 def run_reference(args) -> None:
     rank, world, _ = dist_env()
     if rank != 0:
@@ -544,6 +593,7 @@ def run_gpu(args) -> None:
         + shadow_items * 80,
     }
     per_launch_bytes = alg[dominant] / max(1, kl[dominant])
+    dominant_rays = cnt.rays_shadow if dominant == "shadow" else cnt.rays_primary + cnt.rays_secondary
     per_launch_s = km[dominant] / 1e3 / max(1, kl[dominant])
     achieved = per_launch_bytes / per_launch_s / 1e9
     peak, peak_kind = measured_peaks()
@@ -562,6 +612,7 @@ def run_gpu(args) -> None:
                    "l2": "256 MB buffer written between timed steps; scene inputs (BVH 134 MB + triangles) exceed L2",
                    "rays_per_frame": {"primary": cnt.rays_primary, "secondary": cnt.rays_secondary,
                                       "shadow": cnt.rays_shadow}},
+        "primary_mrays_per_s": round(cnt.rays_primary * args.steps / dev_s / 1e6, 2),
         "e2e": {"value": round(e2e_rays / e2e_s / 1e6, 2), "unit": "Mrays/s",
                 "h2d_bytes_per_step": scene.nbytes, "d2h_bytes_per_step": W * H * 3,
                 "what": "rt_render_host: pinned scene upload + LBVH build + render + uint8 download, wall clock"},
@@ -579,6 +630,7 @@ def run_gpu(args) -> None:
                      "dram_frac": round(traffic / per_launch_s / 1e9 / peak, 4) if traffic else None,
                      "ncu": {k: v for k, v in ncu.items() if k != "traffic_bytes_per_launch"},
                      "peak_source": peak_kind, "alg_bytes_per_launch": int(per_launch_bytes),
+                     "alg_bytes_per_ray": round(alg[dominant] / max(1, dominant_rays), 1),
                      "launch_ms": round(per_launch_s * 1e3, 4)},
         "cpu_baseline": None,
         "clocks": clk.summary(),
@@ -596,6 +648,8 @@ def run_gpu(args) -> None:
         out["served"] = run_served(ctx, args.served_seconds, local)
     if world == 1 and not args.skip_batched:
         out["batched"] = run_batched(ctx, args.batched_scenes, 2)
+    if world == 1 and not args.skip_small:
+        out["small_configs"] = run_small_configs(ctx, flush, os.cpu_count() or 1, not args.skip_cpu)
     if world == 1 and not args.skip_cpu:
         cores = os.cpu_count() or 1
         s = cpu_sample(scene, CPU_SAMPLE_TILES, 0, cores)
@@ -638,6 +692,7 @@ def main() -> None:
     ap.add_argument("--skip-cpu", action="store_true", help="omit the CPU-baseline sample")
     ap.add_argument("--skip-batched", action="store_true", help="omit the config-3 batched comparison")
     ap.add_argument("--skip-served", action="store_true", help="omit the config-4 serving comparison")
+    ap.add_argument("--skip-small", action="store_true", help="omit the config-0 and config-1 frames")
     ap.add_argument("--batched-scenes", type=int, default=256)
     ap.add_argument("--served-seconds", type=float, default=60.0,
                     help="length of each Poisson stream (config 4 asks for 60 s)")
