@@ -694,9 +694,12 @@ def main() -> None:
     ap.add_argument("--skip-served", action="store_true", help="omit the config-4 serving comparison")
     ap.add_argument("--skip-small", action="store_true", help="omit the config-0 and config-1 frames")
     ap.add_argument("--batched-scenes", type=int, default=256)
-    ap.add_argument("--served-seconds", type=float, default=60.0,
-                    help="length of each Poisson stream (config 4 asks for 60 s)")
+    ap.add_argument("--served-seconds", type=float, default=None,
+                    help="length of each Poisson stream (default 60 s, as config 4 asks, on one GPU; 10 s per "
+                         "rank on several, which hold every GPU meanwhile)")
     args = ap.parse_args()
+    if args.served_seconds is None:
+        args.served_seconds = 60.0 if dist_env()[1] == 1 else 10.0
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
