@@ -200,10 +200,14 @@ int wave_enqueue(rt_ctx *ctx, WaveRunner &R, const std::vector<WaveJob *> &jobs,
                  cudaStream_t s, long long *samples_out, KernelProfiler *prof)
 {
     *samples_out = 0;
+    if (R.stages.empty() || R.lanes.empty() || !R.stages[R.next].jobs)
+        return ctx_fail(ctx, RT_ERR_INVALID, "wave runner not initialised");
     WaveStage &st = R.stages[R.next];
     int rc = stage_harvest(ctx, R, st, true);   // the ring is full: wait for its oldest wave
     if (rc) return rc;
     WaveLane &lane = R.lanes[R.next_lane];
+    if (!lane.ws.mem.p)   // a failed re-initialisation left the lane without a workspace
+        return ctx_fail(ctx, RT_ERR_INVALID, "wave lane %zu has no workspace", R.next_lane);
     const long long Q = lane.ws.qcap;
     long long used = 0, samples = 0;
     int n = 0, n_scenes = 0, max_level = 0, max_lights = 0;
