@@ -67,6 +67,19 @@ def test_gpu_matches_oracle_small(ctx, seed, n_spheres, ico, refr):
     assert not ((d > TOL) & ~a).any(), d[~a].max()
 
 
+@pytest.mark.parametrize("w,h", [(2, 2), (3, 5), (65, 2), (2, 70)])
+def test_tiny_frames_match_oracle(ctx, w, h):
+    """Frames of a few pixels, odd sizes and one-tile-wide strips: every pixel against the oracle."""
+    scene = rt.SceneHost.small(5, 6, 4, w, h, 2)
+    out, _ = gpu_render(ctx, scene, w, h, 1, 3, 5, ref_tiles=False)
+    ref = port.render(scene, w, h, 1, 3, 5, ref_tiles=False, check=True)
+    a = ref["ambiguous"]
+    ids_equal = (out["obj"] == ref["obj"]) & (out["prim"] == ref["prim"])
+    assert not (~ids_equal & ~a).any()
+    d = np.abs(out["rgb"] - ref["rgb"]).max(axis=2)
+    assert not ((d > TOL) & ~a).any(), d[~a].max()
+
+
 def _without_planes(scene: rt.SceneHost, camera: rt.Camera) -> rt.SceneHost:
     """A copy of `scene` seen through `camera`, with its planes hidden: every primitive is then
     inside the LBVH, and rays that leave the scene miss everything."""

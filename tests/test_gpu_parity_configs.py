@@ -112,6 +112,23 @@ def test_config0_full_frame_matches_oracle(ctx):
                                 "max_rgb_diff_unambiguous": float(d[~a].max())}))
 
 
+def test_largest_dropin_frame_matches_oracle(ctx):
+    """2048x2048, the largest frame the drop-in's output buffer holds (RayTracer.cpp:603): every
+    pixel against the oracle."""
+    w = h = 2048
+    scene = rt.SceneHost.small(21, 10, 6, w, h, 3)
+    sid = ctx.upload(scene)
+    fid = ctx.frame(w, h)
+    try:
+        ctx.render(sid, fid, ctx.render_desc(w, h, 1, 3, flags=rt.RT_FLAG_HIT_PLANES))
+        out = ctx.download(fid, w, h)
+    finally:
+        ctx.release_frame(fid)
+        ctx.release_scene(sid)
+    stats = oracle_compare(scene, out, w, h, 1, 3, 0, list(range((w // 64) * (h // 64))), label="2048x2048")
+    assert stats["pixels"] == w * h
+
+
 def test_config2_benchmark_frame_matches_oracle_on_row_stratified_tiles(ctx):
     """The frame bench.py times (1920x1080, 4 spp Philox jitter, depth 4, 2.1M-triangle terrain,
     64 spheres of which 16 refract, 4 lights), rendered whole on the GPU; 16 tiles, one per
