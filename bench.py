@@ -686,7 +686,8 @@ def run_gpu(args) -> None:
 def main() -> None:
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=None,
+                    help="timed steps (default 100 frames on the GPU, 20 CPU samples for --impl reference)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--skip-cpu", action="store_true", help="omit the CPU-baseline sample")
@@ -698,6 +699,8 @@ def main() -> None:
                     help="length of each Poisson stream (default 60 s, as config 4 asks, on one GPU; 10 s per "
                          "rank on several, which hold every GPU meanwhile)")
     args = ap.parse_args()
+    if args.steps is None:
+        args.steps = 20 if args.impl == "reference" else 100
     if args.served_seconds is None:
         args.served_seconds = 60.0 if dist_env()[1] == 1 else 10.0
     if args.warmup < 3:
