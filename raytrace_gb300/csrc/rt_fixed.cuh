@@ -84,6 +84,13 @@ __device__ __forceinline__ float dmul_to_float(long long x, DSplit d)
     if (x == 0) return 0.0f;
     const bool neg = x < 0;
     const unsigned long long ax = neg ? 0ull - (unsigned long long)x : (unsigned long long)x;
+    // d a power of two (the resolve scale 2^-32 / spp for a power-of-two spp) and |x| < 2^53:
+    // (double)x and the product are exact, so the value is x rounded once to float (the
+    // hardware's round-to-nearest-even conversion) times d, exact while it stays a normal float
+    if (d.m == (1ull << 52) && ax < (1ull << 53) && d.e >= -178 && d.e <= 22) {
+        const float f = __ull2float_rn(ax) * __int_as_float((d.e + 52 + 127) << 23);
+        return neg ? -f : f;
+    }
     int s0, s1, s2;
     const unsigned long long xr = round_sig(0ull, ax, 53, s0);   // (double)x
     const unsigned long long hi = __umul64hi(xr, d.m), lo = xr * d.m;

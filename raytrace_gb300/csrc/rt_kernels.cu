@@ -386,67 +386,83 @@ __global__ void k_resolve(FrameBufs fb, long long npix, DSplit scale)
         resolve_quad(fb, q, npix, scale);
 }
 
-// the frame of batch quad g: first frame whose quad_end is above g
-__device__ __forceinline__ int frame_of(const FrameJob *fj, int n, long long g)
+// A thread's indices in a batch-wide frame launch only grow, so the frame of each is found by
+// scanning forward from the frame of the last: at most n steps over the whole loop. The resolve
+// goes by quads (six 16-B loads in flight per thread keep enough bytes moving to fill HBM); the
+// preparation, which only stores, by 16-B chunks, six per quad (quad_end * 6 is a frame's chunk
+// range in the batch), so that consecutive threads write consecutive bytes.
+__device__ __forceinline__ int frame_of(const FrameJob *fj, int n, int f, long long g, int per_quad)
 {
-    int lo = 0, hi = n - 1;
-    while (lo < hi) {
-        const int mid = (lo + hi) >> 1;
-        if (fj[mid].quad_end > g) hi = mid;
-        else lo = mid + 1;
-    }
-    return lo;
+    while (f < n - 1 && per_quad * fj[f].quad_end <= g) ++f;
+    return f;
 }
 
 __global__ void k_frames_resolve(const FrameJob *fj, int n, long long quads)
 {
+    // the current frame's buffers, pixel count, scale and quad range, reloaded only when the
+    // thread's quads move on to another frame
+    int f = -1;
+    FrameBufs fb{};
+    long long npix = 0, q0 = 0, q1 = 0;
+    DSplit scale{};
     for (long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x; g < quads; g += (long long)gridDim.x * blockDim.x) {
-        const int f = frame_of(fj, n, g);
-        const FrameJob &F = fj[f];
-        const long long q = g - (f ? fj[f - 1].quad_end : 0);
-        resolve_quad(F.fb, q, F.npix, split_double_bits(F.scale_bits));
+        if (g >= q1) {
+            f = frame_of(fj, n, f < 0 ? 0 : f, g, 1);
+            const FrameJob &F = fj[f];
+            fb = F.fb;
+            npix = F.npix;
+            scale = split_double_bits(F.scale_bits);
+            q0 = f ? fj[f - 1].quad_end : 0;
+            q1 = F.quad_end;
+        }
+        resolve_quad(fb, g - q0, npix, scale);
     }
 }
 
-// quad q of a frame with nq quads: zero its accumulators, reset its hit planes, and fill the
-// axis entries q, q + nq, ... (a frame has at least W + H quads unless it is tiny)
-__device__ __forceinline__ void prepare_quad(const FrameJob &F, long long q, long long nq)
+// 16-B chunk k of a frame's accumulators (24 B per pixel; 6 chunks per 4-pixel quad, the last
+// one 8 B for an odd pixel count) zeroed; the same index k also covers pixel k's hit planes and
+// camera axis entry k (a frame has 6 * ceil(npix / 4) >= npix chunks, and >= w + h): consecutive
+// threads write consecutive bytes
+__device__ __forceinline__ void prepare_chunk(const FrameJob &F, long long k, long long nchunks)
 {
-    const long long p0 = 4 * q, p1 = min(p0 + 4, F.npix);
-    if (p1 - p0 == 4) {
-        longlong2 *a2 = reinterpret_cast<longlong2 *>(F.fb.acc + 12 * q);
-#pragma unroll
-        for (int k = 0; k < 6; ++k) a2[k] = make_longlong2(0, 0);
-    } else {
-        for (long long p = p0; p < p1; ++p) F.fb.acc[3 * p] = F.fb.acc[3 * p + 1] = F.fb.acc[3 * p + 2] = 0;
+    const long long bytes = 24 * F.npix;
+    char *a = reinterpret_cast<char *>(F.fb.acc);
+    if (16 * k + 16 <= bytes) *reinterpret_cast<longlong2 *>(a + 16 * k) = make_longlong2(0, 0);
+    else if (16 * k + 8 <= bytes) *reinterpret_cast<long long *>(a + 16 * k) = 0;
+    if (F.planes && k < F.npix) {
+        F.fb.plane_obj[k] = -1;
+        F.fb.plane_prim[k] = 0;
+        F.fb.plane_t[k] = kMiss;
     }
-    if (F.planes)
-        for (long long p = p0; p < p1; ++p) {
-            F.fb.plane_obj[p] = -1;
-            F.fb.plane_prim[p] = 0;
-            F.fb.plane_t[p] = kMiss;
-        }
     if (F.dp_bits) {   // (float)((double)xcur * dp), xcur = col - W/2, then the rows (RayTracer.cpp:14-18)
         const DSplit d = split_double_bits(F.dp_bits);
-        for (long long k = q; k < F.w + F.h; k += nq)
-            F.fb.axis[k] = dmul_to_float(k < F.w ? k - F.w / 2 : k - F.w - F.h / 2, d);
+        for (long long j = k; j < F.w + F.h; j += nchunks)
+            F.fb.axis[j] = dmul_to_float(j < F.w ? j - F.w / 2 : j - F.w - F.h / 2, d);
     }
 }
 
 __global__ void k_frames_prepare(const FrameJob *fj, int n, long long quads)
 {
-    for (long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x; g < quads; g += (long long)gridDim.x * blockDim.x) {
-        const int f = frame_of(fj, n, g);
-        const long long q0 = f ? fj[f - 1].quad_end : 0;
-        prepare_quad(fj[f], g - q0, fj[f].quad_end - q0);
+    int f = -1;
+    FrameJob F{};
+    long long c0 = 0, c1 = 0;   // the current frame's chunk range, reloaded when the chunks leave it
+    for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < 6 * quads;
+         c += (long long)gridDim.x * blockDim.x) {
+        if (c >= c1) {
+            f = frame_of(fj, n, f < 0 ? 0 : f, c, 6);
+            F = fj[f];
+            c0 = f ? 6 * fj[f - 1].quad_end : 0;
+            c1 = 6 * F.quad_end;
+        }
+        prepare_chunk(F, c - c0, c1 - c0);
     }
 }
 
 __global__ void k_frame_prepare(FrameJob F)
 {
-    const long long nq = (F.npix + 3) >> 2;
-    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += (long long)gridDim.x * blockDim.x)
-        prepare_quad(F, q, nq);
+    const long long nc = 6 * ((F.npix + 3) >> 2);
+    for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < nc; k += (long long)gridDim.x * blockDim.x)
+        prepare_chunk(F, k, nc);
 }
 
 __global__ void k_selftest_conversions(const long long *x, int n, DSplit d, const float *v, float *out_mul,
@@ -521,12 +537,16 @@ void launch_shade(const Wavefront &wf, int sel, int level, const Tuning &t, cuda
     }
 }
 
+// grid of a frame launch over n items: 256 threads a block, at most 8 blocks per SM (grid stride)
+static int item_grid(long long n)
+{
+    return (int)std::max<long long>(1, std::min<long long>((n + 255) / 256, (long long)sm_count() * 8));
+}
+
 void launch_resolve(const FrameBufs &fb, int width, int height, int spp, cudaStream_t s)
 {
-    long long npix = (long long)width * height;
-    int grid = (int)std::min<long long>(((npix + 3) / 4 + 255) / 256, (long long)sm_count() * 8);
-    if (grid < 1) grid = 1;
-    k_resolve<<<grid, 256, 0, s>>>(fb, npix, split_double_bits(resolve_scale_bits(spp)));
+    const long long npix = (long long)width * height;
+    k_resolve<<<item_grid((npix + 3) / 4), 256, 0, s>>>(fb, npix, split_double_bits(resolve_scale_bits(spp)));
 }
 
 unsigned long long resolve_scale_bits(int spp)
@@ -537,24 +557,19 @@ unsigned long long resolve_scale_bits(int spp)
     return bits;
 }
 
-static int quad_grid(long long quads)
-{
-    return (int)std::max<long long>(1, std::min<long long>((quads + 255) / 256, (long long)sm_count() * 8));
-}
-
 void launch_frames_prepare(const FrameJob *jobs, int n, long long quads, cudaStream_t s)
 {
-    if (n > 0 && quads > 0) k_frames_prepare<<<quad_grid(quads), 256, 0, s>>>(jobs, n, quads);
+    if (n > 0 && quads > 0) k_frames_prepare<<<item_grid(6 * quads), 256, 0, s>>>(jobs, n, quads);
 }
 
 void launch_frame_prepare(const FrameJob &job, cudaStream_t s)
 {
-    k_frame_prepare<<<quad_grid((job.npix + 3) / 4), 256, 0, s>>>(job);
+    k_frame_prepare<<<item_grid(6 * ((job.npix + 3) / 4)), 256, 0, s>>>(job);
 }
 
 void launch_frames_resolve(const FrameJob *jobs, int n, long long quads, cudaStream_t s)
 {
-    if (n > 0 && quads > 0) k_frames_resolve<<<quad_grid(quads), 256, 0, s>>>(jobs, n, quads);
+    if (n > 0 && quads > 0) k_frames_resolve<<<item_grid(quads), 256, 0, s>>>(jobs, n, quads);
 }
 
 

@@ -18,8 +18,9 @@ struct FrameBufs {
                         // W columns, then (float)((double)ycur * dp) for the H rows
 };
 
-// one frame of a batch, for the batch-wide prepare and resolve launches. Pixels go in groups
-// of four (quads); the frame's quads are [quad_end of the previous frame, quad_end).
+// one frame of a batch, for the batch-wide prepare and resolve launches. Pixels are counted in
+// groups of four (quads); the frame's quads are [quad_end of the previous frame, quad_end). The
+// resolve gives each quad a thread, the preparation six, one per 16 B of its 96 B of accumulators.
 struct FrameJob {
     FrameBufs fb;
     long long npix;

@@ -394,3 +394,13 @@ def test_server_multi_sample_requests_equal_plain_renders(ctx):
         ref = plain_render(ctx, scenes[sid], w, h, camera=cam, spp=4, level=4, seed=seed)
         assert np.array_equal(ref["rgb"], g)
 
+
+
+def test_cli_serves_a_short_stream():
+    """The CLI's serving mode: a short Poisson stream over a few config-4 scenes completes every
+    request."""
+    from raytrace_gb300 import cli
+
+    st = cli.serve(200.0, 0.25, 4, 16, False, slots=32)
+    assert st["requests"] > 0 and st["completed"] == st["requests"] and st["rejected"] == 0, st
+    assert st["p99_ms"] >= st["p50_ms"] > 0, st
