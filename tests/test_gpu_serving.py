@@ -57,6 +57,35 @@ def test_batch_equals_plain_renders(ctx):
             ctx.release_scene(s)
 
 
+def test_batch_of_odd_sized_frames_equals_plain(ctx):
+    """Frames whose pixel counts are not multiples of four (a partial last quad, an 8-B tail of
+    accumulators) and frames of a few pixels, batched with others and with hit planes: each is
+    its plain render, colour and planes alike."""
+    scenes = small_scenes()[:3]
+    sizes = [(3, 5), (7, 3), (65, 2), (33, 17), (2, 2), (31, 29), (96, 64)]
+    sids = [ctx.upload(scenes[k % 3]) for k in range(len(sizes))]
+    fids = [ctx.frame(w, h) for w, h in sizes]
+    rds = [ctx.render_desc(w, h, 1, 3, flags=rt.RT_FLAG_HIT_PLANES) for w, h in sizes]
+    try:
+        ctx.batch(sids, fids, rds)
+        got = [ctx.download(f, w, h) for f, (w, h) in zip(fids, sizes)]
+        for k, (w, h) in enumerate(sizes):
+            sid1, fid1 = ctx.upload(scenes[k % 3]), ctx.frame(w, h)
+            try:
+                ctx.render(sid1, fid1, rds[k])
+                ref = ctx.download(fid1, w, h)
+            finally:
+                ctx.release_frame(fid1)
+                ctx.release_scene(sid1)
+            for key in ("rgb", "rgb8", "obj", "prim", "t"):
+                np.testing.assert_array_equal(got[k][key].view(np.uint8), ref[key].view(np.uint8), err_msg=f"{key} {w}x{h}")
+    finally:
+        for f in fids:
+            ctx.release_frame(f)
+        for sd in sids:
+            ctx.release_scene(sd)
+
+
 @pytest.mark.parametrize("lanes", [1, 2])
 def test_batch_split_over_many_waves_equals_plain(ctx, lanes):
     """Queues of 2^14 entries cut the batch into dozens of waves; with two lanes consecutive
