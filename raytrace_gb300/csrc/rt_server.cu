@@ -119,6 +119,10 @@ struct rt_server {
     cudaStream_t rsv = nullptr;       // resolves of the finished requests
     cudaEvent_t prep_ev = nullptr;    // the last preparation, before the next wave
     cudaEvent_t wave_ev = nullptr;    // the last wave of a one-lane runner, before its resolves
+    cudaEvent_t solo_ev = nullptr;    // the last frame launch of a solo step, before the side streams
+    // solo step: nothing else was in flight, so the step's preparation, wave, resolve and copies go
+    // on the wave stream itself, without the hops between streams (a lone request's latency)
+    bool solo = false;
     WaveRunner runner;
     // lanes 1 (two concurrent waves served no more rays a second); the waves make primary rays
     // in 8x8 pixel tiles (the served request mix traced 2.7 % faster than row by row), the plain
@@ -311,7 +315,7 @@ static int launch_frames(rt_server *srv, std::vector<FrameJob> &jobs, bool resol
     rt_ctx *ctx = srv->ctx;
     if (jobs.empty()) return RT_OK;
     TableRing &T = srv->tables[resolve ? 1 : 0];
-    cudaStream_t s = resolve ? srv->rsv : srv->prep;
+    cudaStream_t s = srv->solo ? ctx->stream : resolve ? srv->rsv : srv->prep;
     const int k = T.next;
     T.next = (k + 1) % TableRing::kSlots;
     if (!T.copied[k]) CK(ctx, cudaEventCreateWithFlags(&T.copied[k], cudaEventDisableTiming));
@@ -329,6 +333,10 @@ static int launch_frames(rt_server *srv, std::vector<FrameJob> &jobs, bool resol
     if (resolve) launch_frames_resolve(d, (int)jobs.size(), quads, s);
     else launch_frames_prepare(d, (int)jobs.size(), quads, s);
     CK(ctx, cudaGetLastError());
+    if (srv->solo) {   // the side stream's next use of this ring follows the launch
+        CK(ctx, cudaEventRecord(srv->solo_ev, s));
+        CK(ctx, cudaStreamWaitEvent(resolve ? srv->rsv : srv->prep, srv->solo_ev, 0));
+    }
     jobs.clear();
     return RT_OK;
 }
@@ -354,10 +362,13 @@ static int resolve_finished(rt_server *srv)
     if (srv->resolved.empty()) return RT_OK;
     int rc = launch_frames(srv, srv->to_resolve, true);
     if (rc) return rc;
-    cudaEvent_t resolved = take_event(srv);
-    CK(ctx, cudaEventRecord(resolved, srv->rsv));
-    CK(ctx, cudaStreamWaitEvent(srv->copy, resolved, 0));
-    srv->ev_pool.push_back(resolved);   // re-recording later does not affect the wait above
+    const cudaStream_t copy = srv->solo ? ctx->stream : srv->copy;
+    if (!srv->solo) {
+        cudaEvent_t resolved = take_event(srv);
+        CK(ctx, cudaEventRecord(resolved, srv->rsv));
+        CK(ctx, cudaStreamWaitEvent(copy, resolved, 0));
+        srv->ev_pool.push_back(resolved);   // re-recording later does not affect the wait above
+    }
     for (Request *r : srv->resolved) {
         DevSlot &slot = srv->dslots[(size_t)r->dev_slot];
         HostSlot &hs = srv->hslots[(size_t)r->host_slot];
@@ -365,10 +376,10 @@ static int resolve_finished(rt_server *srv)
         // the frame a client receives is the uint8 image (Color::put); float colour only when
         // the server keeps images for inspection
         if (srv->cfg.keep_images)
-            CK(ctx, cudaMemcpyAsync(hs.rgb, slot.fb.rgb, 12 * np, cudaMemcpyDeviceToHost, srv->copy));
-        CK(ctx, cudaMemcpyAsync(hs.rgb8, slot.fb.rgb8, 3 * np, cudaMemcpyDeviceToHost, srv->copy));
+            CK(ctx, cudaMemcpyAsync(hs.rgb, slot.fb.rgb, 12 * np, cudaMemcpyDeviceToHost, copy));
+        CK(ctx, cudaMemcpyAsync(hs.rgb8, slot.fb.rgb8, 3 * np, cudaMemcpyDeviceToHost, copy));
         r->done_ev = take_event(srv);
-        CK(ctx, cudaEventRecord(r->done_ev, srv->copy));
+        CK(ctx, cudaEventRecord(r->done_ev, copy));
         r->state = kResolving;
         srv->resolving.push_back(r);
     }
@@ -528,12 +539,15 @@ static void wave_order(const rt_server *srv, std::vector<WaveJob *> &order)
 static int step_batched(rt_server *srv)
 {
     rt_ctx *ctx = srv->ctx;
+    srv->solo = false;
     int rc = retire(srv, false);
     if (rc) return rc;
+    const bool idle = srv->inflight.empty() && srv->deferred.empty() && srv->resolving.empty();
     rc = admit(srv);
     if (rc) return rc;
     std::vector<WaveJob *> order;
     wave_order(srv, order);
+    srv->solo = idle && srv->runner.lanes.size() == 1 && !order.empty();
     if (order.empty()) {   // no wave to enqueue: the last wave's requests resolve now
         rc = resolve_deferred(srv, true);
         if (rc) return rc;
@@ -548,8 +562,10 @@ static int step_batched(rt_server *srv)
     if (!srv->to_prepare.empty()) {   // the admitted frames, before their first wave
         rc = launch_frames(srv, srv->to_prepare, false);
         if (rc) return rc;
-        CK(ctx, cudaEventRecord(srv->prep_ev, srv->prep));
-        CK(ctx, cudaStreamWaitEvent(ctx->stream, srv->prep_ev, 0));
+        if (!srv->solo) {
+            CK(ctx, cudaEventRecord(srv->prep_ev, srv->prep));
+            CK(ctx, cudaStreamWaitEvent(ctx->stream, srv->prep_ev, 0));
+        }
     }
     if (!order.empty()) {
         long long got = 0;
@@ -559,7 +575,7 @@ static int step_batched(rt_server *srv)
         rc = resolve_deferred(srv, false);
         if (rc) return rc;
         const bool one_lane = srv->runner.lanes.size() == 1;   // one stream: resolve right behind the wave
-        if (one_lane) {
+        if (one_lane && !srv->solo) {
             CK(ctx, cudaEventRecord(srv->wave_ev, ctx->stream));
             CK(ctx, cudaStreamWaitEvent(srv->rsv, srv->wave_ev, 0));
         }
@@ -704,6 +720,7 @@ static int server_init(rt_server *srv)
     CK(ctx, cudaStreamCreateWithFlags(&srv->rsv, cudaStreamNonBlocking));
     CK(ctx, cudaEventCreateWithFlags(&srv->prep_ev, cudaEventDisableTiming));
     CK(ctx, cudaEventCreateWithFlags(&srv->wave_ev, cudaEventDisableTiming));
+    CK(ctx, cudaEventCreateWithFlags(&srv->solo_ev, cudaEventDisableTiming));
     const size_t P = (size_t)c.max_pixels;
     const int n_slots = c.plain ? 1 : c.max_inflight;
     srv->dslots.resize(c.plain ? 0 : (size_t)n_slots);
@@ -796,7 +813,7 @@ void rt_server_destroy(rt_server *srv)
             if (T.host[k]) cudaFreeHost(T.host[k]);
         }
     if (srv->base_ev) cudaEventDestroy(srv->base_ev);
-    for (cudaEvent_t e : {srv->prep_ev, srv->wave_ev})
+    for (cudaEvent_t e : {srv->prep_ev, srv->wave_ev, srv->solo_ev})
         if (e) cudaEventDestroy(e);
     for (cudaStream_t s : {srv->prep, srv->rsv, srv->copy})
         if (s) cudaStreamDestroy(s);
