@@ -372,8 +372,8 @@ int    rt_server_create(rt_ctx *ctx, const rt_server_config *cfg, rt_server **ou
 void   rt_server_destroy(rt_server *srv);
 const char *rt_server_last_error(const rt_server *srv);
 /* kernel tuning of the server's waves, or of the plain mode's renders (NULL = the server's
- * defaults: one lane; primary rays in 8x8 pixel tiles, row by row in the plain mode); requests
- * admitted from now on use it.
+ * defaults: one lane; primary rays in 8x8 pixel tiles, but row by row in the plain mode and for
+ * requests admitted into an idle server); requests admitted from now on use it.
  * Images do not depend on it.
  * A new lane count takes an idle server (RT_ERR_BUSY while requests are pending) and keeps the
  * queue size of a lane (RT_ERR_BUDGET when the new lanes do not fit the budget). */

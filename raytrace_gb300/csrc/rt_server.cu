@@ -123,6 +123,9 @@ struct rt_server {
     // solo step: nothing else was in flight, so the step's preparation, wave, resolve and copies go
     // on the wave stream itself, without the hops between streams (a lone request's latency)
     bool solo = false;
+    // the pixel tile is the default's: requests admitted into an idle server trace row by row (a
+    // lone request's render was 3.5 % slower in tiles; waves of many requests are faster in them)
+    bool default_tile = true;
     WaveRunner runner;
     // lanes 1 (two concurrent waves served no more rays a second); the waves make primary rays
     // in 8x8 pixel tiles (the served request mix traced 2.7 % faster than row by row), the plain
@@ -255,7 +258,7 @@ static void reject(rt_server *srv, Request *r, int status)
 }
 
 // admit queued requests in arrival order
-static int admit(rt_server *srv)
+static int admit(rt_server *srv, bool idle)
 {
     rt_ctx *ctx = srv->ctx;
     while (!srv->queue.empty()) {
@@ -287,7 +290,7 @@ static int admit(rt_server *srv)
             reject(srv, r, rc);
             continue;
         }
-        r->wj.job.pixel_tile = srv->tuning.pixel_tile;
+        r->wj.job.pixel_tile = idle && srv->default_tile ? 0 : srv->tuning.pixel_tile;
         r->wj.scene = &sd;
         r->wj.total = samples;
         r->wj.cursor = 0;
@@ -543,7 +546,7 @@ static int step_batched(rt_server *srv)
     int rc = retire(srv, false);
     if (rc) return rc;
     const bool idle = srv->inflight.empty() && srv->deferred.empty() && srv->resolving.empty();
-    rc = admit(srv);
+    rc = admit(srv, idle);
     if (rc) return rc;
     std::vector<WaveJob *> order;
     wave_order(srv, order);
@@ -555,7 +558,7 @@ static int step_batched(rt_server *srv)
     if (order.empty() && !srv->resolving.empty()) {
         rc = retire(srv, true);
         if (rc) return rc;
-        rc = admit(srv);
+        rc = admit(srv, false);
         if (rc) return rc;
         wave_order(srv, order);
     }
@@ -832,6 +835,7 @@ int rt_server_set_tuning(rt_server *srv, const rt_batch_tuning *tuning)
     }
     if (!tuning) t.pixel_tile = srv->cfg.plain ? 0 : kWavePixelTile;   // the server's defaults
     if (!tuning || !tuning->lanes) t.lanes = 1;
+    srv->default_tile = !tuning;
     if (srv->cfg.plain) {   // its renders take the tuning one at a time; it has no wave lanes
         srv->tuning = t;
         return RT_OK;
